@@ -1,0 +1,305 @@
+"""Benchmark: the gate-engine microbenchmark (28-qubit FP64 state, 1000 random
+gates, a measurement every 100 gates) on one GB300, through libsq.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl own|reference]
+
+A step applies the whole 1000-gate circuit to the resident state.  `value` is
+the algorithmic gate bandwidth: the sum over gates of 2*B*N*f (B = 16 bytes per
+FP64 amplitude, f = fraction of amplitudes the gate must touch) divided by the
+device time of the step, so fused passes can exceed the HBM peak; `roofline`
+reports the bytes the executed passes really moved.  `e2e` repeats the step
+through the public API with the state copied in from, and out to, page-locked
+host memory inside the timed region.  The state (4 GiB) is larger than L2, so
+no flush is needed between steps.  N > 1 runs independent replicas (one state
+per GPU; the path has no exchange step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "gate HBM GB/s (gate-engine microbenchmark)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="own", choices=["own", "reference"])
+    ap.add_argument("--n", type=int, default=28)
+    ap.add_argument("--gates", type=int, default=1000)
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--no-fusion", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--skip-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx),
+                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[2:]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(n, gates, seconds, bytes_per_amp):
+    """The CPU oracle (a restatement of the reference's dense CPU loops, pinned
+    bit-exact to it) on this host's cores, over a time-bounded prefix of the same
+    circuit.  Returns (GB/s, gates timed, threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle
+    from suqa_gb300.workloads import algorithmic_bytes, random_state
+    threads = os.cpu_count() or 1
+    L = oracle.load()
+    L.or_set_threads(threads)
+    ost = oracle.OracleState(n)
+    re, im = random_state(n, 7)
+    N = 1 << n
+    buf = np.ctypeslib.as_array(ost.p.contents.data, shape=(2 * N,))
+    buf[:N] = re
+    buf[N:] = im
+    done = 0
+    t0 = time.perf_counter()
+    while done < len(gates) and time.perf_counter() - t0 < seconds:
+        oracle.apply_circuit(ost, gates[done:done + 1])
+        done += 1
+    dt = time.perf_counter() - t0
+    L.or_set_threads(1)
+    ost.close()
+    alg = algorithmic_bytes(gates[:done], n, bytes_per_amp)
+    return alg / dt / 1e9, done, threads, dt
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    from suqa_gb300.workloads import random_circuit
+    bpa = 16 if args.precision == "f64" else 8
+    gates = random_circuit(args.n, args.gates, seed=7)
+    vals = []
+    sample = None
+    for i in range(args.warmup + args.steps):
+        v, done, threads, dt = cpu_baseline(args.n, gates, args.cpu_seconds, bpa)
+        sample = f"first {done} of {len(gates)} ops of the {args.n}-qubit circuit, {dt:.1f} s"
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
+            "dtype": args.precision, "data": "synthetic",
+            "config": {"workload": f"random circuit, {args.n} qubits {args.precision.upper()}, "
+                                   f"{args.gates} gates, measure every 100", "n_qubits": args.n},
+            "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        return
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from suqa_gb300 import State
+    from suqa_gb300.workloads import algorithmic_bytes, apply_circuit, random_circuit, random_state
+
+    n = args.n
+    bpa = 16 if args.precision == "f64" else 8
+    dt_np = np.float64 if args.precision == "f64" else np.float32
+    gates = random_circuit(n, args.gates, seed=7)
+    alg = algorithmic_bytes(gates, n, bpa)
+    stream = torch.cuda.current_stream()
+    st = State(n, args.precision)
+    st.set_stream(stream.cuda_stream)
+    st.set_fusion(not args.no_fusion)
+    re, im = random_state(n, 7, dt_np)
+    h_re = torch.from_numpy(re).pin_memory()
+    h_im = torch.from_numpy(im).pin_memory()
+    o_re = torch.empty_like(h_re).pin_memory()
+    o_im = torch.empty_like(h_im).pin_memory()
+    del re, im
+    st.upload(h_re.data_ptr(), h_im.data_ptr())
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident: K steps of the circuit on the resident state
+    for _ in range(args.warmup):
+        apply_circuit(st, gates)
+    st.flush()
+    barrier()
+    st.reset_stats()
+    st.set_timing(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            apply_circuit(st, gates)
+        st.flush()
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1)
+    kms, klaunch, kbytes = st.kernel_time()
+    st.set_timing(False)
+    stats = st.stats()
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = alg * world / (ms_step / 1e3) / 1e9
+
+    # ---- end to end: host state in, circuit, host state out, per step
+    for _ in range(1):
+        st.upload(h_re.data_ptr(), h_im.data_ptr())
+        apply_circuit(st, gates)
+        st.download(o_re.data_ptr(), o_im.data_ptr())
+    barrier()
+    t0 = time.perf_counter()
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    bits_all = []
+    for _ in range(args.steps):
+        st.upload(h_re.data_ptr(), h_im.data_ptr())
+        bits_all.append(apply_circuit(st, gates))
+        st.download(o_re.data_ptr(), o_im.data_ptr())
+    e3.record(stream)
+    barrier()
+    ms_e2e = e2.elapsed_time(e3) / args.steps
+    e2e_value = alg * world / (ms_e2e / 1e3) / 1e9
+    state_bytes = (1 << n) * bpa
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = kbytes / (kms / 1e3) / 1e9 if kms > 0 else None
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None,
+                "traffic": traffic_per_launch(),
+                "kernel": "sqk::k_pass<%s>" % ("double" if args.precision == "f64" else "float"),
+                "launches": klaunch, "avg_launch_ms": kms / klaunch if klaunch else None,
+                "bytes_per_launch": kbytes / klaunch if klaunch else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"}
+
+    if rank == 0:
+        cpu = None
+        if not args.skip_cpu:
+            v, done, threads, dt = cpu_baseline(n, gates, args.cpu_seconds, bpa)
+            cpu = {"value": v, "unit": "GB/s", "cores": threads, "kind": "port",
+                   "sample": f"first {done} of {len(gates)} ops of the same {n}-qubit circuit, {dt:.1f} s"}
+        line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": args.precision, "data": "synthetic",
+                "config": {"workload": f"random circuit, {n} qubits {args.precision.upper()}, {args.gates} gates "
+                                       f"(X, H, CX, MCX 2-4 controls, U1, Pauli rotations on 2-6 qubits), "
+                                       f"measure every 100; seed 7",
+                           "n_qubits": n, "gates": args.gates, "fusion": not args.no_fusion,
+                           "parallelism": f"replicas x{world}", "l2": "state (%d MiB) larger than L2" % (2 * state_bytes >> 20)},
+                "gates_per_s": (len([g for g in gates if g[0] != 'measure']) * world) / (ms_step / 1e3),
+                "passes_per_step": stats["passes"] / args.steps,
+                "gpu_launches": stats["launches"],
+                "clocks": clk.summary(),
+                "e2e": {"value": e2e_value, "unit": "GB/s", "ms_per_step": ms_e2e,
+                        "h2d_bytes_per_step": 2 * state_bytes, "d2h_bytes_per_step": 2 * state_bytes},
+                "roofline": roofline,
+                "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    st.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def traffic_per_launch():
+    """DRAM bytes per launch of the pass kernel from the committed ncu summary
+    (profiles/k_pass_f64_n28.txt, line 'traffic_per_launch_bytes: X'), if any."""
+    p = os.path.join(ROOT, "profiles", "k_pass_f64_n28.txt")
+    try:
+        for ln in open(p):
+            if ln.startswith("traffic_per_launch_bytes:"):
+                return float(ln.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+if __name__ == "__main__":
+    main()

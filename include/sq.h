@@ -1,0 +1,141 @@
+/* libsq — C ABI of the GB300 (sm_103a) state-vector engine.
+ *
+ * Drop-in boundary for the gate engine of SUQA: every entry point below
+ * replaces one function of the reference's suqa:: API (include/suqa.cuh:94-176,
+ * implemented in src/suqa.cu) or of the QMS algorithm header
+ * (include/qms.cuh), as cited beside it.  The C++ header-compatible shim in
+ * suqa_gb300/include/ re-exports the exact suqa:: names on top of this ABI.
+ *
+ * Conventions
+ *  - Plain C types only.  Qubit masks are 64-bit; a state holds n <= 33 qubits.
+ *  - Layout: one device allocation of 2*2^n elements, re block then im block,
+ *    as the reference ComplexVec (include/complex_defines.cuh:22-45).
+ *    Elements are double (SQ_F64) or float (SQ_F32).
+ *  - Every call returns SQ_OK (0) or an error code; sq_last_error() gives text.
+ *  - Gates are queued and applied lazily: consecutive gates are fused into as
+ *    few passes over the state as their qubits allow.  Any call that observes
+ *    the state (measure, prob_filter, vnorm, get_state, state_ptrs) first applies
+ *    everything queued.  sq_flush() forces it.
+ *  - Trigonometric and exponential coefficients are computed on the host in
+ *    double precision, as the reference does (src/suqa.cu:274, include/qms.cuh:232).
+ *  - One state is used by one host thread at a time; calls are stream-ordered
+ *    on the state's stream.
+ */
+#ifndef SQ_H
+#define SQ_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sq_state sq_state;
+
+enum {
+    SQ_OK = 0,
+    SQ_ERR_ARG = 1,         /* invalid argument (qubit out of range, overlap, size) */
+    SQ_ERR_CUDA = 2,        /* CUDA runtime error */
+    SQ_ERR_UNSUPPORTED = 3, /* pattern the reference rejects (Pauli string, phase list) */
+    SQ_ERR_NOMEM = 4,       /* device or host allocation failed */
+    SQ_ERR_NODEVICE = 5     /* no usable CUDA device */
+};
+
+enum { SQ_F64 = 0, SQ_F32 = 1 };
+
+/* Pauli rotation flags */
+enum {
+    SQ_PAULI_EXACT = 0,     /* exp(i phase P) for any Pauli string */
+    SQ_PAULI_REFERENCE = 1  /* reference semantics: only its supported patterns
+                               (1 qubit, 2 qubits, Z(x)A(x)A; others -> SQ_ERR_UNSUPPORTED),
+                               and its two-qubit X/Y case as exp(i phase Y(x)X) */
+};
+
+const char* sq_last_error(void);
+const char* sq_version(void);
+
+/* --- state lifecycle: src/suqa.cu:760-866 (allocate_state, setup, clear) --- */
+/* Allocates 2^n amplitudes in the given precision and sets |0...0>. */
+int sq_state_create(sq_state** out, uint32_t n, int precision);
+int sq_state_destroy(sq_state* s);
+/* Device pointers of the re and im blocks (data_re/data_im of the reference
+ * ComplexVec); applies queued gates first. */
+int sq_state_ptrs(sq_state* s, void** data_re, void** data_im);
+int sq_state_nqubits(const sq_state* s, uint32_t* n, int* precision);
+/* Use a caller's CUDA stream (cudaStream_t) for all later work; NULL = the state's own. */
+int sq_set_stream(sq_state* s, void* cuda_stream);
+int sq_flush(sq_state* s);
+int sq_synchronize(sq_state* s);
+/* Host <-> device copies of the whole state as doubles (FP32 states convert). */
+int sq_get_state(sq_state* s, double* re, double* im);
+int sq_set_state(sq_state* s, const double* re, const double* im);
+/* Raw copies in the state's own element type (double for SQ_F64, float for
+ * SQ_F32); with page-locked host buffers these run at full link bandwidth and
+ * are stream-ordered (sq_download returns after the copy completed). */
+int sq_upload(sq_state* s, const void* host_re, const void* host_im);
+int sq_download(sq_state* s, void* host_re, void* host_im);
+/* Gate fusion on/off (default on); off applies every gate as its own pass. */
+int sq_set_fusion(sq_state* s, int enabled);
+
+/* --- state utilities: src/suqa.cu:70-111 --- */
+int sq_init_state(sq_state* s);                   /* suqa::init_state */
+int sq_vnorm(sq_state* s, double* norm);          /* suqa::vnorm */
+int sq_vnormalize(sq_state* s);                   /* suqa::vnormalize (multiply by 1./norm) */
+
+/* --- gates; gc = the global control mask (suqa::gc_mask, src/suqa.cu:36) --- */
+int sq_apply_x(sq_state* s, uint32_t q, uint64_t gc);      /* suqa::apply_x, src/suqa.cu:115 */
+int sq_apply_y(sq_state* s, uint32_t q, uint64_t gc);      /* suqa::apply_y, src/suqa.cu:136 */
+int sq_apply_h(sq_state* s, uint32_t q, uint64_t gc);      /* suqa::apply_h, src/suqa.cu:207 */
+/* suqa::apply_u1(q, q_mask, phase), src/suqa.cu:271: phase on the |q_mask> branch of q */
+int sq_apply_u1(sq_state* s, uint32_t q, uint32_t q_mask, double phase, uint64_t gc);
+/* multi-controlled X with per-control polarity, masks as the reference builds
+ * them (src/suqa.cu:289-344): flips q_target where (i & control_mask) == mask_qs
+ * (control_mask/mask_qs include gc; the target bit is added internally) */
+int sq_apply_mcx(sq_state* s, uint64_t control_mask, uint64_t mask_qs, uint32_t q_target);
+/* controlled phase, src/suqa.cu:346-393: phase where (i & control_mask) == mask_qs */
+int sq_apply_mcu1(sq_state* s, uint64_t control_mask, uint64_t mask_qs, double phase);
+int sq_apply_swap(sq_state* s, uint32_t q1, uint32_t q2, uint64_t gc);  /* src/suqa.cu:396 */
+/* suqa::apply_phase_list, src/suqa.cu:418-455 (the reference's GPU-only API): 2^q_size
+ * phases on qubits q0..q0+q_size-1; keeps the reference's guard (i & gc) != 0,
+ * so it is a no-op when gc == 0.  q_size in 1..7. */
+int sq_apply_phase_list(sq_state* s, uint32_t q0, uint32_t q_size, const double* phases, uint64_t gc);
+/* suqa::apply_pauli_TP_rotation, src/suqa.cu:467-604: exp(i phase P),
+ * P = (x)_k paulis[k] on qubits[k], paulis 1=X 2=Y 3=Z; k in 1..32 */
+int sq_apply_pauli_rotation(sq_state* s, uint32_t k, const uint32_t* qubits, const uint32_t* paulis,
+                            double phase, uint64_t gc, int flags);
+
+/* --- measurement: src/suqa.cu:673-727 --- */
+/* p1 = sum |a_i|^2 over bit q set; c = (r < p1); zero the other branch; rescale
+ * the kept one by 1/sqrt(p_c) */
+int sq_measure_qbit(sq_state* s, uint32_t q, double r, uint32_t* c);
+/* sum |a_i|^2 over (i & mask_qs) == mask */
+int sq_prob_filter(sq_state* s, uint64_t mask_qs, uint64_t mask, double* prob);
+
+/* --- QMS acceptance oracle W: include/qms.cuh:220-329 --- */
+/* Rotation on the acceptance qubit q_acc (pairs i with bit q_acc set and
+ * i without it) with f1 = exp(-dE/2), f2 = sqrt(1-f1^2) for dE > 0 (else 1, 0),
+ * dE = Enew*c - E_old*c, Enew = (i & mask_enew) >> shift.  Like the reference,
+ * it ignores the global control mask.  (mask_enew >> shift) < 128. */
+int sq_apply_qms_w(sq_state* s, uint32_t q_acc, uint64_t mask_enew, uint32_t shift,
+                   uint32_t E_old, double c_factor);
+
+/* --- counters (gate-cost reporting) --- */
+typedef struct sq_stats {
+    uint64_t gates;        /* gates queued */
+    uint64_t passes;       /* passes over the state executed */
+    uint64_t launches;     /* kernel launches */
+    uint64_t reductions;   /* measurement / filter reductions */
+    uint64_t bytes_moved;  /* bytes read + written by executed passes (algorithmic) */
+} sq_stats;
+int sq_get_stats(const sq_state* s, sq_stats* out);
+int sq_reset_stats(sq_state* s);
+/* Kernel timing: when enabled, every pass launch is bracketed by CUDA events on
+ * the state's stream; sq_kernel_time() synchronizes and returns the summed
+ * device time (ms), the launch count and the bytes those launches moved since
+ * the last call (then clears them). */
+int sq_set_timing(sq_state* s, int enabled);
+int sq_kernel_time(sq_state* s, double* ms, uint64_t* launches, uint64_t* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SQ_H */

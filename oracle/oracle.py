@@ -320,3 +320,27 @@ class Pcg32:
 
     def doub(self) -> float:
         return float(self.L.or_pcg_doub(C.byref(self.g)))
+
+
+def apply_circuit(ost: "OracleState", gates):
+    """Applies a benchmark circuit (suqa_gb300.workloads.random_circuit form) on the
+    oracle; used only for CPU-baseline timing."""
+    L = load()
+    p = ost.p
+    for g in gates:
+        k = g[0]
+        if k == "x":
+            L.or_apply_x(p, g[1], 0)
+        elif k == "h":
+            L.or_apply_h(p, g[1], 0)
+        elif k == "cx":
+            L.or_apply_mcx(p, 1 << g[1], 1 << g[1], g[2])
+        elif k == "mcx":
+            m = sum(1 << q for q in g[1])
+            L.or_apply_mcx(p, m, m, g[2])
+        elif k == "u1":
+            L.or_apply_u1(p, g[1], 1, g[2], 0)
+        elif k == "ptp":
+            L.or_apply_pauli(p, len(g[1]), _u32arr(g[1]), _u32arr(g[2]), g[3], 0, 0)
+        elif k == "measure":
+            L.or_measure_qbit(p, g[1], g[2])

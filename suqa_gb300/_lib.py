@@ -1,0 +1,96 @@
+"""ctypes binding of libsq (include/sq.h).  Loading fails loudly: there is no
+CPU fallback for any engine call."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libsq.so")
+
+SQ_OK, SQ_ERR_ARG, SQ_ERR_CUDA, SQ_ERR_UNSUPPORTED, SQ_ERR_NOMEM, SQ_ERR_NODEVICE = range(6)
+SQ_F64, SQ_F32 = 0, 1
+SQ_PAULI_EXACT, SQ_PAULI_REFERENCE = 0, 1
+
+
+class SqError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"libsq error {code}: {msg}")
+        self.code = code
+
+
+class SqUnsupported(SqError):
+    pass
+
+
+class SqStats(C.Structure):
+    _fields_ = [("gates", C.c_uint64), ("passes", C.c_uint64), ("launches", C.c_uint64),
+                ("reductions", C.c_uint64), ("bytes_moved", C.c_uint64)]
+
+
+_lib = None
+
+_SIGS = {
+    "sq_last_error": (C.c_char_p, []),
+    "sq_version": (C.c_char_p, []),
+    "sq_state_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.c_int]),
+    "sq_state_destroy": (C.c_int, [C.c_void_p]),
+    "sq_state_ptrs": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    "sq_state_nqubits": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_int)]),
+    "sq_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sq_flush": (C.c_int, [C.c_void_p]),
+    "sq_synchronize": (C.c_int, [C.c_void_p]),
+    "sq_get_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sq_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sq_set_fusion": (C.c_int, [C.c_void_p, C.c_int]),
+    "sq_upload": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sq_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sq_init_state": (C.c_int, [C.c_void_p]),
+    "sq_vnorm": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "sq_vnormalize": (C.c_int, [C.c_void_p]),
+    "sq_apply_x": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64]),
+    "sq_apply_y": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64]),
+    "sq_apply_h": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64]),
+    "sq_apply_u1": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_uint64]),
+    "sq_apply_mcx": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint32]),
+    "sq_apply_mcu1": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_double]),
+    "sq_apply_swap": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64]),
+    "sq_apply_phase_list": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_double), C.c_uint64]),
+    "sq_apply_pauli_rotation": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                          C.c_double, C.c_uint64, C.c_int]),
+    "sq_measure_qbit": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double, C.POINTER(C.c_uint32)]),
+    "sq_prob_filter": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.POINTER(C.c_double)]),
+    "sq_apply_qms_w": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, C.c_double]),
+    "sq_get_stats": (C.c_int, [C.c_void_p, C.POINTER(SqStats)]),
+    "sq_reset_stats": (C.c_int, [C.c_void_p]),
+    "sq_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "sq_kernel_time": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+}
+
+EXPORTED = tuple(_SIGS)
+
+
+def load():
+    """Load libsq.so.  Raises RuntimeError when the native library is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"libsq not built ({LIB_PATH} missing): run `python -m suqa_gb300.build`; "
+                           "suqa_gb300 has no CPU fallback")
+    L = C.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != SQ_OK:
+        msg = _lib.sq_last_error().decode(errors="replace")
+        if rc == SQ_ERR_UNSUPPORTED:
+            raise SqUnsupported(rc, msg)
+        raise SqError(rc, msg)
+    return rc

@@ -1,0 +1,759 @@
+// libsq host side: state objects, the gate queue, the pass planner and the C ABI
+// declared in include/sq.h.  Device work is the tile-pass kernel in sq_pass.cuh.
+#include "sq.h"
+#include "sq_pass.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define SQ_CUDA(call)                                                                     \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(SQ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+struct HostOp {
+    uint8_t kind = 0;
+    uint8_t ny = 0;
+    uint64_t flip = 0;              // global pair mask (0 for diagonal ops)
+    uint64_t cmask = 0, cval = 0;   // element condition
+    uint64_t skm = 0, skv = 0;      // condition under which the op can touch an element
+    uint64_t zy = 0;
+    uint32_t shift = 0;
+    double c = 0.0, s = 0.0;
+    std::vector<double> tab;        // complex pairs (PLIST: cos/sin, W: f1/f2)
+};
+
+inline int popc(uint64_t x) { return __builtin_popcountll(x); }
+
+}  // namespace
+
+struct sq_state {
+    uint32_t n = 0;
+    int prec = SQ_F64;
+    size_t esz = 8;
+    uint64_t N = 0;
+    void* data = nullptr;           // device: re block then im block
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::vector<HostOp> pending;
+    double* d_partials = nullptr;
+    double* d_result = nullptr;
+    unsigned int* d_ticket = nullptr;
+    double* h_result = nullptr;     // pinned
+    int fusion = 1;
+    int nsm = 1;
+    int max_grid = 1;
+    int kp = 0;                     // default tile size for this state
+    sq_stats stats{};
+    int device = 0;
+    // kernel timing (sq_set_timing)
+    int timing = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_open;
+    std::vector<uint64_t> ev_bytes;
+};
+
+namespace {
+
+constexpr int kSmallMaxF64 = 12;  // whole state in one CTA's shared memory
+constexpr int kSmallMaxF32 = 13;
+constexpr int kTileMaxF64 = 13;
+constexpr int kTileMaxF32 = 14;
+
+int small_max(const sq_state* s) { return s->prec == SQ_F64 ? kSmallMaxF64 : kSmallMaxF32; }
+int tile_cap(const sq_state* s) { return s->prec == SQ_F64 ? kTileMaxF64 : kTileMaxF32; }
+
+int default_tile(const sq_state* s) {
+    if ((int)s->n <= small_max(s)) return (int)s->n;
+    const int kmax = s->prec == SQ_F64 ? 12 : 13;
+    int k = (int)s->n - 8;
+    if (k < 8) k = 8;
+    if (k > kmax) k = kmax;
+    return k;
+}
+
+size_t tile_smem(const sq_state* s, int K, int L) {
+    return (size_t)2 * ((size_t)1 << K) * s->esz + (size_t)8 * ((size_t)1 << (K - L));
+}
+
+template <typename T>
+int launch_pass_t(sq_state* s, const sqk::PassArgs& a, const sqk::Prog& p, int grid, int block, size_t smem) {
+    static int configured_smem = -1;
+    if ((int)smem > 48 * 1024 && configured_smem < (int)smem) {
+        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        configured_smem = 227 * 1024;
+    }
+    sqk::k_pass<T><<<grid, block, smem, s->stream>>>(a, p);
+    SQ_CUDA(cudaGetLastError());
+    return SQ_OK;
+}
+
+// Executes ops[i0, i1) as one pass, with an optional reduction at its end.
+int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, int red, uint64_t rmask,
+             uint64_t rval) {
+    const int n = (int)s->n;
+    uint64_t need = 0;
+    for (size_t i = i0; i < i1; ++i) need |= ops[i].flip;
+    int K = s->kp;
+    const int needbits = popc(need | 3ull);
+    if ((int)s->n > small_max(s) && needbits > K) K = needbits;
+    if (K > n) K = n;
+    if (K > tile_cap(s)) return fail(SQ_ERR_UNSUPPORTED, "gate touches too many qubits for one tile");
+    // contiguous low block L, then the high tile qubits
+    int L = K;
+    while (L > 0 && L + popc(L >= 64 ? 0 : (need >> L)) > K) --L;
+    uint64_t high = (L >= 64) ? 0 : (need & ~((1ull << L) - 1ull));
+    for (int b = L; b < n && L + popc(high) < K; ++b)
+        if (!((high >> b) & 1ull)) high |= 1ull << b;
+    const uint64_t lowm = (L == 0) ? 0ull : ((1ull << L) - 1ull);
+    const uint64_t tilemask = lowm | high;
+    const uint64_t all = (n == 64) ? ~0ull : ((1ull << n) - 1ull);
+    const uint64_t outer = all & ~tilemask;
+
+    sqk::PassArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.re = s->data;
+    a.im = (char*)s->data + s->N * s->esz;
+    a.K = K;
+    a.L = L;
+    a.store = (i1 > i0) ? 1 : 0;
+    a.partials = s->d_partials;
+    a.result = s->d_result;
+    a.ticket = s->d_ticket;
+    int nhb = 0;
+    for (int b = L; b < n; ++b)
+        if ((high >> b) & 1ull) a.hb[nhb++] = (uint8_t)b;
+    // tile-local position of a global bit
+    auto local_of = [&](int b) -> int {
+        if (b < L) return b;
+        for (int j = 0; j < nhb; ++j)
+            if (a.hb[j] == b) return L + j;
+        return -1;
+    };
+
+    // outer qubits every op of the pass requires at one value: the grid skips the rest
+    uint64_t fixm = 0, fixv = 0;
+    if (!red && i1 > i0) {
+        fixm = outer;
+        for (size_t i = i0; i < i1; ++i) fixm &= ops[i].skm;
+        for (size_t i = i0 + 1; i < i1; ++i) fixm &= ~(ops[i].skv ^ ops[i0].skv);
+        fixv = ops[i0].skv & fixm;
+    }
+    a.ofix = fixv;
+    a.ofree = outer & ~fixm;
+    a.ntiles = 1ull << popc(a.ofree);
+
+    static thread_local sqk::Prog p;
+    p.nops = (int)(i1 - i0);
+    p.red = red;
+    p.rmask = rmask;
+    p.rval = rval;
+    uint32_t tabpos = 0;
+    for (size_t i = i0; i < i1; ++i) {
+        const HostOp& h = ops[i];
+        sqk::Op& o = p.ops[i - i0];
+        std::memset(&o, 0, sizeof(o));
+        o.kind = h.kind;
+        o.ny = h.ny;
+        o.fz = (uint8_t)(popc(h.flip & h.zy) & 1);
+        uint32_t lf = 0;
+        for (int b = 0; b < n; ++b) {
+            if (!((h.flip >> b) & 1ull)) continue;
+            const int lb = local_of(b);
+            if (lb < 0) return fail(SQ_ERR_UNSUPPORTED, "internal: gate qubit outside the pass tile");
+            lf |= 1u << lb;
+        }
+        o.lflip = lf;
+        o.lpair = (uint8_t)(lf ? __builtin_ctz(lf) : 0);
+        o.cmask = h.cmask;
+        o.cval = h.cval;
+        o.ocm = h.skm & outer;
+        o.ocv = h.skv & o.ocm;
+        o.zy = h.zy;
+        o.shift = h.shift;
+        o.c = h.c;
+        o.s = h.s;
+        if (!h.tab.empty()) {
+            o.tab = tabpos;
+            std::memcpy(&p.tab[2 * tabpos], h.tab.data(), h.tab.size() * sizeof(double));
+            tabpos += (uint32_t)(h.tab.size() / 2);
+        }
+    }
+
+    const bool single = (K == n);
+    const int block = single ? (K >= 10 ? 1024 : (K >= 8 ? 256 : 128)) : 256;
+    int grid = (int)std::min<uint64_t>(a.ntiles, (uint64_t)s->max_grid);
+    if (grid < 1) grid = 1;
+    const size_t smem = tile_smem(s, K, L);
+    const uint64_t moved = a.ntiles * ((uint64_t)1 << K) * 2ull * s->esz * (a.store ? 2ull : 1ull);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (s->timing) {
+        for (cudaEvent_t* e : {&e0, &e1}) {
+            if (s->ev_pool.empty()) {
+                SQ_CUDA(cudaEventCreate(e));
+            } else {
+                *e = s->ev_pool.back();
+                s->ev_pool.pop_back();
+            }
+        }
+        SQ_CUDA(cudaEventRecord(e0, s->stream));
+    }
+    int rc = (s->prec == SQ_F64) ? launch_pass_t<double>(s, a, p, grid, block, smem)
+                                 : launch_pass_t<float>(s, a, p, grid, block, smem);
+    if (rc) return rc;
+    if (s->timing) {
+        SQ_CUDA(cudaEventRecord(e1, s->stream));
+        s->ev_open.push_back({e0, e1});
+        s->ev_bytes.push_back(moved);
+    }
+    s->stats.passes++;
+    s->stats.launches++;
+    s->stats.bytes_moved += moved;
+    if (red) s->stats.reductions++;
+    return SQ_OK;
+}
+
+// Applies every queued op; with red != 0 the last pass also reduces and the
+// result is copied into s->h_result (synchronously).
+int flush(sq_state* s, int red = 0, uint64_t rmask = 0, uint64_t rval = 0) {
+    std::vector<HostOp> ops;
+    ops.swap(s->pending);
+    size_t i = 0;
+    const int kcap = ((int)s->n <= small_max(s)) ? (int)s->n : std::max(s->kp, std::min(tile_cap(s), (int)s->n));
+    while (i < ops.size()) {
+        size_t j = i;
+        uint64_t need = 0;
+        uint32_t tab = 0;
+        while (j < ops.size()) {
+            const HostOp& h = ops[j];
+            const uint64_t nn = need | h.flip;
+            const int bits = popc(nn | 3ull);
+            const bool fits_tile = ((int)s->n <= small_max(s)) ? true : (bits <= s->kp || (j == i && bits <= kcap));
+            if (j > i && (!s->fusion || !fits_tile)) break;
+            if (j == i && !fits_tile) return fail(SQ_ERR_UNSUPPORTED, "gate touches too many qubits for one tile");
+            if ((int)(j - i) >= sqk::kMaxOps) break;
+            if (tab + h.tab.size() / 2 > (size_t)sqk::kMaxTab) break;
+            need = nn;
+            tab += (uint32_t)(h.tab.size() / 2);
+            ++j;
+        }
+        const bool last = (j == ops.size());
+        int rc = run_pass(s, ops, i, j, last ? red : 0, rmask, rval);
+        if (rc) return rc;
+        i = j;
+    }
+    if (ops.empty() && red) {
+        int rc = run_pass(s, ops, 0, 0, red, rmask, rval);
+        if (rc) return rc;
+    }
+    if (red) {
+        SQ_CUDA(cudaMemcpyAsync(s->h_result, s->d_result, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        SQ_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    return SQ_OK;
+}
+
+int enqueue(sq_state* s, HostOp&& h) {
+    s->pending.push_back(std::move(h));
+    s->stats.gates++;
+    if (s->pending.size() >= 4096) return flush(s);
+    return SQ_OK;
+}
+
+int check_q(const sq_state* s, uint32_t q) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    if (q >= s->n) return fail(SQ_ERR_ARG, "qubit index out of range");
+    return SQ_OK;
+}
+
+int check_mask(const sq_state* s, uint64_t m) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    if (s->n < 64 && (m >> s->n)) return fail(SQ_ERR_ARG, "mask has bits beyond the register");
+    return SQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* sq_last_error(void) { return g_err.c_str(); }
+const char* sq_version(void) { return "libsq 0.1 (sm_103a)"; }
+
+int sq_state_create(sq_state** out, uint32_t n, int precision) {
+    if (!out) return fail(SQ_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    if (n < 1 || n > 33) return fail(SQ_ERR_ARG, "qubit count must be in 1..33");
+    if (precision != SQ_F64 && precision != SQ_F32) return fail(SQ_ERR_ARG, "unknown precision");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(SQ_ERR_NODEVICE, "no CUDA device");
+    sq_state* s = new sq_state();
+    s->n = n;
+    s->prec = precision;
+    s->esz = precision == SQ_F64 ? 8 : 4;
+    s->N = 1ull << n;
+    cudaGetDevice(&s->device);
+    cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device);
+    s->max_grid = s->nsm * 8;
+    s->kp = default_tile(s);
+    size_t bytes = 2 * s->N * s->esz;
+    if (cudaMalloc(&s->data, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        delete s;
+        return fail(SQ_ERR_NOMEM, "device allocation of the state failed");
+    }
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&s->d_partials, sizeof(double) * 2 * (size_t)s->max_grid) != cudaSuccess ||
+        cudaMalloc(&s->d_result, sizeof(double) * 4) != cudaSuccess ||
+        cudaMalloc(&s->d_ticket, sizeof(unsigned int)) != cudaSuccess ||
+        cudaMallocHost(&s->h_result, sizeof(double) * 4) != cudaSuccess) {
+        cudaGetLastError();
+        sq_state_destroy(s);
+        return fail(SQ_ERR_NOMEM, "allocation of work buffers failed");
+    }
+    s->own_stream = true;
+    cudaMemsetAsync(s->d_ticket, 0, sizeof(unsigned int), s->stream);
+    int rc = sq_init_state(s);
+    if (rc) {
+        sq_state_destroy(s);
+        return rc;
+    }
+    *out = s;
+    return SQ_OK;
+}
+
+int sq_state_destroy(sq_state* s) {
+    if (!s) return SQ_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (auto& pr : s->ev_open) {
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+    }
+    for (auto e : s->ev_pool) cudaEventDestroy(e);
+    if (s->data) cudaFree(s->data);
+    if (s->d_partials) cudaFree(s->d_partials);
+    if (s->d_result) cudaFree(s->d_result);
+    if (s->d_ticket) cudaFree(s->d_ticket);
+    if (s->h_result) cudaFreeHost(s->h_result);
+    if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return SQ_OK;
+}
+
+int sq_state_ptrs(sq_state* s, void** re, void** im) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    int rc = flush(s);
+    if (rc) return rc;
+    if (re) *re = s->data;
+    if (im) *im = (char*)s->data + s->N * s->esz;
+    return SQ_OK;
+}
+
+int sq_state_nqubits(const sq_state* s, uint32_t* n, int* precision) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    if (n) *n = s->n;
+    if (precision) *precision = s->prec;
+    return SQ_OK;
+}
+
+int sq_set_stream(sq_state* s, void* stream) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    int rc = flush(s);
+    if (rc) return rc;
+    SQ_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->own_stream) cudaStreamDestroy(s->stream);
+    if (stream) {
+        s->stream = (cudaStream_t)stream;
+        s->own_stream = false;
+    } else {
+        SQ_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+        s->own_stream = true;
+    }
+    return SQ_OK;
+}
+
+int sq_flush(sq_state* s) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    return flush(s);
+}
+
+int sq_synchronize(sq_state* s) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    int rc = flush(s);
+    if (rc) return rc;
+    SQ_CUDA(cudaStreamSynchronize(s->stream));
+    return SQ_OK;
+}
+
+int sq_set_fusion(sq_state* s, int enabled) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    int rc = flush(s);
+    s->fusion = enabled ? 1 : 0;
+    return rc;
+}
+
+int sq_get_state(sq_state* s, double* re, double* im) {
+    if (!s || !re || !im) return fail(SQ_ERR_ARG, "null argument");
+    int rc = flush(s);
+    if (rc) return rc;
+    if (s->prec == SQ_F64) {
+        SQ_CUDA(cudaMemcpyAsync(re, s->data, s->N * 8, cudaMemcpyDeviceToHost, s->stream));
+        SQ_CUDA(cudaMemcpyAsync(im, (char*)s->data + s->N * 8, s->N * 8, cudaMemcpyDeviceToHost, s->stream));
+        SQ_CUDA(cudaStreamSynchronize(s->stream));
+    } else {
+        std::vector<float> tmp(2 * s->N);
+        SQ_CUDA(cudaMemcpyAsync(tmp.data(), s->data, 2 * s->N * 4, cudaMemcpyDeviceToHost, s->stream));
+        SQ_CUDA(cudaStreamSynchronize(s->stream));
+        for (uint64_t i = 0; i < s->N; ++i) {
+            re[i] = tmp[i];
+            im[i] = tmp[s->N + i];
+        }
+    }
+    return SQ_OK;
+}
+
+int sq_set_state(sq_state* s, const double* re, const double* im) {
+    if (!s || !re || !im) return fail(SQ_ERR_ARG, "null argument");
+    s->pending.clear();
+    if (s->prec == SQ_F64) {
+        SQ_CUDA(cudaMemcpyAsync(s->data, re, s->N * 8, cudaMemcpyHostToDevice, s->stream));
+        SQ_CUDA(cudaMemcpyAsync((char*)s->data + s->N * 8, im, s->N * 8, cudaMemcpyHostToDevice, s->stream));
+        SQ_CUDA(cudaStreamSynchronize(s->stream));
+    } else {
+        std::vector<float> tmp(2 * s->N);
+        for (uint64_t i = 0; i < s->N; ++i) {
+            tmp[i] = (float)re[i];
+            tmp[s->N + i] = (float)im[i];
+        }
+        SQ_CUDA(cudaMemcpyAsync(s->data, tmp.data(), 2 * s->N * 4, cudaMemcpyHostToDevice, s->stream));
+        SQ_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    return SQ_OK;
+}
+
+int sq_upload(sq_state* s, const void* re, const void* im) {
+    if (!s || !re || !im) return fail(SQ_ERR_ARG, "null argument");
+    s->pending.clear();
+    const size_t b = s->N * s->esz;
+    SQ_CUDA(cudaMemcpyAsync(s->data, re, b, cudaMemcpyHostToDevice, s->stream));
+    SQ_CUDA(cudaMemcpyAsync((char*)s->data + b, im, b, cudaMemcpyHostToDevice, s->stream));
+    return SQ_OK;
+}
+
+int sq_download(sq_state* s, void* re, void* im) {
+    if (!s || !re || !im) return fail(SQ_ERR_ARG, "null argument");
+    int rc = flush(s);
+    if (rc) return rc;
+    const size_t b = s->N * s->esz;
+    SQ_CUDA(cudaMemcpyAsync(re, s->data, b, cudaMemcpyDeviceToHost, s->stream));
+    SQ_CUDA(cudaMemcpyAsync(im, (char*)s->data + b, b, cudaMemcpyDeviceToHost, s->stream));
+    SQ_CUDA(cudaStreamSynchronize(s->stream));
+    return SQ_OK;
+}
+
+int sq_init_state(sq_state* s) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    s->pending.clear();
+    SQ_CUDA(cudaMemsetAsync(s->data, 0, 2 * s->N * s->esz, s->stream));
+    if (s->prec == SQ_F64) {
+        const double one = 1.0;
+        SQ_CUDA(cudaMemcpyAsync(s->data, &one, 8, cudaMemcpyHostToDevice, s->stream));
+    } else {
+        const float one = 1.0f;
+        SQ_CUDA(cudaMemcpyAsync(s->data, &one, 4, cudaMemcpyHostToDevice, s->stream));
+    }
+    SQ_CUDA(cudaStreamSynchronize(s->stream));
+    return SQ_OK;
+}
+
+int sq_vnorm(sq_state* s, double* norm) {
+    if (!s || !norm) return fail(SQ_ERR_ARG, "null argument");
+    int rc = flush(s, 2, 0, 0);
+    if (rc) return rc;
+    *norm = std::sqrt(s->h_result[0]);
+    return SQ_OK;
+}
+
+int sq_vnormalize(sq_state* s) {
+    double nrm = 0.0;
+    int rc = sq_vnorm(s, &nrm);
+    if (rc) return rc;
+    HostOp h;
+    h.kind = sqk::OP_SCALE;
+    h.s = 1. / nrm;
+    return enqueue(s, std::move(h));
+}
+
+static int pair_op(sq_state* s, uint8_t kind, uint32_t q, uint64_t gc) {
+    int rc = check_q(s, q);
+    if (rc || (rc = check_mask(s, gc))) return rc;
+    const uint64_t b = 1ull << q;
+    if (gc & b) return fail(SQ_ERR_ARG, "global control mask overlaps the target qubit");
+    HostOp h;
+    h.kind = kind;
+    h.flip = b;
+    h.cmask = gc;
+    h.cval = gc;
+    h.skm = gc;
+    h.skv = gc;
+    return enqueue(s, std::move(h));
+}
+
+int sq_apply_x(sq_state* s, uint32_t q, uint64_t gc) { return pair_op(s, sqk::OP_SWAPP, q, gc); }
+int sq_apply_y(sq_state* s, uint32_t q, uint64_t gc) { return pair_op(s, sqk::OP_YP, q, gc); }
+int sq_apply_h(sq_state* s, uint32_t q, uint64_t gc) { return pair_op(s, sqk::OP_HP, q, gc); }
+
+int sq_apply_u1(sq_state* s, uint32_t q, uint32_t q_mask, double phase, uint64_t gc) {
+    int rc = check_q(s, q);
+    if (rc || (rc = check_mask(s, gc))) return rc;
+    const uint64_t b = 1ull << q;
+    if (gc & b) return fail(SQ_ERR_ARG, "global control mask overlaps the target qubit");
+    // src/suqa.cu:271-285: condition (i & (gc | 1<<q)) == gc | (q_mask << q)
+    HostOp h;
+    h.kind = sqk::OP_PHASE;
+    h.cmask = gc | b;
+    h.cval = gc | ((uint64_t)(q_mask & 1u) << q);
+    h.skm = h.cmask;
+    h.skv = h.cval;
+    sincos(phase, &h.s, &h.c);
+    return enqueue(s, std::move(h));
+}
+
+int sq_apply_mcx(sq_state* s, uint64_t control_mask, uint64_t mask_qs, uint32_t q_target) {
+    int rc = check_q(s, q_target);
+    if (rc || (rc = check_mask(s, control_mask)) || (rc = check_mask(s, mask_qs))) return rc;
+    const uint64_t b = 1ull << q_target;
+    if ((control_mask & b) || (mask_qs & b)) return fail(SQ_ERR_ARG, "control mask contains the target");
+    if (mask_qs & ~control_mask) return fail(SQ_ERR_ARG, "mask_qs has bits outside control_mask");
+    HostOp h;
+    h.kind = sqk::OP_SWAPP;
+    h.flip = b;
+    h.cmask = control_mask;
+    h.cval = mask_qs;
+    h.skm = control_mask;
+    h.skv = mask_qs;
+    return enqueue(s, std::move(h));
+}
+
+int sq_apply_mcu1(sq_state* s, uint64_t control_mask, uint64_t mask_qs, double phase) {
+    int rc = check_mask(s, control_mask);
+    if (rc || (rc = check_mask(s, mask_qs))) return rc;
+    if (mask_qs & ~control_mask) return fail(SQ_ERR_ARG, "mask_qs has bits outside control_mask");
+    HostOp h;
+    h.kind = sqk::OP_PHASE;
+    h.cmask = control_mask;
+    h.cval = mask_qs;
+    h.skm = control_mask;
+    h.skv = mask_qs;
+    sincos(phase, &h.s, &h.c);
+    return enqueue(s, std::move(h));
+}
+
+int sq_apply_swap(sq_state* s, uint32_t q1, uint32_t q2, uint64_t gc) {
+    int rc = check_q(s, q1);
+    if (rc || (rc = check_q(s, q2)) || (rc = check_mask(s, gc))) return rc;
+    if (q1 == q2) return fail(SQ_ERR_ARG, "swap of a qubit with itself");
+    const uint64_t b1 = 1ull << q1, b2 = 1ull << q2;
+    if (gc & (b1 | b2)) return fail(SQ_ERR_ARG, "global control mask overlaps the swapped qubits");
+    // pairs (i|b1, i|b2) for (i & (gc|b1|b2)) == gc: the pair's lower-bit element has
+    // the higher bit set
+    const uint64_t bhi = b1 > b2 ? b1 : b2;
+    HostOp h;
+    h.kind = sqk::OP_SWAPP;
+    h.flip = b1 | b2;
+    h.cmask = gc | bhi;
+    h.cval = gc | bhi;
+    h.skm = gc;
+    h.skv = gc;
+    return enqueue(s, std::move(h));
+}
+
+int sq_apply_phase_list(sq_state* s, uint32_t q0, uint32_t q_size, const double* phases, uint64_t gc) {
+    if (!s || !phases) return fail(SQ_ERR_ARG, "null argument");
+    // src/suqa.cu:420-422 validates q_size > 0 and the list length; the device table
+    // holds 128 entries (include/suqa_kernels.cuh:242)
+    if (q_size == 0 || q_size > 7) return fail(SQ_ERR_UNSUPPORTED, "invalid q_size for a phase list");
+    if (q0 + q_size > s->n) return fail(SQ_ERR_ARG, "phase-list register out of range");
+    int rc = check_mask(s, gc);
+    if (rc) return rc;
+    HostOp h;
+    h.kind = sqk::OP_PLIST;
+    h.cmask = gc;
+    h.zy = (1ull << q_size) - 1ull;
+    h.shift = q0;
+    const uint32_t L = 1u << q_size;
+    h.tab.resize(2 * L);
+    for (uint32_t k = 0; k < L; ++k) sincos(phases[k], &h.tab[2 * k + 1], &h.tab[2 * k]);
+    if (gc == 0) {  // the reference guard (i & gc) never holds: nothing to do
+        s->stats.gates++;
+        return SQ_OK;
+    }
+    return enqueue(s, std::move(h));
+}
+
+static bool ref_supported(uint32_t k, const uint32_t* ps) {
+    if (k == 1 || k == 2) return true;
+    if (k == 3) {
+        uint32_t a[3] = {ps[0], ps[1], ps[2]};
+        std::sort(a, a + 3);
+        return a[2] == 3 && a[0] == a[1];
+    }
+    return false;
+}
+
+int sq_apply_pauli_rotation(sq_state* s, uint32_t k, const uint32_t* qubits, const uint32_t* paulis,
+                            double phase, uint64_t gc, int flags) {
+    if (!s || !qubits || !paulis) return fail(SQ_ERR_ARG, "null argument");
+    if (k == 0 || k > 32) return fail(SQ_ERR_ARG, "Pauli string length must be in 1..32");
+    int rc = check_mask(s, gc);
+    if (rc) return rc;
+    for (uint32_t t = 0; t < k; ++t)
+        if (paulis[t] < 1 || paulis[t] > 3) return fail(SQ_ERR_ARG, "Pauli type must be 1 (X), 2 (Y) or 3 (Z)");
+    const bool refmode = (flags & SQ_PAULI_REFERENCE) != 0;
+    if (refmode && !ref_supported(k, paulis))
+        return fail(SQ_ERR_UNSUPPORTED, "ERROR: unimplemented pauli TP rotation in the selected configuration");
+    uint32_t pl[32];
+    for (uint32_t t = 0; t < k; ++t) pl[t] = paulis[t];
+    // reference XY kernel (include/suqa_cpu.hpp:408-411) applies exp(i t Y(x)X)
+    if (refmode && k == 2 && ((pl[0] == 1 && pl[1] == 2) || (pl[0] == 2 && pl[1] == 1))) std::swap(pl[0], pl[1]);
+    HostOp h;
+    h.kind = sqk::OP_PAULI;
+    uint64_t seen = 0;
+    for (uint32_t t = 0; t < k; ++t) {
+        if ((rc = check_q(s, qubits[t]))) return rc;
+        const uint64_t b = 1ull << qubits[t];
+        if (seen & b) return fail(SQ_ERR_ARG, "repeated qubit in a Pauli string");
+        seen |= b;
+        if (pl[t] == 1 || pl[t] == 2) h.flip |= b;
+        if (pl[t] == 2 || pl[t] == 3) h.zy |= b;
+        if (pl[t] == 2) h.ny++;
+    }
+    if (gc & seen) return fail(SQ_ERR_ARG, "global control mask overlaps the rotated qubits");
+    // pair ops test the control on g0 (lowest flipped bit clear); diagonal ops on g
+    h.cmask = gc;
+    h.cval = gc;
+    h.skm = gc;
+    h.skv = gc;
+    sincos(phase, &h.s, &h.c);
+    return enqueue(s, std::move(h));
+}
+
+int sq_apply_qms_w(sq_state* s, uint32_t q_acc, uint64_t mask_enew, uint32_t shift, uint32_t E_old,
+                   double c_factor) {
+    int rc = check_q(s, q_acc);
+    if (rc || (rc = check_mask(s, mask_enew))) return rc;
+    if (mask_enew & (1ull << q_acc)) return fail(SQ_ERR_ARG, "energy mask contains the acceptance qubit");
+    const uint64_t levels = (mask_enew >> shift) + 1ull;
+    if (levels > (uint64_t)sqk::kMaxTab) return fail(SQ_ERR_UNSUPPORTED, "energy register wider than 7 qubits");
+    HostOp h;
+    h.kind = sqk::OP_W;
+    h.flip = 1ull << q_acc;
+    h.zy = mask_enew;
+    h.shift = shift;
+    h.tab.resize(2 * levels);
+    // include/qms.cuh:288-297: dE = Enew*c - E_old*c; f1 = exp(-dE/2), f2 = sqrt(1 - f1^2)
+    for (uint64_t e = 0; e < levels; ++e) {
+        const uint32_t Enew = (uint32_t)e;
+        const double dE = (Enew * c_factor - E_old * c_factor);
+        double fs1, fs2;
+        if (dE > 0) {
+            fs1 = std::exp(-dE / 2.0);
+            fs2 = std::sqrt(1.0 - fs1 * fs1);
+        } else {
+            fs1 = 1.0;
+            fs2 = 0.0;
+        }
+        h.tab[2 * e] = fs1;
+        h.tab[2 * e + 1] = fs2;
+    }
+    return enqueue(s, std::move(h));
+}
+
+int sq_measure_qbit(sq_state* s, uint32_t q, double r, uint32_t* c) {
+    int rc = check_q(s, q);
+    if (rc) return rc;
+    if (!c) return fail(SQ_ERR_ARG, "null output");
+    const uint64_t b = 1ull << q;
+    rc = flush(s, 1, b, 0);
+    if (rc) return rc;
+    const double p0 = s->h_result[0], p1 = s->h_result[1];
+    // src/suqa.cu:690-695: c = r < prob1; keep branch c; multiply by 1./norm
+    const uint32_t cc = (uint32_t)(r < p1);
+    const double keep = cc ? p1 : p0;
+    HostOp h;
+    h.kind = sqk::OP_COLLAPSE;
+    h.cmask = b;
+    h.cval = cc ? b : 0ull;
+    h.s = 1. / std::sqrt(keep);
+    *c = cc;
+    return enqueue(s, std::move(h));
+}
+
+int sq_prob_filter(sq_state* s, uint64_t mask_qs, uint64_t mask, double* prob) {
+    int rc = check_mask(s, mask_qs);
+    if (rc) return rc;
+    if (!prob) return fail(SQ_ERR_ARG, "null output");
+    rc = flush(s, 2, mask_qs, mask);
+    if (rc) return rc;
+    *prob = s->h_result[0];
+    return SQ_OK;
+}
+
+int sq_get_stats(const sq_state* s, sq_stats* out) {
+    if (!s || !out) return fail(SQ_ERR_ARG, "null argument");
+    *out = s->stats;
+    return SQ_OK;
+}
+
+int sq_set_timing(sq_state* s, int enabled) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    int rc = flush(s);
+    s->timing = enabled ? 1 : 0;
+    return rc;
+}
+
+int sq_kernel_time(sq_state* s, double* ms, uint64_t* launches, uint64_t* bytes) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    int rc = flush(s);
+    if (rc) return rc;
+    SQ_CUDA(cudaStreamSynchronize(s->stream));
+    double tot = 0.0;
+    uint64_t by = 0;
+    for (size_t i = 0; i < s->ev_open.size(); ++i) {
+        float t = 0.f;
+        SQ_CUDA(cudaEventElapsedTime(&t, s->ev_open[i].first, s->ev_open[i].second));
+        tot += t;
+        by += s->ev_bytes[i];
+        s->ev_pool.push_back(s->ev_open[i].first);
+        s->ev_pool.push_back(s->ev_open[i].second);
+    }
+    if (ms) *ms = tot;
+    if (launches) *launches = s->ev_open.size();
+    if (bytes) *bytes = by;
+    s->ev_open.clear();
+    s->ev_bytes.clear();
+    return SQ_OK;
+}
+
+int sq_reset_stats(sq_state* s) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    std::memset(&s->stats, 0, sizeof(s->stats));
+    return SQ_OK;
+}
+
+}  // extern "C"

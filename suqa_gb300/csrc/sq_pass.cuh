@@ -1,0 +1,320 @@
+// Tile-pass kernel of the state-vector engine (sm_103a).
+//
+// One pass = one read and one write of (part of) the state.  The state index
+// space is split into tiles of 2^K amplitudes: the tile holds the L lowest
+// qubits (contiguous in memory, so loads are 16-byte vectors in runs of 2^L
+// elements) plus K-L "high" qubits chosen by the host planner so that every
+// non-diagonal qubit of every gate in the pass lies inside the tile.  A CTA
+// stages a tile's re and im blocks in shared memory, applies the pass's gate
+// list (each gate is one sweep of the tile with a barrier in between), folds in
+// an optional reduction (measurement probabilities or a filtered norm) and
+// writes the tile back.  Gates whose controls sit on qubits outside the tile
+// are resolved per tile: a tile whose fixed bits fail a gate's controls skips
+// that gate, and a tile that no gate touches is neither loaded nor stored.
+//
+// Element formulas restate the reference kernels (include/suqa_kernels.cuh and
+// include/suqa_cpu.hpp of SUQA); each case names its source below.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sqk {
+
+constexpr int kMaxOps = 24;   // gates per launch (kernel parameter space <= 4 KB)
+constexpr int kMaxTab = 128;  // complex table entries per launch (W factors, phase lists)
+constexpr int kMaxHigh = 16;  // tile qubits above the contiguous low block
+
+enum OpKind : uint8_t {
+    OP_SWAPP = 0,     // a0 <-> a1 over pairs (X, CX, MCX, SWAP)
+    OP_YP = 1,        // Y: a0' = -i a1, a1' = i a0
+    OP_HP = 2,        // Hadamard with the literal 0.7071067811865475
+    OP_PAULI = 3,     // exp(i theta P) (pair form, or diagonal when no X/Y)
+    OP_PHASE = 4,     // a *= c + i s on (g & cmask) == cval  (U1, CU1, MCU1)
+    OP_PLIST = 5,     // a *= tab[(g >> shift) & zy] where (g & cmask) != 0
+    OP_W = 6,         // QMS acceptance rotation, (f1, f2) = tab[(g0 & zy) >> shift]
+    OP_COLLAPSE = 7,  // keep (g & cmask) == cval scaled by s, zero the rest
+    OP_SCALE = 8      // a *= s everywhere
+};
+
+// One gate in tile-local form (64 bytes).  For pair operations the pairs are
+// (t0, t0 ^ lflip) with t0 the tile index whose bit lpair is clear; control
+// conditions are tested on g0, the global index of t0.
+struct Op {
+    uint8_t kind;
+    uint8_t lpair;   // tile-local bit that orders the pair
+    uint8_t ny;      // Pauli: number of Y factors
+    uint8_t fz;      // Pauli: parity of (flip & zy)
+    uint32_t lflip;  // tile-local flip mask
+    uint64_t cmask, cval;  // element condition
+    uint64_t ocm, ocv;     // part of the condition on qubits outside the tile
+    uint64_t zy;           // Pauli: Y|Z mask; PLIST/W: extraction mask
+    uint32_t shift, tab;   // PLIST/W: shift and table offset (in complex entries)
+    double c, s;
+};
+
+struct Prog {
+    int nops;
+    int red;             // 0 none, 1 measurement split by rmask, 2 filter (g & rmask) == rval
+    uint64_t rmask, rval;
+    Op ops[kMaxOps];
+    double tab[2 * kMaxTab];
+};
+
+struct PassArgs {
+    void* re;
+    void* im;
+    uint64_t ofree;   // outer qubits enumerated by the tile index
+    uint64_t ofix;    // value of the fixed outer qubits
+    uint64_t ntiles;
+    double* partials; // 2 per CTA
+    double* result;   // 2 doubles
+    unsigned int* ticket;
+    int K, L;
+    int store;        // 0 for a reduction-only pass
+    int pad;
+    uint8_t hb[kMaxHigh];  // global positions of the tile qubits >= L
+};
+
+template <typename T> struct VecT;
+template <> struct VecT<double> { typedef double2 type; static constexpr int W = 2; };
+template <> struct VecT<float>  { typedef float4  type; static constexpr int W = 4; };
+
+__device__ __forceinline__ uint32_t insert_zero(uint32_t p, uint32_t b) {
+    const uint32_t lo = p & ((1u << b) - 1u);
+    return ((p >> b) << (b + 1u)) | lo;
+}
+
+__device__ __forceinline__ int parity64(uint64_t x) { return __popcll(x) & 1; }
+
+// out = c*a + s*(i^k * b), written as the reference's rotate2 (a*c -/+ x*s)
+template <typename T>
+__device__ __forceinline__ void rot_k(T ar, T ai, T br, T bi, int k, T c, T s, T& outr, T& outi) {
+    T xr = (k & 1) ? bi : br;
+    T xi = (k & 1) ? br : bi;
+    if (k == 1 || k == 2) xr = -xr;
+    if (k >= 2) xi = -xi;
+    outr = ar * c + xr * s;
+    outi = ai * c + xi * s;
+}
+
+template <typename T>
+__device__ __forceinline__ double sqnorm(T r, T i) {
+    return (double)(r * r + i * i);
+}
+
+template <typename T>
+__device__ __forceinline__ void block_reduce2(double& a, double& b, double (*sh)[33]) {
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { sh[0][w] = a; sh[1][w] = b; }
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    if (w == 0) {
+        a = l < nw ? sh[0][l] : 0.0;
+        b = l < nw ? sh[1][l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            b += __shfl_down_sync(0xffffffffu, b, o);
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs a,
+                                               const __grid_constant__ Prog p) {
+    typedef typename VecT<T>::type V;
+    constexpr int W = VecT<T>::W;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double red_sh[2][33];
+    __shared__ int last_flag;
+
+    const int K = a.K, L = a.L;
+    const uint32_t TS = 1u << K;
+    const uint32_t lowmask = (1u << L) - 1u;
+    T* sre = reinterpret_cast<T*>(smem_raw);
+    T* sim = sre + TS;
+    uint64_t* offs = reinterpret_cast<uint64_t*>(sim + TS);
+    const uint32_t nh = 1u << (K - L);
+    for (uint32_t h = threadIdx.x; h < nh; h += blockDim.x) {
+        uint64_t o = 0;
+        for (int j = 0; j < K - L; ++j)
+            if ((h >> j) & 1u) o |= 1ull << a.hb[j];
+        offs[h] = o;
+    }
+    __syncthreads();
+
+    T* gre = reinterpret_cast<T*>(a.re);
+    T* gim = reinterpret_cast<T*>(a.im);
+    double acc0 = 0.0, acc1 = 0.0;
+
+    for (uint64_t tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        uint64_t base = a.ofix;
+        {
+            uint64_t f = a.ofree, t = tile;
+            while (f) {
+                const uint64_t b = f & (~f + 1ull);
+                if (t & 1ull) base |= b;
+                t >>= 1;
+                f ^= b;
+            }
+        }
+        bool any = p.red != 0;
+        for (int k = 0; k < p.nops && !any; ++k)
+            any = (base & p.ops[k].ocm) == p.ops[k].ocv;
+        if (!any) continue;  // uniform over the CTA
+
+        // ---- load the tile (16-byte vectors, runs of 2^L contiguous elements)
+        if ((1u << L) >= (uint32_t)W) {
+            for (uint32_t v = threadIdx.x; v < TS / W; v += blockDim.x) {
+                const uint32_t t = v * W;
+                const uint64_t g = base | offs[t >> L] | (t & lowmask);
+                *reinterpret_cast<V*>(sre + t) = __ldcs(reinterpret_cast<const V*>(gre + g));
+                *reinterpret_cast<V*>(sim + t) = __ldcs(reinterpret_cast<const V*>(gim + g));
+            }
+        } else {  // states narrower than one vector
+            for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
+                const uint64_t g = base | offs[t >> L] | (t & lowmask);
+                sre[t] = gre[g];
+                sim[t] = gim[g];
+            }
+        }
+        __syncthreads();
+
+        // ---- gates
+        for (int k = 0; k < p.nops; ++k) {
+            const Op& op = p.ops[k];
+            if ((base & op.ocm) != op.ocv) continue;
+            const T c = (T)op.c, s = (T)op.s;
+            const int kind = op.kind;
+            if (kind <= OP_PAULI && !(kind == OP_PAULI && op.lflip == 0u) || kind == OP_W) {
+                const uint32_t lp = op.lpair, lf = op.lflip;
+                for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
+                    const uint32_t t0 = insert_zero(pp, lp);
+                    const uint32_t t1 = t0 ^ lf;
+                    const uint64_t g0 = base | offs[t0 >> L] | (t0 & lowmask);
+                    if ((g0 & op.cmask) != op.cval) continue;
+                    const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
+                    if (kind == OP_SWAPP) {
+                        // include/suqa_cpu.hpp:223-253 (MCX), :268-319 (SWAP)
+                        sre[t0] = a1r; sim[t0] = a1i; sre[t1] = a0r; sim[t1] = a0i;
+                    } else if (kind == OP_YP) {
+                        // include/suqa_cpu.hpp:96-122: a1' = i a0, a0' = -i a1
+                        sre[t1] = -a0i; sim[t1] = a0r; sre[t0] = a1i; sim[t0] = -a1r;
+                    } else if (kind == OP_HP) {
+                        // include/suqa_cpu.hpp:150-206
+                        const T h = (T)0.7071067811865475;
+                        sre[t0] = h * (a0r + a1r); sim[t0] = h * (a0i + a1i);
+                        sre[t1] = h * (a0r - a1r); sim[t1] = h * (a0i - a1i);
+                    } else if (kind == OP_PAULI) {
+                        // exp(i th P): a0' = c a0 + i s w(g1) a1, a1' = c a1 + i s w(g0) a0
+                        const int pz0 = parity64(g0 & op.zy);
+                        const int k1 = 1 + op.ny + 2 * pz0;
+                        const int k0 = 1 + op.ny + 2 * (pz0 ^ op.fz);
+                        T r0, i0, r1, i1;
+                        rot_k<T>(a0r, a0i, a1r, a1i, k0 & 3, c, s, r0, i0);
+                        rot_k<T>(a1r, a1i, a0r, a0i, k1 & 3, c, s, r1, i1);
+                        sre[t0] = r0; sim[t0] = i0; sre[t1] = r1; sim[t1] = i1;
+                    } else {  // OP_W: include/qms.cuh:245-309
+                        const uint32_t e = (uint32_t)((g0 & op.zy) >> op.shift);
+                        const T f1 = (T)p.tab[2 * (op.tab + e)], f2 = (T)p.tab[2 * (op.tab + e) + 1];
+                        sre[t0] = f2 * a0r + f1 * a1r; sim[t0] = f2 * a0i + f1 * a1i;
+                        sre[t1] = f1 * a0r - f2 * a1r; sim[t1] = f1 * a0i - f2 * a1i;
+                    }
+                }
+            } else {
+                for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
+                    const uint64_t g = base | offs[t >> L] | (t & lowmask);
+                    T ar = sre[t], ai = sim[t];
+                    if (kind == OP_PHASE) {
+                        // include/suqa_kernels.cuh:175-190, :209-221
+                        if ((g & op.cmask) != op.cval) continue;
+                        sre[t] = ar * c - ai * s;
+                        sim[t] = ai * c + ar * s;
+                    } else if (kind == OP_PAULI) {  // all-Z string: diagonal
+                        if ((g & op.cmask) != op.cval) continue;
+                        T r, i;
+                        rot_k<T>(ar, ai, ar, ai, 1 + 2 * parity64(g & op.zy), c, s, r, i);
+                        sre[t] = r; sim[t] = i;
+                    } else if (kind == OP_PLIST) {
+                        // include/suqa_kernels.cuh:246-259 (guard: any gc bit set)
+                        if ((g & op.cmask) == 0ull) continue;
+                        const uint32_t e = (uint32_t)((g >> op.shift) & op.zy);
+                        const T cx = (T)p.tab[2 * (op.tab + e)], cy = (T)p.tab[2 * (op.tab + e) + 1];
+                        sre[t] = ar * cx - ai * cy;
+                        sim[t] = ar * cy + ai * cx;
+                    } else if (kind == OP_COLLAPSE) {
+                        // src/suqa.cu:664-696: zero the discarded branch, rescale the kept one
+                        const bool keep = (g & op.cmask) == op.cval;
+                        sre[t] = keep ? ar * s : (T)0;
+                        sim[t] = keep ? ai * s : (T)0;
+                    } else {  // OP_SCALE
+                        sre[t] = ar * s;
+                        sim[t] = ai * s;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+
+        // ---- reduction contribution and store
+        if (p.red) {
+            for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
+                const uint64_t g = base | offs[t >> L] | (t & lowmask);
+                const double w = sqnorm<T>(sre[t], sim[t]);
+                if (p.red == 1) {
+                    if (g & p.rmask) acc1 += w; else acc0 += w;
+                } else if ((g & p.rmask) == p.rval) {
+                    acc0 += w;
+                }
+            }
+        }
+        if (a.store) {
+            if ((1u << L) >= (uint32_t)W) {
+                for (uint32_t v = threadIdx.x; v < TS / W; v += blockDim.x) {
+                    const uint32_t t = v * W;
+                    const uint64_t g = base | offs[t >> L] | (t & lowmask);
+                    __stcs(reinterpret_cast<V*>(gre + g), *reinterpret_cast<const V*>(sre + t));
+                    __stcs(reinterpret_cast<V*>(gim + g), *reinterpret_cast<const V*>(sim + t));
+                }
+            } else {
+                for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
+                    const uint64_t g = base | offs[t >> L] | (t & lowmask);
+                    gre[g] = sre[t];
+                    gim[g] = sim[t];
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    if (!p.red) return;
+    // ---- deterministic two-level reduction: per-CTA partials, last CTA sums them
+    block_reduce2<T>(acc0, acc1, red_sh);
+    if (threadIdx.x == 0) {
+        a.partials[2 * blockIdx.x] = acc0;
+        a.partials[2 * blockIdx.x + 1] = acc1;
+        __threadfence();
+        const unsigned int tk = atomicAdd(a.ticket, 1u);
+        last_flag = (tk == gridDim.x - 1u);
+    }
+    __syncthreads();
+    if (!last_flag) return;
+    __threadfence();
+    double s0 = 0.0, s1 = 0.0;
+    for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+        s0 += __ldcg(a.partials + 2 * b);
+        s1 += __ldcg(a.partials + 2 * b + 1);
+    }
+    block_reduce2<T>(s0, s1, red_sh);
+    if (threadIdx.x == 0) {
+        a.result[0] = s0;
+        a.result[1] = s1;
+        *a.ticket = 0u;
+    }
+}
+
+}  // namespace sqk

@@ -1,0 +1,97 @@
+"""Synthetic workloads of the benchmark configurations (seeded, no datasets).
+
+random_circuit: the gate-engine microbenchmark — gates drawn uniformly from
+{X, H, CX, MCX with 2-4 controls, U1 with theta ~ U[0, 2pi), Pauli
+tensor-product rotation on 2-6 qubits with Paulis uniform over X/Y/Z}, distinct
+qubits per gate, and a measure_qbit on a random qubit every 100 gates with r
+from the same stream."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+KINDS = ("x", "h", "cx", "mcx", "u1", "ptp")
+
+
+def random_circuit(n: int, ngates: int = 1000, seed: int = 7, measure_every: int = 100):
+    rng = np.random.default_rng(seed)
+    gates = []
+    for g in range(ngates):
+        kind = KINDS[int(rng.integers(len(KINDS)))]
+        if kind in ("x", "h"):
+            gates.append((kind, int(rng.integers(n))))
+        elif kind == "cx":
+            c, t = (int(q) for q in rng.choice(n, size=2, replace=False))
+            gates.append(("cx", c, t))
+        elif kind == "mcx":
+            k = int(rng.integers(2, 5))
+            qs = [int(q) for q in rng.choice(n, size=k + 1, replace=False)]
+            gates.append(("mcx", qs[:k], qs[k]))
+        elif kind == "u1":
+            gates.append(("u1", int(rng.integers(n)), float(rng.uniform(0.0, 2.0 * math.pi))))
+        else:
+            k = int(rng.integers(2, 7))
+            qs = [int(q) for q in rng.choice(n, size=k, replace=False)]
+            ps = [int(p) for p in rng.integers(1, 4, size=k)]
+            gates.append(("ptp", qs, ps, float(rng.uniform(0.0, 2.0 * math.pi))))
+        if measure_every and (g + 1) % measure_every == 0:
+            gates.append(("measure", int(rng.integers(n)), float(rng.random())))
+    return gates
+
+
+def random_state(n: int, seed: int = 7, dtype=np.float64):
+    """re, im ~ N(0, 1), normalised in FP64; returned as two arrays of dtype."""
+    rng = np.random.default_rng(seed)
+    N = 1 << n
+    re = rng.standard_normal(N)
+    im = rng.standard_normal(N)
+    nrm = math.sqrt(float(np.dot(re, re)) + float(np.dot(im, im)))
+    re /= nrm
+    im /= nrm
+    return re.astype(dtype, copy=False), im.astype(dtype, copy=False)
+
+
+def apply_circuit(st, gates):
+    """Applies a circuit through the suqa:: mirror; returns the measured bits."""
+    bits = []
+    for g in gates:
+        k = g[0]
+        if k == "x":
+            st.apply_x(g[1])
+        elif k == "h":
+            st.apply_h(g[1])
+        elif k == "cx":
+            st.apply_cx(g[1], g[2])
+        elif k == "mcx":
+            st.apply_mcx(g[1], g[2])
+        elif k == "u1":
+            st.apply_u1(g[1], g[2])
+        elif k == "ptp":
+            st.apply_pauli_rotation(g[1], g[2], g[3])
+        elif k == "measure":
+            bits.append(st.measure_qbit(g[1], g[2]))
+    return bits
+
+
+def algorithmic_bytes(gates, n: int, bytes_per_amp: int) -> int:
+    """Sum over gates of 2 * B * N * f (f = fraction of amplitudes a gate must
+    read and write): 1 for X, H and Pauli rotations, 2^-c for c controls, 1/2
+    for U1; a measurement counts 2 * B * N (probability read of half, zero-write
+    of half, rescale of the kept half)."""
+    N = 1 << n
+    tot = 0.0
+    for g in gates:
+        k = g[0]
+        if k in ("x", "h", "ptp"):
+            f = 1.0
+        elif k == "cx":
+            f = 0.5
+        elif k == "mcx":
+            f = 2.0 ** -len(g[1])
+        elif k == "u1":
+            f = 0.5
+        else:  # measure
+            f = 1.0
+        tot += 2.0 * bytes_per_amp * N * f
+    return int(tot)

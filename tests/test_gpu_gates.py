@@ -1,0 +1,136 @@
+"""Gate-engine parity on the GPU (libsq through the suqa:: mirror) against the
+committed reference fixtures and the CPU oracle.  FP64 tolerance: 1e-12 of the
+state's largest amplitude per amplitude; measured bits identical."""
+import math
+
+import numpy as np
+import pytest
+
+import circuits
+import golden_io
+import gpu_script
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+RTOL64 = 1e-12
+RTOL32 = 2e-5
+
+
+@pytest.mark.parametrize("fusion", [True, False])
+def test_golden_fixtures_fp64(fusion):
+    worst = 0.0
+    n = 0
+    for name, lines, want in golden_io.gate_cases():
+        got = gpu_script.run_script(lines, "f64", fusion)
+        worst = max(worst, golden_io.compare_results(got, want, rtol=RTOL64))
+        n += 1
+    assert n >= 30
+    print("worst relative amplitude error", worst)
+
+
+@pytest.mark.parametrize("seed", range(20))
+def test_random_scripts_vs_oracle_fp64(seed):
+    n = [3, 5, 8, 11, 12, 13, 14, 15, 16, 17][seed % 10]
+    lines = circuits.random_script(1000 + seed, n, 70, reference_only=False, random_init=n <= 12,
+                                   dump_every=10 if n <= 12 else 35)
+    want = oracle.run_script(lines)
+    got = gpu_script.run_script(lines, "f64")
+    golden_io.compare_results(got, want, rtol=RTOL64)
+
+
+@pytest.mark.parametrize("n", [18, 20, 22])
+def test_large_random_vs_oracle_fp64(n):
+    lines = circuits.random_script(77 + n, n, 40, reference_only=False, random_init=False,
+                                   dump_every=0, measure_every=9)
+    want = oracle.run_script(lines, threads=8)
+    got = gpu_script.run_script(lines, "f64")
+    golden_io.compare_results(got, want, rtol=RTOL64)
+
+
+@pytest.mark.parametrize("n", [4, 10, 14, 18])
+def test_fp32_vs_oracle(n):
+    # no projective measurement: an FP32 rounding can legitimately flip a draw
+    lines = circuits.random_script(500 + n, n, 60, reference_only=False, random_init=n <= 10,
+                                   measure_every=0, dump_every=15)
+    lines += ["prob 2 0 1 1 0", "vnorm", "dump"]
+    want = oracle.run_script(lines)
+    got = gpu_script.run_script(lines, "f32")
+    golden_io.compare_results(got, want, rtol=RTOL32)
+
+
+def test_fp32_measurement_far_from_threshold():
+    lines = ["setup 12"] + [f"h {q}" for q in range(12)] + [f"u1 {q} {circuits.hx(0.3 * q)}" for q in range(12)]
+    lines += ["measure 3 0x1.0p-3", "measure 7 0x1.cp-1", "dump", "vnorm"]
+    golden_io.compare_results(gpu_script.run_script(lines, "f32"), oracle.run_script(lines), rtol=RTOL32)
+
+
+def test_qms_w_vs_oracle():
+    from suqa_gb300 import State
+    rng = np.random.default_rng(9)
+    for n, ene in [(8, 4), (10, 6), (15, 5)]:
+        N = 1 << n
+        a = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+        a /= np.linalg.norm(a)
+        o = oracle.OracleState(n)
+        o.set_array(a)
+        mask = ((1 << ene) - 1) << 3
+        for e_old, cf in [(0, 0.7), (5, 1.3), ((1 << ene) - 1, 0.05)]:
+            oracle.load().or_apply_qms_w(o.p, n - 1, mask, 3, e_old, cf)
+        with State(n) as s:
+            s.set_state(a)
+            for e_old, cf in [(0, 0.7), (5, 1.3), ((1 << ene) - 1, 0.05)]:
+                s.apply_qms_w(n - 1, mask, 3, e_old, cf)
+            got = s.get_state()
+        want = o.array()
+        assert np.max(np.abs(got - want)) <= RTOL64 * np.max(np.abs(want))
+
+
+def test_errors_and_edge_cases():
+    from suqa_gb300 import SqError, SqUnsupported, State
+    with State(4) as s:
+        with pytest.raises(SqError):
+            s.apply_x(4)
+        s.activate_gc_mask([1])
+        with pytest.raises(SqError):
+            s.apply_h(1)  # target inside the global control mask
+        s.deactivate_gc_mask([1])
+        with pytest.raises(SqUnsupported):
+            s.apply_pauli_TP_rotation([0, 1, 2], [1, 2, 3], 0.3)
+        with pytest.raises(RuntimeError):
+            s.apply_phase_list(0, 2, [0.1, 0.2, 0.3])
+        before = s.get_state()
+        s.apply_phase_list(0, 2, [0.1, 0.2, 0.3, 0.4])  # gc == 0: reference no-op
+        assert np.array_equal(s.get_state(), before)
+        assert abs(s.vnorm() - 1.0) < 1e-15
+    for n in (1, 2):
+        for prec in ("f64", "f32"):
+            with State(n, prec) as s:
+                s.apply_h(0)
+                s.apply_pauli_rotation([0], [2], 0.4)
+                st = s.get_state()
+                assert abs(np.linalg.norm(st) - 1.0) < 1e-6
+
+
+def test_wide_pauli_strings_cross_tiles():
+    """Pauli strings with 6-11 flipped qubits spread over a 20-qubit state."""
+    rng = np.random.default_rng(21)
+    lines = ["setup 20"] + [f"h {q}" for q in range(20)] + [f"u1 {q} {circuits.hx(0.1 * q + 0.05)}" for q in range(20)]
+    for k in (6, 8, 11):
+        qs = [int(q) for q in rng.choice(20, size=k, replace=False)]
+        ps = [int(p) for p in rng.integers(1, 3, size=k)]
+        lines.append(f"ptpg {k} " + " ".join(map(str, qs)) + " " + " ".join(map(str, ps)) + f" {circuits.hx(0.37 * k)}")
+        lines.append("dump")
+    golden_io.compare_results(gpu_script.run_script(lines), oracle.run_script(lines, threads=8), rtol=RTOL64)
+
+
+def test_fusion_counts_fewer_passes():
+    from suqa_gb300 import State
+    with State(22) as s:
+        rng = np.random.default_rng(1)
+        for _ in range(200):
+            s.apply_h(int(rng.integers(0, 22)))
+        s.synchronize()
+        st = s.stats()
+    assert st["gates"] == 200
+    assert st["passes"] < 60

@@ -243,7 +243,7 @@ def main():
     barrier()
     ms_e2e = e2.elapsed_time(e3) / args.steps
     e2e_value = alg * world / (ms_e2e / 1e3) / 1e9
-    state_bytes = (1 << n) * bpa
+    state_bytes = (1 << n) * bpa  # re + im
 
     peaks = {}
     try:
@@ -273,13 +273,13 @@ def main():
                                        f"(X, H, CX, MCX 2-4 controls, U1, Pauli rotations on 2-6 qubits), "
                                        f"measure every 100; seed 7",
                            "n_qubits": n, "gates": args.gates, "fusion": not args.no_fusion,
-                           "parallelism": f"replicas x{world}", "l2": "state (%d MiB) larger than L2" % (2 * state_bytes >> 20)},
+                           "parallelism": f"replicas x{world}", "l2": "state (%d MiB) larger than L2" % (state_bytes >> 20)},
                 "gates_per_s": (len([g for g in gates if g[0] != 'measure']) * world) / (ms_step / 1e3),
                 "passes_per_step": stats["passes"] / args.steps,
                 "gpu_launches": stats["launches"],
                 "clocks": clk.summary(),
                 "e2e": {"value": e2e_value, "unit": "GB/s", "ms_per_step": ms_e2e,
-                        "h2d_bytes_per_step": 2 * state_bytes, "d2h_bytes_per_step": 2 * state_bytes},
+                        "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes},
                 "roofline": roofline,
                 "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)

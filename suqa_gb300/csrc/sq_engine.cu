@@ -96,8 +96,14 @@ template <typename T>
 int launch_pass_t(sq_state* s, const sqk::PassArgs& a, const sqk::Prog& p, int grid, int block, size_t smem) {
     static int configured_smem = -1;
     if ((int)smem > 48 * 1024 && configured_smem < (int)smem) {
-        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-        configured_smem = 227 * 1024;
+        int optin = 0;
+        cudaFuncAttributes fa;
+        SQ_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
+        SQ_CUDA(cudaFuncGetAttributes(&fa, sqk::k_pass<T>));
+        const int dyn = optin - (int)fa.sharedSizeBytes;
+        if ((int)smem > dyn) return fail(SQ_ERR_UNSUPPORTED, "tile does not fit in shared memory");
+        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+        configured_smem = dyn;
     }
     sqk::k_pass<T><<<grid, block, smem, s->stream>>>(a, p);
     SQ_CUDA(cudaGetLastError());

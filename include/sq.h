@@ -135,6 +135,24 @@ int sq_reset_stats(sq_state* s);
 int sq_set_timing(sq_state* s, int enabled);
 int sq_kernel_time(sq_state* s, double* ms, uint64_t* launches, uint64_t* bytes);
 
+/* --- allocation-free measurement probabilities (no counterpart in the reference) ---
+ * For callers that may not allocate device memory on the call path: their host
+ * application's memory manager owns all device buffers, or they are a plugin
+ * handed raw device pointers by another runtime, or an allocation's latency and
+ * implicit synchronisation are unacceptable.  Computes p0 and p1 of qubit q
+ * (sum of |a_i|^2 over i with bit q clear / set, reduced in FP64) of a state the
+ * caller owns (re, im: device arrays of 2^n doubles for SQ_F64 or floats for
+ * SQ_F32) and writes them to out_p01 (device memory, 2 doubles), on the given
+ * CUDA stream (NULL = legacy default stream), without allocating anything.
+ * The scratch is one static device array (partial sums of at most 4096 CTAs,
+ * 64 KiB + 256 B, resident on every GPU that loads the library until exit);
+ * launches needing more are rejected with SQ_ERR_ARG.  All calls share it:
+ * calls whose kernels overlap on the GPU race; calls ordered on one stream are
+ * safe.  The first call on a device performs a one-time set-up on it and
+ * should come before any stream capture. */
+int sq_qubit_probs_noalloc(const void* re, const void* im, uint32_t n, int precision, uint32_t q,
+                           double* out_p01, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -65,6 +65,8 @@ _SIGS = {
     "sq_reset_stats": (C.c_int, [C.c_void_p]),
     "sq_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "sq_kernel_time": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "sq_qubit_probs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_uint32, C.c_void_p,
+                                         C.c_void_p]),
 }
 
 EXPORTED = tuple(_SIGS)

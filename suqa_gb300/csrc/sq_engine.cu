@@ -43,6 +43,11 @@ inline int popc(uint64_t x) { return __builtin_popcountll(x); }
 
 }  // namespace
 
+// error text shared with the other translation units of libsq
+namespace sqi {
+void set_error(const char* msg) { g_err = msg; }
+}  // namespace sqi
+
 struct sq_state {
     uint32_t n = 0;
     int prec = SQ_F64;

@@ -321,6 +321,109 @@ static void pauli_range(void* cx, uint64_t lo, uint64_t hi, int tid) {
     }
 }
 
+
+/* Literal restatement of the reference's dense Pauli loops
+ * (include/suqa_cpu.hpp:338-527, dispatch src/suqa.cu:467-581), used in strict
+ * mode so that the oracle also reproduces the reference when the global control
+ * mask overlaps the rotated qubits (the loops then alias elements). */
+static inline void rot2(double* a, double* b, double c, double s) {
+    double cpy = *a;
+    *a = cpy * c - (*b) * s;
+    *b = (*b) * c + cpy * s;
+}
+static inline void rot4(double* a, double* b, double* c2, double* d, double c, double s) {
+    rot2(a, b, c, s);
+    rot2(c2, d, c, s);
+}
+static void ref_pauli1(uint32_t p1, double* re, double* im, uint64_t m0, uint64_t m1, uint64_t mq1, double c,
+                       double s, uint64_t N) {
+    for (uint64_t i0 = 0; i0 < N; ++i0) {
+        if ((i0 & m1) != m0) continue;
+        uint64_t i[2] = {i0, i0 | mq1};
+        switch (p1) {
+        case 1: rot4(&re[i[0]], &im[i[1]], &re[i[1]], &im[i[0]], c, s); break;
+        case 2: rot4(&re[i[0]], &re[i[1]], &im[i[0]], &im[i[1]], c, -s); break;
+        case 3: rot4(&re[i[0]], &im[i[0]], &im[i[1]], &re[i[1]], c, s); break;
+        }
+    }
+}
+static void ref_pauli2(uint32_t p1, uint32_t p2, double* re, double* im, uint64_t m0, uint64_t m1, uint64_t mq1,
+                       uint64_t mq2, double c, double s, uint64_t N) {
+    for (uint64_t i0 = 0; i0 < N; ++i0) {
+        if ((i0 & m1) != m0) continue;
+        uint64_t i[4];
+        i[0] = i0; i[1] = i0 | mq1; i[2] = i0 | mq2; i[3] = i[2] | i[1];
+        if (p1 == 1 && p2 == 1) {
+            rot4(&re[i[0]], &im[i[3]], &re[i[3]], &im[i[0]], c, s);
+            rot4(&re[i[1]], &im[i[2]], &re[i[2]], &im[i[1]], c, s);
+        } else if (p1 == 2 && p2 == 2) {
+            rot4(&re[i[0]], &im[i[3]], &re[i[3]], &im[i[0]], c, -s);
+            rot4(&re[i[1]], &im[i[2]], &re[i[2]], &im[i[1]], c, s);
+        } else if (p1 == 3 && p2 == 3) {
+            rot4(&re[i[0]], &im[i[0]], &re[i[3]], &im[i[3]], c, s);
+            rot4(&re[i[1]], &im[i[1]], &re[i[2]], &im[i[2]], c, -s);
+        } else if (p1 == 1 && p2 == 2) {
+            rot4(&re[i[0]], &re[i[3]], &im[i[0]], &im[i[3]], c, -s);
+            rot4(&re[i[2]], &re[i[1]], &im[i[2]], &im[i[1]], c, -s);
+        } else if (p1 == 1 && p2 == 3) {
+            rot4(&re[i[0]], &im[i[1]], &re[i[1]], &im[i[0]], c, s);
+            rot4(&re[i[2]], &im[i[3]], &re[i[3]], &im[i[2]], c, -s);
+        } else if (p1 == 2 && p2 == 3) {
+            rot4(&re[i[0]], &re[i[1]], &im[i[0]], &im[i[1]], c, -s);
+            rot4(&re[i[2]], &re[i[3]], &im[i[2]], &im[i[3]], c, s);
+        }
+    }
+}
+static void ref_pauli3(uint32_t p2, double* re, double* im, uint64_t m0, uint64_t m1, uint64_t mq1,
+                       uint64_t mq2, uint64_t mq3, double c, double s, uint64_t N) {
+    for (uint64_t i0 = 0; i0 < N; ++i0) {
+        if ((i0 & m1) != m0) continue;
+        uint64_t i[8];
+        i[0] = i0; i[1] = i0 | mq1; i[2] = i0 | mq2; i[3] = i[2] | i[1];
+        i[4] = i0 | mq3; i[5] = i[4] | i[1]; i[6] = i[4] | i[2]; i[7] = i[4] | i[3];
+        if (p2 == 1) {
+            rot4(&re[i[0]], &im[i[3]], &re[i[3]], &im[i[0]], c, s);
+            rot4(&re[i[1]], &im[i[2]], &re[i[2]], &im[i[1]], c, s);
+            rot4(&re[i[4]], &im[i[7]], &re[i[7]], &im[i[4]], c, -s);
+            rot4(&re[i[5]], &im[i[6]], &re[i[6]], &im[i[5]], c, -s);
+        } else if (p2 == 2) {
+            rot4(&re[i[0]], &im[i[3]], &re[i[3]], &im[i[0]], c, -s);
+            rot4(&re[i[1]], &im[i[2]], &re[i[2]], &im[i[1]], c, s);
+            rot4(&re[i[4]], &im[i[7]], &re[i[7]], &im[i[4]], c, s);
+            rot4(&re[i[5]], &im[i[6]], &re[i[6]], &im[i[5]], c, -s);
+        } else {
+            rot4(&re[i[0]], &im[i[0]], &re[i[3]], &im[i[3]], c, s);
+            rot4(&re[i[5]], &im[i[5]], &re[i[6]], &im[i[6]], c, s);
+            rot4(&re[i[1]], &im[i[1]], &re[i[2]], &im[i[2]], c, -s);
+            rot4(&re[i[4]], &im[i[4]], &re[i[7]], &im[i[7]], c, -s);
+        }
+    }
+}
+static int ref_pauli(or_state* st, uint32_t k, const uint32_t* qubits, const uint32_t* paulis, double phase,
+                     uint64_t gc) {
+    double sph, cph;
+    sincos(phase, &sph, &cph);
+    uint64_t m0 = gc, m1 = gc;
+    for (uint32_t t = 0; t < k; ++t) m1 |= 1ULL << qubits[t];
+    uint32_t p[3] = {0, 0, 0}, q[3] = {0, 0, 0};
+    for (uint32_t t = 0; t < k; ++t) { p[t] = paulis[t]; q[t] = qubits[t]; }
+    uint32_t tt;
+#define OR_SWAP2(a, b) do { tt = p[a]; p[a] = p[b]; p[b] = tt; tt = q[a]; q[a] = q[b]; q[b] = tt; } while (0)
+    if (k == 1) {
+        ref_pauli1(p[0], st->re, st->im, m0, m1, 1ULL << q[0], cph, sph, st->N);
+    } else if (k == 2) {
+        if (p[0] > p[1]) OR_SWAP2(0, 1);
+        ref_pauli2(p[0], p[1], st->re, st->im, m0, m1, 1ULL << q[0], 1ULL << q[1], cph, sph, st->N);
+    } else {
+        if (p[0] > p[1]) OR_SWAP2(0, 1);
+        if (p[1] > p[2]) OR_SWAP2(1, 2);
+        if (p[0] > p[1]) OR_SWAP2(0, 1);
+        ref_pauli3(p[0], st->re, st->im, m0, m1, 1ULL << q[0], 1ULL << q[1], 1ULL << q[2], cph, sph, st->N);
+    }
+#undef OR_SWAP2
+    return 0;
+}
+
 /* supported set of the reference: src/suqa.cu:484-581 */
 static int ref_supported(uint32_t k, const uint32_t* ps) {
     if (k == 1 || k == 2) return 1;
@@ -338,6 +441,11 @@ int or_apply_pauli(or_state* s, uint32_t k, const uint32_t* qubits, const uint32
                    double phase, uint64_t gc, int strict) {
     if (k == 0 || k > 64) return -1;
     if (strict && !ref_supported(k, paulis)) return -1;
+    if (strict) {
+        uint64_t qm = 0;
+        for (uint32_t t = 0; t < k; ++t) qm |= 1ULL << qubits[t];
+        if (qm & gc) return ref_pauli(s, k, qubits, paulis, phase, gc);
+    }
     pauli_ctx p;
     memset(&p, 0, sizeof(p));
     p.re = s->re; p.im = s->im; p.gc = gc;

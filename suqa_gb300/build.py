@@ -70,8 +70,45 @@ def build_libsq(force=False):
     return lib
 
 
+CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-w", "-I" + SHIM_INCLUDE, "-I" + INCLUDE]
+DRIVERS = ["qms", "qsa", "evo"]
+
+
+def cxx():
+    return shutil.which("g++") or "g++"
+
+
+def build_dropin(force=False):
+    """The suqa:: shim, the triangle system plugin and the qms/qsa/evo drivers
+    (C++ over libsq)."""
+    headers = [os.path.join(SHIM_INCLUDE, f) for f in os.listdir(SHIM_INCLUDE)] + [os.path.join(INCLUDE, "sq.h")]
+    units = {"suqa_shim": os.path.join(PKG, "shim", "suqa_shim.cpp"),
+             "triangle": os.path.join(PKG, "systems", "triangle.cpp")}
+    for d in DRIVERS:
+        units["app_" + d] = os.path.join(PKG, "apps", d + ".cpp")
+    jobs, objs = [], {}
+    for name, src in units.items():
+        o = os.path.join(BUILD, name + ".o")
+        objs[name] = o
+        if force or not _newer(o, [src] + headers):
+            jobs.append([cxx()] + CXX_FLAGS + ["-c", src, "-o", o])
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
+        list(ex.map(_run, jobs))
+    lib = os.path.join(BUILD, "libsq.so")
+    outs = []
+    for d in DRIVERS:
+        exe = os.path.join(BUILD, d)
+        deps = [objs["app_" + d], objs["suqa_shim"], objs["triangle"], lib]
+        if force or jobs or not _newer(exe, deps):
+            _run([cxx(), objs["app_" + d], objs["suqa_shim"], objs["triangle"], "-L" + BUILD, "-lsq",
+                  "-Wl,-rpath," + BUILD, "-o", exe])
+        outs.append(exe)
+    return outs
+
+
 def build_all(force=False):
     lib = build_libsq(force)
+    build_dropin(force)
     return lib
 
 

@@ -510,18 +510,31 @@ int sq_vnormalize(sq_state* s) {
     return enqueue(s, std::move(h));
 }
 
+// A global control mask may contain the gate's own qubits (the reference's QSA
+// does this through aliased registers).  The reference loops then have definite
+// semantics, reproduced here: X and Y act on the pair controlled by the other
+// gc bits (include/suqa_cpu.hpp:69-122), H zeroes the amplitudes where every gc
+// bit is set (its two output writes alias, :150-206).
 static int pair_op(sq_state* s, uint8_t kind, uint32_t q, uint64_t gc) {
     int rc = check_q(s, q);
     if (rc || (rc = check_mask(s, gc))) return rc;
     const uint64_t b = 1ull << q;
-    if (gc & b) return fail(SQ_ERR_ARG, "global control mask overlaps the target qubit");
     HostOp h;
+    if ((gc & b) && kind == sqk::OP_HP) {
+        h.kind = sqk::OP_PHASE;  // multiply by 0 + 0i
+        h.cmask = gc;
+        h.cval = gc;
+        h.skm = gc;
+        h.skv = gc;
+        return enqueue(s, std::move(h));
+    }
+    const uint64_t g = gc & ~b;
     h.kind = kind;
     h.flip = b;
-    h.cmask = gc;
-    h.cval = gc;
-    h.skm = gc;
-    h.skv = gc;
+    h.cmask = g;
+    h.cval = g;
+    h.skm = g;
+    h.skv = g;
     return enqueue(s, std::move(h));
 }
 
@@ -529,11 +542,22 @@ int sq_apply_x(sq_state* s, uint32_t q, uint64_t gc) { return pair_op(s, sqk::OP
 int sq_apply_y(sq_state* s, uint32_t q, uint64_t gc) { return pair_op(s, sqk::OP_YP, q, gc); }
 int sq_apply_h(sq_state* s, uint32_t q, uint64_t gc) { return pair_op(s, sqk::OP_HP, q, gc); }
 
+static int phase_op(sq_state* s, uint64_t cmask, uint64_t cval, double c, double sn) {
+    HostOp h;
+    h.kind = sqk::OP_PHASE;
+    h.cmask = cmask;
+    h.cval = cval;
+    h.skm = cmask;
+    h.skv = cval;
+    h.c = c;
+    h.s = sn;
+    return enqueue(s, std::move(h));
+}
+
 int sq_apply_u1(sq_state* s, uint32_t q, uint32_t q_mask, double phase, uint64_t gc) {
     int rc = check_q(s, q);
     if (rc || (rc = check_mask(s, gc))) return rc;
     const uint64_t b = 1ull << q;
-    if (gc & b) return fail(SQ_ERR_ARG, "global control mask overlaps the target qubit");
     // src/suqa.cu:271-285: condition (i & (gc | 1<<q)) == gc | (q_mask << q)
     HostOp h;
     h.kind = sqk::OP_PHASE;
@@ -549,15 +573,17 @@ int sq_apply_mcx(sq_state* s, uint64_t control_mask, uint64_t mask_qs, uint32_t 
     int rc = check_q(s, q_target);
     if (rc || (rc = check_mask(s, control_mask)) || (rc = check_mask(s, mask_qs))) return rc;
     const uint64_t b = 1ull << q_target;
-    if ((control_mask & b) || (mask_qs & b)) return fail(SQ_ERR_ARG, "control mask contains the target");
     if (mask_qs & ~control_mask) return fail(SQ_ERR_ARG, "mask_qs has bits outside control_mask");
+    // the reference adds the target bit to both masks (include/suqa_cpu.hpp:237-238) and
+    // tests the element with the target set; on the pair's lower element that is the
+    // condition without the target bit
     HostOp h;
     h.kind = sqk::OP_SWAPP;
     h.flip = b;
-    h.cmask = control_mask;
-    h.cval = mask_qs;
-    h.skm = control_mask;
-    h.skv = mask_qs;
+    h.cmask = control_mask & ~b;
+    h.cval = mask_qs & ~b;
+    h.skm = h.cmask;
+    h.skv = h.cval;
     return enqueue(s, std::move(h));
 }
 
@@ -580,11 +606,26 @@ int sq_apply_swap(sq_state* s, uint32_t q1, uint32_t q2, uint64_t gc) {
     if (rc || (rc = check_q(s, q2)) || (rc = check_mask(s, gc))) return rc;
     if (q1 == q2) return fail(SQ_ERR_ARG, "swap of a qubit with itself");
     const uint64_t b1 = 1ull << q1, b2 = 1ull << q2;
-    if (gc & (b1 | b2)) return fail(SQ_ERR_ARG, "global control mask overlaps the swapped qubits");
+    HostOp h;
+    if (gc & (b1 | b2)) {
+        // reference loop (include/suqa_cpu.hpp:299-311) with a swapped qubit inside gc:
+        // it exchanges the other qubit where every gc bit is set; both inside: nothing
+        const uint64_t freeb = (b1 | b2) & ~gc;
+        if (!freeb) {
+            s->stats.gates++;
+            return SQ_OK;
+        }
+        h.kind = sqk::OP_SWAPP;
+        h.flip = freeb;
+        h.cmask = gc;
+        h.cval = gc;
+        h.skm = gc;
+        h.skv = gc;
+        return enqueue(s, std::move(h));
+    }
     // pairs (i|b1, i|b2) for (i & (gc|b1|b2)) == gc: the pair's lower-bit element has
     // the higher bit set
     const uint64_t bhi = b1 > b2 ? b1 : b2;
-    HostOp h;
     h.kind = sqk::OP_SWAPP;
     h.flip = b1 | b2;
     h.cmask = gc | bhi;
@@ -654,7 +695,48 @@ int sq_apply_pauli_rotation(sq_state* s, uint32_t k, const uint32_t* qubits, con
         if (pl[t] == 2 || pl[t] == 3) h.zy |= b;
         if (pl[t] == 2) h.ny++;
     }
-    if (gc & seen) return fail(SQ_ERR_ARG, "global control mask overlaps the rotated qubits");
+    if (gc & seen) {
+        if (!refmode) return fail(SQ_ERR_ARG, "global control mask overlaps the rotated qubits");
+        // Reference loops with the global control on a rotated qubit
+        // (include/suqa_cpu.hpp:338-527): their element pointers alias.  One qubit:
+        // X applies e^{i phase} twice, Z applies e^{i phase} then e^{-i phase}, on the
+        // elements with every gc bit set.  X(x)X with one qubit in gc applies
+        // exp(i phase X) twice to the other qubit under gc; with both in gc it applies
+        // e^{i phase} four times.  Other aliased patterns are not reproduced.
+        double sn, cs;
+        sincos(phase, &sn, &cs);
+        if (k == 1 && pl[0] == 1) {
+            if ((rc = phase_op(s, gc, gc, cs, sn))) return rc;
+            return phase_op(s, gc, gc, cs, sn);
+        }
+        if (k == 1 && pl[0] == 3) {
+            if ((rc = phase_op(s, gc, gc, cs, sn))) return rc;
+            return phase_op(s, gc, gc, cs, -sn);
+        }
+        if (k == 2 && pl[0] == 1 && pl[1] == 1) {
+            const uint64_t freeb = seen & ~gc;
+            if (!freeb) {
+                for (int r = 0; r < 4; ++r)
+                    if ((rc = phase_op(s, gc, gc, cs, sn))) return rc;
+                return SQ_OK;
+            }
+            for (int r = 0; r < 2; ++r) {
+                HostOp x;
+                x.kind = sqk::OP_PAULI;
+                x.flip = freeb;
+                x.cmask = gc;
+                x.cval = gc;
+                x.skm = gc;
+                x.skv = gc;
+                x.c = cs;
+                x.s = sn;
+                if ((rc = enqueue(s, std::move(x)))) return rc;
+            }
+            return SQ_OK;
+        }
+        return fail(SQ_ERR_UNSUPPORTED, "Pauli rotation with the global control on a rotated qubit "
+                                        "(only X, Z and X(x)X reproduce the reference)");
+    }
     // pair ops test the control on g0 (lowest flipped bit clear); diagonal ops on g
     h.cmask = gc;
     h.cval = gc;

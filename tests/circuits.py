@@ -31,10 +31,12 @@ def _ref_supported_ptp(ps):
 
 def random_script(seed: int, n: int, ngates: int, *, reference_only: bool = True,
                   with_gc: bool = True, measure_every: int = 7, random_init: bool = True,
-                  dump_every: int = 5):
+                  dump_every: int = 5, overlap: str = "none"):
     """A script over n qubits.  reference_only keeps to the gate patterns the
     reference supports (its CPU build throws on other Pauli strings and has no
-    phase-list symbol)."""
+    phase-list symbol).  overlap="all" lets gate qubits fall inside the global
+    control mask (the reference then follows its loops' aliasing semantics);
+    overlap="engine" restricts that to the patterns libsq reproduces."""
     rng = np.random.default_rng(seed)
     lines = [f"setup {n}"]
     if random_init:
@@ -62,6 +64,34 @@ def random_script(seed: int, n: int, ngates: int, *, reference_only: bool = True
         if len(free) < 2:
             continue
         kind = kinds[int(rng.integers(len(kinds)))]
+        if overlap != "none" and gc_on and rng.random() < 0.5:
+            # a gate acting on a qubit of the global control mask
+            q0 = int(rng.choice(gc_on))
+            other = int(rng.choice(free))
+            ph = hx(rng.uniform(-2 * math.pi, 2 * math.pi))
+            opts = ["x", "y", "h", "u1", "cx", "swap", "ptp1", "xx"]
+            if overlap == "all":
+                opts += ["ptp2"]
+            k = opts[int(rng.integers(len(opts)))]
+            if k in ("x", "y", "h"):
+                lines.append(f"{k} {q0}")
+            elif k == "u1":
+                lines.append(f"u1m {q0} {int(rng.integers(2))} {ph}")
+            elif k == "cx":
+                lines.append(f"cx {other} {q0} 1")
+            elif k == "swap":
+                lines.append(f"swap {q0} {other}" if rng.random() < 0.5 else f"swap {other} {q0}")
+            elif k == "ptp1":
+                pz = int(rng.integers(1, 4)) if overlap == "all" else [1, 3][int(rng.integers(2))]
+                lines.append(f"ptp 1 {q0} {pz} {ph}")
+            elif k == "xx":
+                pair = [q0, other] if rng.random() < 0.5 else [other, q0]
+                if len(gc_on) > 1 and rng.random() < 0.3:
+                    pair = list(gc_on[:2])
+                lines.append(f"ptp 2 {pair[0]} {pair[1]} 1 1 {ph}")
+            else:
+                lines.append(f"ptp 2 {q0} {other} {int(rng.integers(1, 4))} {int(rng.integers(1, 4))} {ph}")
+            continue
         ph = hx(rng.uniform(-2 * math.pi, 2 * math.pi))
         pick = lambda k: [int(q) for q in rng.choice(free, size=k, replace=False)]
         if kind in ("x", "y", "z", "h", "s", "t", "tdg"):

@@ -35,6 +35,9 @@ REF = os.path.join(ROOT, "oracle", "_ref")
 
 # (name, seed, n, ngates, dump_every) — n up to 12 so the GPU tile path is exercised
 GATE_CASES = [(f"rand{s}", s, 3 + s % 10, 60, 5) for s in range(36)]
+# scripts whose gates may act on qubits of the global control mask (the patterns
+# the reference's QSA produces through its aliased registers)
+OVERLAP_CASES = [(f"ovl{s}", 900 + s, 4 + s % 6, 60) for s in range(10)]
 
 RUNS = [
     # config 1: the triangle, 3 + 4 + 1 = 8 qubits
@@ -70,6 +73,18 @@ def gate_fixtures():
         for name, seed, n, ng, _ in GATE_CASES:
             lines = circuits.random_script(seed, n, ng, random_init=n <= 8,
                                            dump_every=5 if n <= 8 else 30)
+            res = oracle.run_reference(lines, d)
+            blocks.append(f"## {name}\n" + "\n".join(lines))
+            kinds = []
+            for k, (kind, val) in enumerate(res):
+                kinds.append(kind)
+                if kind == "S":
+                    arrays[f"{name}__{k}"] = val
+                elif kind in ("M", "P", "N"):
+                    arrays[f"{name}__{k}"] = np.array([val], dtype=np.float64)
+            meta.append({"name": name, "kinds": "".join(kinds)})
+        for name, seed, n, ng in OVERLAP_CASES:
+            lines = circuits.random_script(seed, n, ng, overlap="engine", dump_every=6)
             res = oracle.run_reference(lines, d)
             blocks.append(f"## {name}\n" + "\n".join(lines))
             kinds = []

@@ -134,3 +134,12 @@ def test_fusion_counts_fewer_passes():
         st = s.stats()
     assert st["gates"] == 200
     assert st["passes"] < 60
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_overlapping_global_control_vs_oracle(seed):
+    """Gates acting on qubits of the global control mask follow the reference
+    loops' semantics (the oracle restates them literally)."""
+    n = 4 + seed % 9
+    lines = circuits.random_script(2000 + seed, n, 80, overlap="engine", dump_every=8)
+    golden_io.compare_results(gpu_script.run_script(lines), oracle.run_script(lines), rtol=RTOL64)

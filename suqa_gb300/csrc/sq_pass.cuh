@@ -247,10 +247,11 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                         sre[t] = ar * cx - ai * cy;
                         sim[t] = ar * cy + ai * cx;
                     } else if (kind == OP_COLLAPSE) {
-                        // src/suqa.cu:664-696: zero the discarded branch, rescale the kept one
+                        // src/suqa.cu:664-696: zero the discarded branch, rescale everything
+                        // (a zero state gives 0 * inf = NaN everywhere, like the reference)
                         const bool keep = (g & op.cmask) == op.cval;
-                        sre[t] = keep ? ar * s : (T)0;
-                        sim[t] = keep ? ai * s : (T)0;
+                        sre[t] = (keep ? ar : (T)0) * s;
+                        sim[t] = (keep ? ai : (T)0) * s;
                     } else {  // OP_SCALE
                         sre[t] = ar * s;
                         sim[t] = ai * s;

@@ -135,6 +135,41 @@ int sq_reset_stats(sq_state* s);
 int sq_set_timing(sq_state* s, int enabled);
 int sq_kernel_time(sq_state* s, double* ms, uint64_t* launches, uint64_t* bytes);
 
+/* --- batched quantum Metropolis sampling: many independent chains on the device ---
+ * No single reference function: each chain is one run of the reference's qms
+ * driver (src/qms.cu:51-178, include/qms.cuh:373-545) for a transverse-field
+ * Ising ring plugin, H = -J sum Z_i Z_{i+1} - h sum X_i (ring of `spins`),
+ * exp(-iHt) by ceil(|t|/dt) first-order Trotter steps (bond phases, then X
+ * rotations), moves = Hadamard on a uniformly drawn spin, observable = Z-basis
+ * magnetisation.  Register layout: spins, energy register, acceptance qubit. */
+typedef struct sq_tfim_chain {
+    uint32_t spins;           /* ring length s (system qubits) */
+    uint32_t ene_qbits;       /* energy register width e */
+    uint32_t steps;           /* Metropolis steps */
+    uint32_t thermalization;  /* sampling starts after this many steps */
+    uint32_t reset_each;      /* sample every reset_each steps */
+    uint32_t max_reverse;     /* restoration attempts (the reference default is 100) */
+    double J, h, beta;
+    double ene_min, ene_max;  /* phase-estimation window */
+    double dt;                /* Trotter step width */
+    uint64_t seed;            /* PCG32 seed, stream 1 (as pcg::set_seed) */
+} sq_tfim_chain;
+
+typedef struct sq_chain_result {
+    uint32_t accepted;        /* steps returning 1 or 2 */
+    uint32_t failures;        /* failed restorations (state re-initialised) */
+    uint32_t samples;         /* (E, A) samples written */
+    uint32_t pad;
+} sq_chain_result;
+
+/* Runs every chain to completion on the current device (one persistent launch per
+ * chain-size class).  Host arrays: results[nchains]; samples_E/A/step (may be
+ * NULL) hold sum(steps) entries, chain i's samples starting at the sum of the
+ * steps of chains 0..i-1 (E = energy reading, A = magnetisation, step = step
+ * index).  kernel_ms (may be NULL) receives the device time of the launches. */
+int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, int precision, sq_chain_result* results,
+                      double* samples_E, double* samples_A, uint32_t* samples_step, void* stream, float* kernel_ms);
+
 /* --- allocation-free measurement probabilities (no counterpart in the reference) ---
  * For callers that may not allocate device memory on the call path: their host
  * application's memory manager owns all device buffers, or they are a plugin

@@ -28,6 +28,17 @@ class SqStats(C.Structure):
                 ("reductions", C.c_uint64), ("bytes_moved", C.c_uint64)]
 
 
+class SqTfimChain(C.Structure):
+    _fields_ = [("spins", C.c_uint32), ("ene_qbits", C.c_uint32), ("steps", C.c_uint32),
+                ("thermalization", C.c_uint32), ("reset_each", C.c_uint32), ("max_reverse", C.c_uint32),
+                ("J", C.c_double), ("h", C.c_double), ("beta", C.c_double), ("ene_min", C.c_double),
+                ("ene_max", C.c_double), ("dt", C.c_double), ("seed", C.c_uint64)]
+
+
+class SqChainResult(C.Structure):
+    _fields_ = [("accepted", C.c_uint32), ("failures", C.c_uint32), ("samples", C.c_uint32), ("pad", C.c_uint32)]
+
+
 _lib = None
 
 _SIGS = {
@@ -65,6 +76,8 @@ _SIGS = {
     "sq_reset_stats": (C.c_int, [C.c_void_p]),
     "sq_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "sq_kernel_time": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "sq_qms_tfim_batch": (C.c_int, [C.POINTER(SqTfimChain), C.c_uint32, C.c_int, C.POINTER(SqChainResult),
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_float)]),
     "sq_qubit_probs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_uint32, C.c_void_p,
                                          C.c_void_p]),
 }

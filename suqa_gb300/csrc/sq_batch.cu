@@ -1,0 +1,665 @@
+// Batched quantum Metropolis sampling of transverse-field Ising rings, one chain
+// per CTA, entirely on the device.
+//
+// System: H = -J sum_i Z_i Z_{i+1} - h sum_i X_i on a ring of s spins; exp(-iHt)
+// as ceil(|t|/dt) first-order Trotter steps of width d = t/steps, each the ZZ
+// bond phases exp(i J d Z_i Z_{i+1}) then exp(i h d X_i) on every spin; moves:
+// Hadamard on spin i with probability 1/s; observable: magnetisation read in
+// the Z basis.  The register layout, the QMS step (reset, phase estimation,
+// move, acceptance oracle W, accept / restore loop, sampling branch) and the
+// order of every PCG32 draw restate the reference's include/qms.cuh:128-545 and
+// the driver loop of src/qms.cu:114-149, so each chain reproduces the reference
+// CPU `qms` binary built with the same system (measured outcomes identical,
+// amplitudes to rounding).
+//
+// GB300 mapping: a persistent grid of CTAs pulls chains from an atomic work
+// counter (largest first); a chain's 2^n amplitudes stay in shared memory for
+// its whole run (n <= 13 FP64 / 14 FP32; larger chains use a per-CTA buffer in
+// global memory that stays L2-resident); gates are CTA-wide sweeps with no
+// kernel launches and no host round trips; measurement probabilities are FP64
+// block reductions; the bond phases of a Trotter step are applied as one
+// diagonal (their product depends only on the number of domain walls).
+#include <cmath>
+#include <cstdint>
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sq.h"
+
+namespace sqi {
+void set_error(const char* msg);
+}
+
+namespace sqb {
+
+constexpr int kThreads = 512;
+
+struct DevChain {
+    int s, e, n, steps, therm, reset_each, max_reverse;
+    double J, h, beta, dt;
+    double t_pe, t_shift, pe_factor, c_factor;  // as the reference driver computes them
+    uint64_t seed;
+    int out_offset;  // first sample slot of this chain
+};
+
+struct Shared {
+    double red[2][32];
+    double bcast_d[4];
+    int bcast_i[4];
+    uint64_t rng_state, rng_inc;
+};
+
+__device__ __forceinline__ uint32_t pcg_next(Shared& sh) {
+    const uint64_t old = sh.rng_state;
+    sh.rng_state = old * 6364136223846793005ULL + sh.rng_inc;
+    const uint32_t x = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    const uint32_t rot = (uint32_t)(old >> 59u);
+    return (x >> rot) | (x << ((0u - rot) & 31u));
+}
+
+__device__ __forceinline__ double pcg_doub(Shared& sh) {
+    const uint64_t bits = ((uint64_t)pcg_next(sh) << 20) | 0x3ff0000000000000ULL;
+    return __longlong_as_double((long long)bits) - 1.0;
+}
+
+__device__ __forceinline__ void pcg_seed(Shared& sh, uint64_t s) {
+    sh.rng_state = 0U;
+    sh.rng_inc = (1ull << 1u) | 1u;
+    pcg_next(sh);
+    sh.rng_state += s;
+    pcg_next(sh);
+}
+
+__device__ __forceinline__ uint32_t ins0(uint32_t p, uint32_t b) {
+    return ((p >> b) << (b + 1u)) | (p & ((1u << b) - 1u));
+}
+
+// index p of the subspace with bit q = 0 and (if c >= 0) bit c = 1
+__device__ __forceinline__ uint32_t pair_idx(uint32_t p, int q, int c) {
+    if (c < 0) return ins0(p, (uint32_t)q);
+    const uint32_t lo = q < c ? (uint32_t)q : (uint32_t)c, hi = q < c ? (uint32_t)c : (uint32_t)q;
+    return ins0(ins0(p, lo), hi) | (1u << c);
+}
+
+template <typename T>
+struct Ctx {
+    T* re;
+    T* im;
+    int n;
+    uint32_t N;
+    Shared* sh;
+
+    __device__ void sync() const { __syncthreads(); }
+
+    __device__ void init() {
+        for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
+            re[i] = (T)0;
+            im[i] = (T)0;
+        }
+        sync();
+        if (threadIdx.x == 0) re[0] = (T)1;
+        sync();
+    }
+
+    // Hadamard on q, optionally controlled on bit c
+    __device__ void h(int q, int c) {
+        const uint32_t cnt = c < 0 ? N / 2 : N / 4;
+        const T k = (T)0.7071067811865475;
+        for (uint32_t p = threadIdx.x; p < cnt; p += blockDim.x) {
+            const uint32_t i0 = pair_idx(p, q, c), i1 = i0 | (1u << q);
+            const T a0r = re[i0], a0i = im[i0], a1r = re[i1], a1i = im[i1];
+            re[i0] = k * (a0r + a1r);
+            im[i0] = k * (a0i + a1i);
+            re[i1] = k * (a0r - a1r);
+            im[i1] = k * (a0i - a1i);
+        }
+        sync();
+    }
+
+    __device__ void x(int q) {
+        for (uint32_t p = threadIdx.x; p < N / 2; p += blockDim.x) {
+            const uint32_t i0 = ins0(p, (uint32_t)q), i1 = i0 | (1u << q);
+            const T r = re[i0], i = im[i0];
+            re[i0] = re[i1];
+            im[i0] = im[i1];
+            re[i1] = r;
+            im[i1] = i;
+        }
+        sync();
+    }
+
+    // exp(i theta X_q) controlled on bit c: a0' = c a0 + i s a1, a1' = c a1 + i s a0
+    __device__ void rx(int q, int c, T cs, T sn) {
+        const uint32_t cnt = c < 0 ? N / 2 : N / 4;
+        for (uint32_t p = threadIdx.x; p < cnt; p += blockDim.x) {
+            const uint32_t i0 = pair_idx(p, q, c), i1 = i0 | (1u << q);
+            const T a0r = re[i0], a0i = im[i0], a1r = re[i1], a1i = im[i1];
+            re[i0] = a0r * cs - a1i * sn;
+            im[i0] = a0i * cs + a1r * sn;
+            re[i1] = a1r * cs - a0i * sn;
+            im[i1] = a1i * cs + a0r * sn;
+        }
+        sync();
+    }
+
+    // phase (cs + i sn) on the elements with bit q == val (U1 with q_mask = val)
+    __device__ void u1(int q, int val, T cs, T sn) {
+        for (uint32_t p = threadIdx.x; p < N / 2; p += blockDim.x) {
+            const uint32_t i = ins0(p, (uint32_t)q) | ((uint32_t)val << q);
+            const T a = re[i];
+            re[i] = a * cs - im[i] * sn;
+            im[i] = im[i] * cs + a * sn;
+        }
+        sync();
+    }
+
+    // controlled phase: both bits set
+    __device__ void cu1(int qc, int qt, T cs, T sn) {
+        const uint32_t lo = qc < qt ? qc : qt, hi = qc < qt ? qt : qc;
+        for (uint32_t p = threadIdx.x; p < N / 4; p += blockDim.x) {
+            const uint32_t i = ins0(ins0(p, lo), hi) | (1u << qc) | (1u << qt);
+            const T a = re[i];
+            re[i] = a * cs - im[i] * sn;
+            im[i] = im[i] * cs + a * sn;
+        }
+        sync();
+    }
+
+    // product of exp(i J d Z_i Z_{i+1}) over the ring bonds, on the half with bit c set:
+    // phase table[w], w = number of domain walls of the s spin bits
+    __device__ void zz_layer(int s, int c, const T* tc, const T* ts) {
+        const uint32_t smask = (1u << s) - 1u;
+        for (uint32_t p = threadIdx.x; p < N / 2; p += blockDim.x) {
+            const uint32_t i = ins0(p, (uint32_t)c) | (1u << c);
+            const uint32_t xs = i & smask;
+            const uint32_t rot = ((xs >> 1) | ((xs & 1u) << (s - 1))) & smask;
+            const int w = __popc(xs ^ rot);
+            const T cs = tc[w], sn = ts[w];
+            const T a = re[i];
+            re[i] = a * cs - im[i] * sn;
+            im[i] = im[i] * cs + a * sn;
+        }
+        sync();
+    }
+
+    // QMS acceptance rotation W on the acceptance qubit (the MSB), factors per
+    // energy reading Enew = (i >> shift) & (L-1)
+    __device__ void w_oracle(int qacc, int shift, uint32_t L, const double* f1, const double* f2) {
+        const uint32_t half = 1u << qacc;
+        for (uint32_t j = threadIdx.x; j < half; j += blockDim.x) {
+            const uint32_t i = j | half;
+            const uint32_t e = (j >> shift) & (L - 1u);
+            const T a = (T)f1[e], b = (T)f2[e];
+            const T jr = re[j], ji = im[j], ir = re[i], ii = im[i];
+            re[j] = b * jr + a * ir;
+            im[j] = b * ji + a * ii;
+            re[i] = a * jr - b * ir;
+            im[i] = a * ji - b * ii;
+        }
+        sync();
+    }
+
+    // projective measurement of q with the draw r: returns c = (r < p1)
+    __device__ int measure(int q, double r) {
+        double p0 = 0.0, p1 = 0.0;
+        for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
+            const double w = (double)re[i] * (double)re[i] + (double)im[i] * (double)im[i];
+            if ((i >> q) & 1u) p1 += w; else p0 += w;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            p0 += __shfl_down_sync(0xffffffffu, p0, o);
+            p1 += __shfl_down_sync(0xffffffffu, p1, o);
+        }
+        const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        if (lane == 0) {
+            sh->red[0][wid] = p0;
+            sh->red[1][wid] = p1;
+        }
+        sync();
+        if (threadIdx.x == 0) {
+            double a = 0.0, b = 0.0;
+            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+                a += sh->red[0][k];
+                b += sh->red[1][k];
+            }
+            const int cc = (int)(r < b);
+            sh->bcast_i[0] = cc;
+            sh->bcast_d[0] = 1. / sqrt(cc ? b : a);
+        }
+        sync();
+        const int cc = sh->bcast_i[0];
+        const T sc = (T)sh->bcast_d[0];
+        for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
+            const bool keep = (int)((i >> q) & 1u) == cc;
+            re[i] = (keep ? re[i] : (T)0) * sc;
+            im[i] = (keep ? im[i] : (T)0) * sc;
+        }
+        sync();
+        return cc;
+    }
+};
+
+// one draw, made by thread 0 and broadcast
+__device__ __forceinline__ double draw(Shared& sh) {
+    __syncthreads();
+    if (threadIdx.x == 0) sh.bcast_d[1] = pcg_doub(sh);
+    __syncthreads();
+    return sh.bcast_d[1];
+}
+
+template <typename T>
+struct Qms {
+    Ctx<T> cx;
+    const DevChain* P;
+    int s, e, acc;
+    uint32_t L;
+    uint32_t E_old;
+    int gCi;
+
+    // exp(-iHt) on the spins, controlled on bit c (a phase-estimation target)
+    __device__ void evolution(double t, int c) {
+        const double at = fabs(t);
+        int steps = (int)ceil(at / P->dt - 1e-9);
+        if (steps < 1) steps = 1;
+        const double d = t / (double)steps;
+        __shared__ T tc[24], ts[24];
+        __shared__ T xc, xs;
+        if (threadIdx.x <= (unsigned)s) {
+            double sn, cs;
+            sincos(P->J * d * (double)(s - 2 * (int)threadIdx.x), &sn, &cs);
+            tc[threadIdx.x] = (T)cs;
+            ts[threadIdx.x] = (T)sn;
+        }
+        if (threadIdx.x == 32) {
+            double sn, cs;
+            sincos(P->h * d, &sn, &cs);
+            xc = (T)cs;
+            xs = (T)sn;
+        }
+        __syncthreads();
+        for (int k = 0; k < steps; ++k) {
+            cx.zz_layer(s, c, tc, ts);
+            for (int i = 0; i < s; ++i) cx.rx(i, c, xc, xs);
+        }
+    }
+
+    __device__ void u1(int q, double phase) {
+        double sn, cs;
+        sincos(phase, &sn, &cs);
+        cx.u1(q, 1, (T)cs, (T)sn);
+    }
+
+    __device__ void cu1(int qc, int qt, double phase) {
+        double sn, cs;
+        sincos(phase, &sn, &cs);
+        cx.cu1(qc, qt, (T)cs, (T)sn);
+    }
+
+    // QFT over the energy register (phases 2 pi / 2^m, the reference's table)
+    __device__ void qft(bool inverse) {
+        if (!inverse) {
+            for (int o = e - 1; o >= 0; o--) {
+                cx.h(s + o, -1);
+                for (int i = o - 1; i >= 0; i--) cu1(s + i, s + o, 2.0 * M_PI / (double)(1u << (1 + (o - i))));
+            }
+        } else {
+            for (int o = 0; o < e; o++) {
+                for (int i = 0; i < o; i++) cu1(s + i, s + o, -(2.0 * M_PI / (double)(1u << (1 + (o - i)))));
+                cx.h(s + o, -1);
+            }
+        }
+    }
+
+    __device__ void phi() {
+        const double t = P->t_pe;
+        for (int k = 0; k < e; ++k) cx.h(s + k, -1);
+        for (int trg = e - 1; trg > -1; --trg) {
+            const double powr = (double)(1u << (e - 1 - trg));
+            evolution(-powr * t, s + trg);
+            u1(s + trg, -powr * t * P->t_shift);
+        }
+        qft(true);
+    }
+
+    __device__ void phi_inverse() {
+        const double t = P->t_pe;
+        qft(false);
+        for (int trg = 0; trg < e; ++trg) {
+            const double powr = (double)(1u << (e - 1 - trg));
+            evolution(powr * t, s + trg);
+            u1(s + trg, powr * t * P->t_shift);
+        }
+        for (int k = 0; k < e; ++k) cx.h(s + k, -1);
+    }
+
+    __device__ void w() {
+        __shared__ double f1[128], f2[128];
+        for (uint32_t en = threadIdx.x; en < L; en += blockDim.x) {
+            const double dE = (en * P->c_factor - E_old * P->c_factor);
+            if (dE > 0) {
+                f1[en] = exp(-dE / 2.0);
+                f2[en] = sqrt(1.0 - f1[en] * f1[en]);
+            } else {
+                f1[en] = 1.0;
+                f2[en] = 0.0;
+            }
+        }
+        __syncthreads();
+        cx.w_oracle(acc, s, L, f1, f2);
+    }
+
+    __device__ void apply_U() {
+        cx.h(gCi, -1);
+        phi();
+        w();
+    }
+
+    __device__ void apply_U_inverse() {
+        w();
+        phi_inverse();
+        cx.h(gCi, -1);
+    }
+
+    __device__ void reset(int q) {
+        const double r = draw(*cx.sh);
+        if (cx.measure(q, r)) cx.x(q);
+    }
+
+    __device__ uint32_t read_energy() {
+        uint32_t v = 0;
+        for (int k = 0; k < e; ++k) {
+            const double r = draw(*cx.sh);
+            v += (uint32_t)cx.measure(s + k, r) << k;
+        }
+        return v;
+    }
+
+    __device__ double energy_of(uint32_t v) const { return P->t_shift + v / (double)(P->pe_factor * L); }
+
+    __device__ double measure_magnetisation() {
+        double r[24];
+        for (int i = 0; i < s; ++i) r[i] = draw(*cx.sh);
+        double m = 0.0;
+        for (int i = 0; i < s; ++i) m += cx.measure(i, r[i]) ? -1.0 : 1.0;
+        return m;
+    }
+
+    __device__ int draw_C() {
+        const double xr = draw(*cx.sh);
+        for (int i = 0; i < s; ++i) {
+            const double wsum = (i + 1 == s) ? 1.0 : (double)(i + 1) / (double)s;
+            if (xr < wsum) return i;
+        }
+        return s;
+    }
+
+    // one Metropolis step; returns 1/2 accepted (not/sampled), 3/4 restored, -1 failed
+    __device__ int metro_step(bool take, double* Eout, double* Aout, bool* sampled) {
+        *sampled = false;
+        for (int k = 0; k < e; ++k) reset(s + k);
+        reset(acc);
+        phi();
+        const uint32_t eo = read_energy();
+        E_old = eo;
+        for (int k = 0; k < e; ++k)
+            if ((eo >> k) & 1u) cx.x(s + k);
+        gCi = draw_C();
+        apply_U();
+        const int c_acc = cx.measure(acc, draw(*cx.sh));
+        if (c_acc == 1) {
+            const uint32_t en = read_energy();
+            phi_inverse();
+            if (!take) return 1;
+            *Eout = energy_of(en);
+            for (int k = 0; k < e; ++k)
+                if ((en >> k) & 1u) cx.x(s + k);
+            *Aout = measure_magnetisation();
+            *sampled = true;
+            for (int k = 0; k < e; ++k) reset(s + k);
+            phi();
+            read_energy();
+            phi_inverse();
+            return 2;
+        }
+        apply_U_inverse();
+        int ret = 0;
+        int iters = 0;
+        while (iters < P->max_reverse) {
+            phi();
+            const uint32_t en = read_energy();
+            phi_inverse();
+            if (E_old == en) {
+                if (take) {
+                    *Eout = energy_of(E_old);
+                    for (int k = 0; k < e; ++k) reset(s + k);
+                    *Aout = measure_magnetisation();
+                    *sampled = true;
+                    for (int k = 0; k < e; ++k) reset(s + k);
+                    phi();
+                    read_energy();
+                    phi_inverse();
+                    ret = 4;
+                } else {
+                    ret = 3;
+                }
+                break;
+            }
+            apply_U();
+            cx.measure(acc, draw(*cx.sh));
+            apply_U_inverse();
+            iters++;
+        }
+        if (iters == P->max_reverse) return -1;
+        return ret;
+    }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_qms_tfim(const DevChain* __restrict__ chains, const int* __restrict__ order,
+                                                       int nchains, unsigned int* next, sq_chain_result* res,
+                                                       double* sE, double* sA, uint32_t* sStep, T* gbuf,
+                                                       int smem_qubits, int gbuf_qubits) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ Shared sh;
+    __shared__ int cur;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) cur = (int)atomicAdd(next, 1u);
+        __syncthreads();
+        if (cur >= nchains) return;
+        const int ci = order[cur];
+        const DevChain& P = chains[ci];
+        Qms<T> q;
+        q.P = &P;
+        q.s = P.s;
+        q.e = P.e;
+        q.acc = P.s + P.e;
+        q.L = 1u << P.e;
+        q.cx.n = P.n;
+        q.cx.N = 1u << P.n;
+        q.cx.sh = &sh;
+        if (P.n <= smem_qubits) {
+            q.cx.re = reinterpret_cast<T*>(smem_raw);
+        } else {
+            q.cx.re = gbuf + (size_t)blockIdx.x * 2 * ((size_t)1 << gbuf_qubits);
+        }
+        q.cx.im = q.cx.re + q.cx.N;
+        if (threadIdx.x == 0) pcg_seed(sh, P.seed);
+        q.cx.init();
+        uint32_t s0 = 0, accepted = 0, failures = 0, ns = 0;
+        for (uint32_t st = 0; st < (uint32_t)P.steps; ++st) {
+            const bool take = (st > s0 + (uint32_t)P.therm) && ((st - s0) % (uint32_t)P.reset_each == 0u);
+            double E = 0.0, A = 0.0;
+            bool sampled = false;
+            const int ret = q.metro_step(take, &E, &A, &sampled);
+            if (threadIdx.x == 0 && sampled) {
+                const size_t o = (size_t)P.out_offset + ns;
+                sE[o] = E;
+                sA[o] = A;
+                sStep[o] = st;
+            }
+            if (sampled) ns++;
+            if (ret < 0) {
+                q.cx.init();
+                s0 = st + 1;
+                failures++;
+            }
+            if (ret == 1 || ret == 2) accepted++;
+        }
+        if (threadIdx.x == 0) {
+            res[ci].accepted = accepted;
+            res[ci].failures = failures;
+            res[ci].samples = ns;
+            res[ci].pad = 0;
+        }
+    }
+}
+
+}  // namespace sqb
+
+namespace {
+int fail(int code, const std::string& m) {
+    sqi::set_error(m.c_str());
+    return code;
+}
+#define SQB_CUDA(call)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) return fail(SQ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+}  // namespace
+
+extern "C" int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, int precision, sq_chain_result* results,
+                                 double* samples_E, double* samples_A, uint32_t* samples_step, void* stream,
+                                 float* kernel_ms) {
+    using namespace sqb;
+    if (!chains || !results || nchains == 0) return fail(SQ_ERR_ARG, "null or empty chain list");
+    if (precision != SQ_F64 && precision != SQ_F32) return fail(SQ_ERR_ARG, "unknown precision");
+    std::vector<DevChain> dc(nchains);
+    size_t total = 0;
+    int nmax = 0;
+    for (uint32_t i = 0; i < nchains; ++i) {
+        const sq_tfim_chain& c = chains[i];
+        if (c.spins < 2 || c.spins > 20 || c.ene_qbits < 1 || c.ene_qbits > 7)
+            return fail(SQ_ERR_ARG, "chain sizes out of range (spins 2..20, energy qubits 1..7)");
+        if (c.spins + c.ene_qbits + 1 > 22) return fail(SQ_ERR_ARG, "chain wider than 22 qubits");
+        if (c.reset_each == 0 || c.max_reverse == 0 || !(c.ene_max > c.ene_min) || !(c.dt > 0))
+            return fail(SQ_ERR_ARG, "invalid chain parameters");
+        DevChain& d = dc[i];
+        d.s = (int)c.spins;
+        d.e = (int)c.ene_qbits;
+        d.n = d.s + d.e + 1;
+        d.steps = (int)c.steps;
+        d.therm = (int)c.thermalization;
+        d.reset_each = (int)c.reset_each;
+        d.max_reverse = (int)c.max_reverse;
+        d.J = c.J;
+        d.h = c.h;
+        d.beta = c.beta;
+        d.dt = c.dt;
+        const uint32_t L = 1u << c.ene_qbits;
+        // the reference driver's derived constants (src/qms.cu:82-84, qms.cuh:96-103)
+        d.t_shift = c.ene_min;
+        d.pe_factor = (L - 1) / (double)(L * (c.ene_max - c.ene_min));
+        d.t_pe = d.pe_factor * 8. * atan(1.0);
+        d.c_factor = c.beta / (d.pe_factor * L);
+        d.seed = c.seed;
+        d.out_offset = (int)total;
+        total += c.steps;
+        if (d.n > nmax) nmax = d.n;
+    }
+    // chains grouped by width; each class is one persistent launch sized for it
+    int dev = 0, nsm = 1, optin = 0;
+    SQB_CUDA(cudaGetDevice(&dev));
+    SQB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    SQB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const size_t esz = precision == SQ_F64 ? 8 : 4;
+    const size_t static_smem = 4096;
+    int smem_q = 0;
+    while (smem_q < 22 && 2 * ((size_t)1 << (smem_q + 1)) * esz + static_smem <= (size_t)optin) ++smem_q;
+
+    std::vector<int> order(nchains);
+    for (uint32_t i = 0; i < nchains; ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return dc[a].n > dc[b].n; });
+    struct Class { int n, first, count; };
+    std::vector<Class> classes;
+    for (uint32_t k = 0; k < nchains; ++k) {
+        const int n = dc[order[k]].n;
+        if (classes.empty() || classes.back().n != n) classes.push_back({n, (int)k, 0});
+        classes.back().count++;
+    }
+    int gmax_grid = 0;
+    for (const auto& c : classes)
+        if (c.n > smem_q) gmax_grid = std::max(gmax_grid, std::min(c.count, nsm * 2));
+
+    cudaStream_t st = (cudaStream_t)stream;
+    DevChain* d_ch = nullptr;
+    int* d_order = nullptr;
+    unsigned int* d_next = nullptr;
+    sq_chain_result* d_res = nullptr;
+    double *d_E = nullptr, *d_A = nullptr;
+    uint32_t* d_step = nullptr;
+    void* d_g = nullptr;
+    const size_t gq = nmax > smem_q ? (size_t)nmax : 0;
+    auto cleanup = [&]() {
+        cudaFree(d_ch); cudaFree(d_order); cudaFree(d_next); cudaFree(d_res);
+        cudaFree(d_E); cudaFree(d_A); cudaFree(d_step); cudaFree(d_g);
+    };
+    if (cudaMalloc(&d_ch, sizeof(DevChain) * nchains) != cudaSuccess ||
+        cudaMalloc(&d_order, sizeof(int) * nchains) != cudaSuccess ||
+        cudaMalloc(&d_next, sizeof(unsigned int) * classes.size()) != cudaSuccess ||
+        cudaMalloc(&d_res, sizeof(sq_chain_result) * nchains) != cudaSuccess ||
+        cudaMalloc(&d_E, sizeof(double) * (total + 1)) != cudaSuccess ||
+        cudaMalloc(&d_A, sizeof(double) * (total + 1)) != cudaSuccess ||
+        cudaMalloc(&d_step, sizeof(uint32_t) * (total + 1)) != cudaSuccess ||
+        (gq && cudaMalloc(&d_g, (size_t)gmax_grid * 2 * ((size_t)1 << gq) * esz) != cudaSuccess)) {
+        cudaGetLastError();
+        cleanup();
+        return fail(SQ_ERR_NOMEM, "device allocation for the chain batch failed");
+    }
+    cudaMemcpyAsync(d_ch, dc.data(), sizeof(DevChain) * nchains, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_order, order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(d_next, 0, sizeof(unsigned int) * classes.size(), st);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    cudaError_t err = cudaSuccess;
+    for (size_t ci = 0; ci < classes.size() && err == cudaSuccess; ++ci) {
+        const Class& c = classes[ci];
+        const bool in_smem = c.n <= smem_q;
+        const size_t smem = in_smem ? 2 * ((size_t)1 << c.n) * esz : 16;
+        int per_sm = (int)((size_t)(228 * 1024) / (smem + static_smem + 1024));
+        per_sm = std::max(1, std::min(per_sm, 4));
+        int grid = in_smem ? nsm * per_sm : std::min(c.count, nsm * 2);
+        grid = std::min(grid, c.count);
+        if (precision == SQ_F64) {
+            cudaFuncSetAttribute(k_qms_tfim<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_qms_tfim<double><<<grid, kThreads, smem, st>>>(d_ch, d_order + c.first, c.count, d_next + ci, d_res,
+                                                             d_E, d_A, d_step, (double*)d_g, in_smem ? c.n : -1, (int)gq);
+        } else {
+            cudaFuncSetAttribute(k_qms_tfim<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_qms_tfim<float><<<grid, kThreads, smem, st>>>(d_ch, d_order + c.first, c.count, d_next + ci, d_res,
+                                                            d_E, d_A, d_step, (float*)d_g, in_smem ? c.n : -1, (int)gq);
+        }
+        err = cudaGetLastError();
+    }
+    cudaEventRecord(e1, st);
+    if (err == cudaSuccess) {
+        cudaMemcpyAsync(results, d_res, sizeof(sq_chain_result) * nchains, cudaMemcpyDeviceToHost, st);
+        if (samples_E) cudaMemcpyAsync(samples_E, d_E, sizeof(double) * total, cudaMemcpyDeviceToHost, st);
+        if (samples_A) cudaMemcpyAsync(samples_A, d_A, sizeof(double) * total, cudaMemcpyDeviceToHost, st);
+        if (samples_step) cudaMemcpyAsync(samples_step, d_step, sizeof(uint32_t) * total, cudaMemcpyDeviceToHost, st);
+        err = cudaStreamSynchronize(st);
+    }
+    float ms = 0.f;
+    if (err == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    if (kernel_ms) *kernel_ms = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cleanup();
+    if (err != cudaSuccess) return fail(SQ_ERR_CUDA, std::string("chain batch: ") + cudaGetErrorString(err));
+    return SQ_OK;
+}

@@ -91,10 +91,13 @@ def test_errors_and_edge_cases():
     with State(4) as s:
         with pytest.raises(SqError):
             s.apply_x(4)
+        s.apply_h([0, 1, 2, 3])
         s.activate_gc_mask([1])
-        with pytest.raises(SqError):
-            s.apply_h(1)  # target inside the global control mask
+        s.apply_h(1)  # target inside the global control mask: the reference zeroes that subspace
         s.deactivate_gc_mask([1])
+        st = s.get_state()
+        assert np.all(st[[i for i in range(16) if i & 2]] == 0)
+        s.init_state()
         with pytest.raises(SqUnsupported):
             s.apply_pauli_TP_rotation([0, 1, 2], [1, 2, 3], 0.3)
         with pytest.raises(RuntimeError):

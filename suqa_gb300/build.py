@@ -106,9 +106,33 @@ def build_dropin(force=False):
     return outs
 
 
+TFIM_SPINS = range(4, 11)
+
+
+def build_tfim_drivers(force=False):
+    """qms drivers with the transverse-field Ising ring plugin, one per ring length
+    (the plugin API fixes the system width at compile time)."""
+    tdir = os.path.join(PKG, "systems", "tfim")
+    src_app = os.path.join(PKG, "apps", "qms.cpp")
+    src_sys = os.path.join(PKG, "systems", "tfim_ring.cpp")
+    headers = [os.path.join(SHIM_INCLUDE, f) for f in os.listdir(SHIM_INCLUDE)] + [os.path.join(tdir, "system.cuh")]
+    shim = os.path.join(BUILD, "suqa_shim.o")
+    lib = os.path.join(BUILD, "libsq.so")
+    jobs = []
+    for sp in TFIM_SPINS:
+        exe = os.path.join(BUILD, f"qms_tfim_s{sp}")
+        if force or not _newer(exe, [src_app, src_sys, shim, lib] + headers):
+            jobs.append([cxx(), "-std=c++17", "-O2", "-ffp-contract=off", "-w", f"-DTFIM_SPINS={sp}", "-I" + tdir,
+                         "-I" + SHIM_INCLUDE, "-I" + INCLUDE, src_app, src_sys, shim, "-L" + BUILD, "-lsq",
+                         "-Wl,-rpath," + BUILD, "-o", exe])
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
+        list(ex.map(_run, jobs))
+
+
 def build_all(force=False):
     lib = build_libsq(force)
     build_dropin(force)
+    build_tfim_drivers(force)
     return lib
 
 

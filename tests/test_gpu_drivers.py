@@ -18,7 +18,7 @@ BUILD = os.path.join(ROOT, "suqa_gb300", "_build")
 def run_driver(name, tmp_path):
     man = golden_io.run_manifest()[name]
     out = str(tmp_path / f"{name}.txt")
-    exe = os.path.join(BUILD, man["driver"])
+    exe = os.path.join(BUILD, man["driver"] if not name.startswith("tfim") else "qms_tfim_s" + name.split("_s")[1])
     argv = [exe] + [a.replace("{out}", out) for a in man["args"]]
     env = dict(os.environ)
     env.update(man["env"])
@@ -49,3 +49,10 @@ def test_evo_probabilities_match_reference(tmp_path):
     want = np.loadtxt(os.path.join(golden_io.GOLDEN, "runs", "evo.txt"))
     assert got.shape == want.shape
     assert np.max(np.abs(got - want)) < 1e-11
+
+
+@pytest.mark.parametrize("name", ["tfim_s4", "tfim_s5", "tfim_s6"])
+def test_qms_tfim_drivers_match_reference_output(name, tmp_path):
+    """The host-driven drop-in path with the TFIM ring plugin."""
+    man, out, stdout = run_driver(name, tmp_path)
+    assert open(out).read() == golden_io.run_output(name)

@@ -34,7 +34,7 @@ void set_error(const char* msg);
 
 namespace sqb {
 
-constexpr int kThreads = 512;
+constexpr int kThreads = 256;
 
 struct DevChain {
     int s, e, n, steps, therm, reset_each, max_reverse;
@@ -83,6 +83,10 @@ __device__ __forceinline__ uint32_t pair_idx(uint32_t p, int q, int c) {
     return ins0(ins0(p, lo), hi) | (1u << c);
 }
 
+// Shared-memory layout: element i lives at i + i/32 (one pad word per 32), which
+// makes the strided group loads of the fused Trotter sweeps bank-conflict free.
+__device__ __forceinline__ uint32_t pad(uint32_t i) { return i + (i >> 5); }
+
 template <typename T>
 struct Ctx {
     T* re;
@@ -95,11 +99,11 @@ struct Ctx {
 
     __device__ void init() {
         for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
-            re[i] = (T)0;
-            im[i] = (T)0;
+            re[pad(i)] = (T)0;
+            im[pad(i)] = (T)0;
         }
         sync();
-        if (threadIdx.x == 0) re[0] = (T)1;
+        if (threadIdx.x == 0) re[pad(0)] = (T)1;
         sync();
     }
 
@@ -109,11 +113,11 @@ struct Ctx {
         const T k = (T)0.7071067811865475;
         for (uint32_t p = threadIdx.x; p < cnt; p += blockDim.x) {
             const uint32_t i0 = pair_idx(p, q, c), i1 = i0 | (1u << q);
-            const T a0r = re[i0], a0i = im[i0], a1r = re[i1], a1i = im[i1];
-            re[i0] = k * (a0r + a1r);
-            im[i0] = k * (a0i + a1i);
-            re[i1] = k * (a0r - a1r);
-            im[i1] = k * (a0i - a1i);
+            const T a0r = re[pad(i0)], a0i = im[pad(i0)], a1r = re[pad(i1)], a1i = im[pad(i1)];
+            re[pad(i0)] = k * (a0r + a1r);
+            im[pad(i0)] = k * (a0i + a1i);
+            re[pad(i1)] = k * (a0r - a1r);
+            im[pad(i1)] = k * (a0i - a1i);
         }
         sync();
     }
@@ -121,11 +125,11 @@ struct Ctx {
     __device__ void x(int q) {
         for (uint32_t p = threadIdx.x; p < N / 2; p += blockDim.x) {
             const uint32_t i0 = ins0(p, (uint32_t)q), i1 = i0 | (1u << q);
-            const T r = re[i0], i = im[i0];
-            re[i0] = re[i1];
-            im[i0] = im[i1];
-            re[i1] = r;
-            im[i1] = i;
+            const T r = re[pad(i0)], i = im[pad(i0)];
+            re[pad(i0)] = re[pad(i1)];
+            im[pad(i0)] = im[pad(i1)];
+            re[pad(i1)] = r;
+            im[pad(i1)] = i;
         }
         sync();
     }
@@ -135,11 +139,11 @@ struct Ctx {
         const uint32_t cnt = c < 0 ? N / 2 : N / 4;
         for (uint32_t p = threadIdx.x; p < cnt; p += blockDim.x) {
             const uint32_t i0 = pair_idx(p, q, c), i1 = i0 | (1u << q);
-            const T a0r = re[i0], a0i = im[i0], a1r = re[i1], a1i = im[i1];
-            re[i0] = a0r * cs - a1i * sn;
-            im[i0] = a0i * cs + a1r * sn;
-            re[i1] = a1r * cs - a0i * sn;
-            im[i1] = a1i * cs + a0r * sn;
+            const T a0r = re[pad(i0)], a0i = im[pad(i0)], a1r = re[pad(i1)], a1i = im[pad(i1)];
+            re[pad(i0)] = a0r * cs - a1i * sn;
+            im[pad(i0)] = a0i * cs + a1r * sn;
+            re[pad(i1)] = a1r * cs - a0i * sn;
+            im[pad(i1)] = a1i * cs + a0r * sn;
         }
         sync();
     }
@@ -148,9 +152,9 @@ struct Ctx {
     __device__ void u1(int q, int val, T cs, T sn) {
         for (uint32_t p = threadIdx.x; p < N / 2; p += blockDim.x) {
             const uint32_t i = ins0(p, (uint32_t)q) | ((uint32_t)val << q);
-            const T a = re[i];
-            re[i] = a * cs - im[i] * sn;
-            im[i] = im[i] * cs + a * sn;
+            const T a = re[pad(i)];
+            re[pad(i)] = a * cs - im[pad(i)] * sn;
+            im[pad(i)] = im[pad(i)] * cs + a * sn;
         }
         sync();
     }
@@ -160,9 +164,9 @@ struct Ctx {
         const uint32_t lo = qc < qt ? qc : qt, hi = qc < qt ? qt : qc;
         for (uint32_t p = threadIdx.x; p < N / 4; p += blockDim.x) {
             const uint32_t i = ins0(ins0(p, lo), hi) | (1u << qc) | (1u << qt);
-            const T a = re[i];
-            re[i] = a * cs - im[i] * sn;
-            im[i] = im[i] * cs + a * sn;
+            const T a = re[pad(i)];
+            re[pad(i)] = a * cs - im[pad(i)] * sn;
+            im[pad(i)] = im[pad(i)] * cs + a * sn;
         }
         sync();
     }
@@ -177,11 +181,81 @@ struct Ctx {
             const uint32_t rot = ((xs >> 1) | ((xs & 1u) << (s - 1))) & smask;
             const int w = __popc(xs ^ rot);
             const T cs = tc[w], sn = ts[w];
-            const T a = re[i];
-            re[i] = a * cs - im[i] * sn;
-            im[i] = im[i] * cs + a * sn;
+            const T a = re[pad(i)];
+            re[pad(i)] = a * cs - im[pad(i)] * sn;
+            im[pad(i)] = im[pad(i)] * cs + a * sn;
         }
         sync();
+    }
+
+
+    // One Trotter step on the half with bit c set: the ZZ bond phases (a diagonal
+    // indexed by the number of domain walls), then exp(i h d X_i) on every spin.
+    // Spins are processed M at a time: a thread loads the 2^M amplitudes that
+    // differ only in those spins into registers, applies the M rotations there
+    // (they commute) and stores them back, so a step costs ceil(s/4) sweeps.
+    template <int M>
+    __device__ void trotter_group(int s, int g0, int c, bool with_zz, const T* tc, const T* ts, T xc, T xs) {
+        constexpr int G = 1 << M;
+        const uint32_t smask = (1u << s) - 1u;
+        const uint32_t ngroups = N >> (M + 1);
+        for (uint32_t gi = threadIdx.x; gi < ngroups; gi += blockDim.x) {
+            // insert M zero bits at g0, then the control bit (c > every spin bit)
+            uint32_t base = ((gi >> g0) << (g0 + M)) | (gi & ((1u << g0) - 1u));
+            base = ins0(base, (uint32_t)c) | (1u << c);
+            T ar[G], ai[G];
+#pragma unroll
+            for (int r = 0; r < G; ++r) {
+                const uint32_t i = base | ((uint32_t)r << g0);
+                ar[r] = re[pad(i)];
+                ai[r] = im[pad(i)];
+            }
+            if (with_zz) {
+#pragma unroll
+                for (int r = 0; r < G; ++r) {
+                    const uint32_t xsb = (base | ((uint32_t)r << g0)) & smask;
+                    const uint32_t rot = ((xsb >> 1) | ((xsb & 1u) << (s - 1))) & smask;
+                    const int w = __popc(xsb ^ rot);
+                    const T cs = tc[w], sn = ts[w];
+                    const T a = ar[r];
+                    ar[r] = a * cs - ai[r] * sn;
+                    ai[r] = ai[r] * cs + a * sn;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < M; ++k) {
+#pragma unroll
+                for (int r = 0; r < G; ++r) {
+                    if (r & (1 << k)) continue;
+                    const int r1 = r | (1 << k);
+                    const T a0r = ar[r], a0i = ai[r], a1r = ar[r1], a1i = ai[r1];
+                    ar[r] = a0r * xc - a1i * xs;
+                    ai[r] = a0i * xc + a1r * xs;
+                    ar[r1] = a1r * xc - a0i * xs;
+                    ai[r1] = a1i * xc + a0r * xs;
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < G; ++r) {
+                const uint32_t i = base | ((uint32_t)r << g0);
+                re[pad(i)] = ar[r];
+                im[pad(i)] = ai[r];
+            }
+        }
+        sync();
+    }
+
+    __device__ void trotter_step(int s, int c, const T* tc, const T* ts, T xc, T xs) {
+        for (int g0 = 0; g0 < s; g0 += 4) {
+            const int m = s - g0 < 4 ? s - g0 : 4;
+            const bool zz = (g0 == 0);
+            switch (m) {
+                case 4: trotter_group<4>(s, g0, c, zz, tc, ts, xc, xs); break;
+                case 3: trotter_group<3>(s, g0, c, zz, tc, ts, xc, xs); break;
+                case 2: trotter_group<2>(s, g0, c, zz, tc, ts, xc, xs); break;
+                default: trotter_group<1>(s, g0, c, zz, tc, ts, xc, xs); break;
+            }
+        }
     }
 
     // QMS acceptance rotation W on the acceptance qubit (the MSB), factors per
@@ -192,11 +266,11 @@ struct Ctx {
             const uint32_t i = j | half;
             const uint32_t e = (j >> shift) & (L - 1u);
             const T a = (T)f1[e], b = (T)f2[e];
-            const T jr = re[j], ji = im[j], ir = re[i], ii = im[i];
-            re[j] = b * jr + a * ir;
-            im[j] = b * ji + a * ii;
-            re[i] = a * jr - b * ir;
-            im[i] = a * ji - b * ii;
+            const T jr = re[pad(j)], ji = im[pad(j)], ir = re[pad(i)], ii = im[pad(i)];
+            re[pad(j)] = b * jr + a * ir;
+            im[pad(j)] = b * ji + a * ii;
+            re[pad(i)] = a * jr - b * ir;
+            im[pad(i)] = a * ji - b * ii;
         }
         sync();
     }
@@ -205,7 +279,7 @@ struct Ctx {
     __device__ int measure(int q, double r) {
         double p0 = 0.0, p1 = 0.0;
         for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
-            const double w = (double)re[i] * (double)re[i] + (double)im[i] * (double)im[i];
+            const double w = (double)re[pad(i)] * (double)re[pad(i)] + (double)im[pad(i)] * (double)im[pad(i)];
             if ((i >> q) & 1u) p1 += w; else p0 += w;
         }
         for (int o = 16; o > 0; o >>= 1) {
@@ -233,8 +307,8 @@ struct Ctx {
         const T sc = (T)sh->bcast_d[0];
         for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
             const bool keep = (int)((i >> q) & 1u) == cc;
-            re[i] = (keep ? re[i] : (T)0) * sc;
-            im[i] = (keep ? im[i] : (T)0) * sc;
+            re[pad(i)] = (keep ? re[pad(i)] : (T)0) * sc;
+            im[pad(i)] = (keep ? im[pad(i)] : (T)0) * sc;
         }
         sync();
         return cc;
@@ -279,10 +353,7 @@ struct Qms {
             xs = (T)sn;
         }
         __syncthreads();
-        for (int k = 0; k < steps; ++k) {
-            cx.zz_layer(s, c, tc, ts);
-            for (int i = 0; i < s; ++i) cx.rx(i, c, xc, xs);
-        }
+        for (int k = 0; k < steps; ++k) cx.trotter_step(s, c, tc, ts, xc, xs);
     }
 
     __device__ void u1(int q, double phase) {
@@ -457,7 +528,7 @@ struct Qms {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_qms_tfim(const DevChain* __restrict__ chains, const int* __restrict__ order,
+__global__ void __launch_bounds__(kThreads, 2) k_qms_tfim(const DevChain* __restrict__ chains, const int* __restrict__ order,
                                                        int nchains, unsigned int* next, sq_chain_result* res,
                                                        double* sE, double* sA, uint32_t* sStep, T* gbuf,
                                                        int smem_qubits, int gbuf_qubits) {
@@ -483,9 +554,10 @@ __global__ void __launch_bounds__(kThreads) k_qms_tfim(const DevChain* __restric
         if (P.n <= smem_qubits) {
             q.cx.re = reinterpret_cast<T*>(smem_raw);
         } else {
-            q.cx.re = gbuf + (size_t)blockIdx.x * 2 * ((size_t)1 << gbuf_qubits);
+            const size_t cap = ((size_t)1 << gbuf_qubits) + ((size_t)1 << gbuf_qubits) / 32 + 1;
+            q.cx.re = gbuf + (size_t)blockIdx.x * 2 * cap;
         }
-        q.cx.im = q.cx.re + q.cx.N;
+        q.cx.im = q.cx.re + (q.cx.N + q.cx.N / 32 + 1);
         if (threadIdx.x == 0) pcg_seed(sh, P.seed);
         q.cx.init();
         uint32_t s0 = 0, accepted = 0, failures = 0, ns = 0;
@@ -578,7 +650,8 @@ extern "C" int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, 
     const size_t esz = precision == SQ_F64 ? 8 : 4;
     const size_t static_smem = 4096;
     int smem_q = 0;
-    while (smem_q < 22 && 2 * ((size_t)1 << (smem_q + 1)) * esz + static_smem <= (size_t)optin) ++smem_q;
+    auto padded = [](int q) { return (size_t)(((size_t)1 << q) + ((size_t)1 << q) / 32 + 1); };
+    while (smem_q < 22 && 2 * padded(smem_q + 1) * esz + static_smem <= (size_t)optin) ++smem_q;
 
     std::vector<int> order(nchains);
     for (uint32_t i = 0; i < nchains; ++i) order[i] = (int)i;
@@ -614,7 +687,7 @@ extern "C" int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, 
         cudaMalloc(&d_E, sizeof(double) * (total + 1)) != cudaSuccess ||
         cudaMalloc(&d_A, sizeof(double) * (total + 1)) != cudaSuccess ||
         cudaMalloc(&d_step, sizeof(uint32_t) * (total + 1)) != cudaSuccess ||
-        (gq && cudaMalloc(&d_g, (size_t)gmax_grid * 2 * ((size_t)1 << gq) * esz) != cudaSuccess)) {
+        (gq && cudaMalloc(&d_g, (size_t)gmax_grid * 2 * padded((int)gq) * esz) != cudaSuccess)) {
         cudaGetLastError();
         cleanup();
         return fail(SQ_ERR_NOMEM, "device allocation for the chain batch failed");
@@ -630,9 +703,9 @@ extern "C" int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, 
     for (size_t ci = 0; ci < classes.size() && err == cudaSuccess; ++ci) {
         const Class& c = classes[ci];
         const bool in_smem = c.n <= smem_q;
-        const size_t smem = in_smem ? 2 * ((size_t)1 << c.n) * esz : 16;
+        const size_t smem = in_smem ? 2 * padded(c.n) * esz : 16;
         int per_sm = (int)((size_t)(228 * 1024) / (smem + static_smem + 1024));
-        per_sm = std::max(1, std::min(per_sm, 4));
+        per_sm = std::max(1, std::min(per_sm, 8));
         int grid = in_smem ? nsm * per_sm : std::min(c.count, nsm * 2);
         grid = std::min(grid, c.count);
         if (precision == SQ_F64) {

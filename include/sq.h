@@ -159,7 +159,8 @@ typedef struct sq_chain_result {
     uint32_t accepted;        /* steps returning 1 or 2 */
     uint32_t failures;        /* failed restorations (state re-initialised) */
     uint32_t samples;         /* (E, A) samples written */
-    uint32_t pad;
+    uint32_t phase_estimations; /* energy phase estimations (forward and inverse) applied */
+    uint64_t cycles;          /* SM clock cycles the chain took */
 } sq_chain_result;
 
 /* Runs every chain to completion on the current device (one persistent launch per

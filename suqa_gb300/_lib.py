@@ -36,7 +36,8 @@ class SqTfimChain(C.Structure):
 
 
 class SqChainResult(C.Structure):
-    _fields_ = [("accepted", C.c_uint32), ("failures", C.c_uint32), ("samples", C.c_uint32), ("pad", C.c_uint32)]
+    _fields_ = [("accepted", C.c_uint32), ("failures", C.c_uint32), ("samples", C.c_uint32),
+                ("phase_estimations", C.c_uint32), ("cycles", C.c_uint64)]
 
 
 _lib = None

@@ -47,6 +47,8 @@ class ChainRun:
     E: np.ndarray
     A: np.ndarray
     step: np.ndarray = field(default_factory=lambda: np.zeros(0, np.uint32))
+    phase_estimations: int = 0
+    cycles: int = 0
 
     def reference_rows(self, steps: int):
         """Rows the reference qms driver would have written to its output file: it
@@ -81,6 +83,6 @@ def run_tfim_batch(chains: list[TfimChain], precision: str = "f32", stream: int 
     for i, c in enumerate(chains):
         k = res[i].samples
         out.append(ChainRun(res[i].accepted, res[i].failures, E[off:off + k].copy(), A[off:off + k].copy(),
-                            S[off:off + k].copy()))
+                            S[off:off + k].copy(), res[i].phase_estimations, res[i].cycles))
         off += c.steps
     return out, ms.value

@@ -26,7 +26,11 @@
 #include <string>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "sq.h"
+
+namespace cg = cooperative_groups;
 
 namespace sqi {
 void set_error(const char* msg);
@@ -87,43 +91,104 @@ __device__ __forceinline__ uint32_t pair_idx(uint32_t p, int q, int c) {
 // makes the strided group loads of the fused Trotter sweeps bank-conflict free.
 __device__ __forceinline__ uint32_t pad(uint32_t i) { return i + (i >> 5); }
 
-template <typename T>
+// A chain's state.  Chains wider than one CTA's shared memory run on a cluster
+// of 2^k CTAs: the k most significant qubits (the acceptance qubit and the top
+// energy qubits) are distributed, CTA rank r holding the slice whose top bits
+// equal r.  Gates on local qubits never leave the CTA; a distributed qubit used
+// as a control is a per-CTA predicate; only H/X/W on a distributed qubit and the
+// measurement reductions exchange data through distributed shared memory.
+// Rank 0 owns the chain's random stream and broadcasts every decision, so all
+// ranks follow the same control flow.
+template <typename T, bool CL>
 struct Ctx {
     T* re;
     T* im;
-    int n;
-    uint32_t N;
+    int n, k, nl;      // total, distributed, local qubits
+    uint32_t Nl;       // local amplitudes
+    uint32_t rank;
     Shared* sh;
 
     __device__ void sync() const { __syncthreads(); }
+    __device__ void csync() const {
+        if (CL) cg::this_cluster().sync(); else __syncthreads();
+    }
+    __device__ bool dist(int q) const { return q >= nl; }
+    __device__ uint32_t rbit(int q) const { return (rank >> (q - nl)) & 1u; }
+    __device__ T* peer_re(uint32_t r) const { return cg::this_cluster().map_shared_rank(re, r); }
+    __device__ T* peer_im(uint32_t r) const { return cg::this_cluster().map_shared_rank(im, r); }
+    __device__ Shared* peer_sh(uint32_t r) const { return cg::this_cluster().map_shared_rank(sh, r); }
 
     __device__ void init() {
-        for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
+        for (uint32_t i = threadIdx.x; i < Nl; i += blockDim.x) {
             re[pad(i)] = (T)0;
             im[pad(i)] = (T)0;
         }
         sync();
-        if (threadIdx.x == 0) re[pad(0)] = (T)1;
-        sync();
+        if (threadIdx.x == 0 && rank == 0) re[pad(0)] = (T)1;
+        csync();
     }
 
-    // Hadamard on q, optionally controlled on bit c
-    __device__ void h(int q, int c) {
-        const uint32_t cnt = c < 0 ? N / 2 : N / 4;
-        const T k = (T)0.7071067811865475;
-        for (uint32_t p = threadIdx.x; p < cnt; p += blockDim.x) {
-            const uint32_t i0 = pair_idx(p, q, c), i1 = i0 | (1u << q);
+    // 2x2 update of a pair across the cluster: this CTA holds the element with
+    // bit value `mine` of the distributed qubit q, the partner CTA the other.
+    // op: 0 = X (swap), 1 = H
+    __device__ void cross_pair(int q, int op) {
+        const uint32_t partner = rank ^ (1u << (q - nl));
+        const uint32_t mine = rbit(q);
+        T* pre = peer_re(partner);
+        T* pim = peer_im(partner);
+        csync();  // partner's previous writes are visible
+        const T kh = (T)0.7071067811865475;
+        // read phase into registers (at most Nl/blockDim elements per thread)
+        for (uint32_t base = 0; base < Nl; base += blockDim.x * 8u) {
+            T nr[8], ni[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t i = base + threadIdx.x + u * blockDim.x;
+                if (i < Nl) {
+                    const T ar = re[pad(i)], ai = im[pad(i)], br = pre[pad(i)], bi = pim[pad(i)];
+                    if (op == 0) {
+                        nr[u] = br;
+                        ni[u] = bi;
+                    } else if (mine == 0) {
+                        nr[u] = kh * (ar + br);
+                        ni[u] = kh * (ai + bi);
+                    } else {
+                        nr[u] = kh * (br - ar);
+                        ni[u] = kh * (bi - ai);
+                    }
+                }
+            }
+            csync();  // everyone has read before anyone writes
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t i = base + threadIdx.x + u * blockDim.x;
+                if (i < Nl) {
+                    re[pad(i)] = nr[u];
+                    im[pad(i)] = ni[u];
+                }
+            }
+            csync();
+        }
+    }
+
+    // Hadamard on q (uncontrolled)
+    __device__ void h(int q) {
+        if (CL && dist(q)) { cross_pair(q, 1); return; }
+        const T kk = (T)0.7071067811865475;
+        for (uint32_t p = threadIdx.x; p < Nl / 2; p += blockDim.x) {
+            const uint32_t i0 = ins0(p, (uint32_t)q), i1 = i0 | (1u << q);
             const T a0r = re[pad(i0)], a0i = im[pad(i0)], a1r = re[pad(i1)], a1i = im[pad(i1)];
-            re[pad(i0)] = k * (a0r + a1r);
-            im[pad(i0)] = k * (a0i + a1i);
-            re[pad(i1)] = k * (a0r - a1r);
-            im[pad(i1)] = k * (a0i - a1i);
+            re[pad(i0)] = kk * (a0r + a1r);
+            im[pad(i0)] = kk * (a0i + a1i);
+            re[pad(i1)] = kk * (a0r - a1r);
+            im[pad(i1)] = kk * (a0i - a1i);
         }
         sync();
     }
 
     __device__ void x(int q) {
-        for (uint32_t p = threadIdx.x; p < N / 2; p += blockDim.x) {
+        if (CL && dist(q)) { cross_pair(q, 0); return; }
+        for (uint32_t p = threadIdx.x; p < Nl / 2; p += blockDim.x) {
             const uint32_t i0 = ins0(p, (uint32_t)q), i1 = i0 | (1u << q);
             const T r = re[pad(i0)], i = im[pad(i0)];
             re[pad(i0)] = re[pad(i1)];
@@ -134,23 +199,20 @@ struct Ctx {
         sync();
     }
 
-    // exp(i theta X_q) controlled on bit c: a0' = c a0 + i s a1, a1' = c a1 + i s a0
-    __device__ void rx(int q, int c, T cs, T sn) {
-        const uint32_t cnt = c < 0 ? N / 2 : N / 4;
-        for (uint32_t p = threadIdx.x; p < cnt; p += blockDim.x) {
-            const uint32_t i0 = pair_idx(p, q, c), i1 = i0 | (1u << q);
-            const T a0r = re[pad(i0)], a0i = im[pad(i0)], a1r = re[pad(i1)], a1i = im[pad(i1)];
-            re[pad(i0)] = a0r * cs - a1i * sn;
-            im[pad(i0)] = a0i * cs + a1r * sn;
-            re[pad(i1)] = a1r * cs - a0i * sn;
-            im[pad(i1)] = a1i * cs + a0r * sn;
-        }
-        sync();
-    }
-
     // phase (cs + i sn) on the elements with bit q == val (U1 with q_mask = val)
     __device__ void u1(int q, int val, T cs, T sn) {
-        for (uint32_t p = threadIdx.x; p < N / 2; p += blockDim.x) {
+        if (CL && dist(q)) {
+            if (rbit(q) == (uint32_t)val) {
+                for (uint32_t i = threadIdx.x; i < Nl; i += blockDim.x) {
+                    const T a = re[pad(i)];
+                    re[pad(i)] = a * cs - im[pad(i)] * sn;
+                    im[pad(i)] = im[pad(i)] * cs + a * sn;
+                }
+            }
+            sync();
+            return;
+        }
+        for (uint32_t p = threadIdx.x; p < Nl / 2; p += blockDim.x) {
             const uint32_t i = ins0(p, (uint32_t)q) | ((uint32_t)val << q);
             const T a = re[pad(i)];
             re[pad(i)] = a * cs - im[pad(i)] * sn;
@@ -161,33 +223,34 @@ struct Ctx {
 
     // controlled phase: both bits set
     __device__ void cu1(int qc, int qt, T cs, T sn) {
-        const uint32_t lo = qc < qt ? qc : qt, hi = qc < qt ? qt : qc;
-        for (uint32_t p = threadIdx.x; p < N / 4; p += blockDim.x) {
-            const uint32_t i = ins0(ins0(p, lo), hi) | (1u << qc) | (1u << qt);
-            const T a = re[pad(i)];
-            re[pad(i)] = a * cs - im[pad(i)] * sn;
-            im[pad(i)] = im[pad(i)] * cs + a * sn;
+        int fixed[2];
+        int nf = 0;
+        bool skip = false;
+        for (int q : {qc, qt}) {
+            if (CL && dist(q)) {
+                if (!rbit(q)) skip = true;
+            } else {
+                fixed[nf++] = q;
+            }
+        }
+        if (!skip) {
+            const uint32_t cnt = Nl >> nf;
+            for (uint32_t p = threadIdx.x; p < cnt; p += blockDim.x) {
+                uint32_t i = p;
+                if (nf == 2) {
+                    const int lo = fixed[0] < fixed[1] ? fixed[0] : fixed[1], hi = fixed[0] < fixed[1] ? fixed[1] : fixed[0];
+                    i = ins0(ins0(i, lo), hi);
+                } else if (nf == 1) {
+                    i = ins0(i, fixed[0]);
+                }
+                for (int f = 0; f < nf; ++f) i |= 1u << fixed[f];
+                const T a = re[pad(i)];
+                re[pad(i)] = a * cs - im[pad(i)] * sn;
+                im[pad(i)] = im[pad(i)] * cs + a * sn;
+            }
         }
         sync();
     }
-
-    // product of exp(i J d Z_i Z_{i+1}) over the ring bonds, on the half with bit c set:
-    // phase table[w], w = number of domain walls of the s spin bits
-    __device__ void zz_layer(int s, int c, const T* tc, const T* ts) {
-        const uint32_t smask = (1u << s) - 1u;
-        for (uint32_t p = threadIdx.x; p < N / 2; p += blockDim.x) {
-            const uint32_t i = ins0(p, (uint32_t)c) | (1u << c);
-            const uint32_t xs = i & smask;
-            const uint32_t rot = ((xs >> 1) | ((xs & 1u) << (s - 1))) & smask;
-            const int w = __popc(xs ^ rot);
-            const T cs = tc[w], sn = ts[w];
-            const T a = re[pad(i)];
-            re[pad(i)] = a * cs - im[pad(i)] * sn;
-            im[pad(i)] = im[pad(i)] * cs + a * sn;
-        }
-        sync();
-    }
-
 
     // One Trotter step on the half with bit c set: the ZZ bond phases (a diagonal
     // indexed by the number of domain walls), then exp(i h d X_i) on every spin.
@@ -198,11 +261,13 @@ struct Ctx {
     __device__ void trotter_group(int s, int g0, int c, bool with_zz, const T* tc, const T* ts, T xc, T xs) {
         constexpr int G = 1 << M;
         const uint32_t smask = (1u << s) - 1u;
-        const uint32_t ngroups = N >> (M + 1);
+        const bool local_c = !(CL && dist(c));
+        if (!local_c && !rbit(c)) { sync(); return; }
+        const uint32_t ngroups = local_c ? (Nl >> (M + 1)) : (Nl >> M);
         for (uint32_t gi = threadIdx.x; gi < ngroups; gi += blockDim.x) {
             // insert M zero bits at g0, then the control bit (c > every spin bit)
             uint32_t base = ((gi >> g0) << (g0 + M)) | (gi & ((1u << g0) - 1u));
-            base = ins0(base, (uint32_t)c) | (1u << c);
+            if (local_c) base = ins0(base, (uint32_t)c) | (1u << c);
             T ar[G], ai[G];
 #pragma unroll
             for (int r = 0; r < G; ++r) {
@@ -223,11 +288,11 @@ struct Ctx {
                 }
             }
 #pragma unroll
-            for (int k = 0; k < M; ++k) {
+            for (int kq = 0; kq < M; ++kq) {
 #pragma unroll
                 for (int r = 0; r < G; ++r) {
-                    if (r & (1 << k)) continue;
-                    const int r1 = r | (1 << k);
+                    if (r & (1 << kq)) continue;
+                    const int r1 = r | (1 << kq);
                     const T a0r = ar[r], a0i = ai[r], a1r = ar[r1], a1i = ai[r1];
                     ar[r] = a0r * xc - a1i * xs;
                     ai[r] = a0i * xc + a1r * xs;
@@ -259,8 +324,48 @@ struct Ctx {
     }
 
     // QMS acceptance rotation W on the acceptance qubit (the MSB), factors per
-    // energy reading Enew = (i >> shift) & (L-1)
+    // energy reading Enew = (j >> shift) & (L-1), j the element with acc = 0
     __device__ void w_oracle(int qacc, int shift, uint32_t L, const double* f1, const double* f2) {
+        if (CL && dist(qacc)) {
+            const uint32_t accbit = 1u << (qacc - nl);
+            const uint32_t partner = rank ^ accbit;
+            const bool is_j = (rank & accbit) == 0u;
+            const uint32_t jrank = rank & ~accbit;
+            T* pre = peer_re(partner);
+            T* pim = peer_im(partner);
+            csync();
+            for (uint32_t base = 0; base < Nl; base += blockDim.x * 8u) {
+                T nr[8], ni[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const uint32_t l = base + threadIdx.x + u * blockDim.x;
+                    if (l < Nl) {
+                        const uint32_t gj = l | (jrank << nl);
+                        const uint32_t e = (gj >> shift) & (L - 1u);
+                        const T a = (T)f1[e], b = (T)f2[e];
+                        const T mr = re[pad(l)], mi = im[pad(l)], pr = pre[pad(l)], pi = pim[pad(l)];
+                        if (is_j) {
+                            nr[u] = b * mr + a * pr;
+                            ni[u] = b * mi + a * pi;
+                        } else {
+                            nr[u] = a * pr - b * mr;
+                            ni[u] = a * pi - b * mi;
+                        }
+                    }
+                }
+                csync();
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const uint32_t l = base + threadIdx.x + u * blockDim.x;
+                    if (l < Nl) {
+                        re[pad(l)] = nr[u];
+                        im[pad(l)] = ni[u];
+                    }
+                }
+                csync();
+            }
+            return;
+        }
         const uint32_t half = 1u << qacc;
         for (uint32_t j = threadIdx.x; j < half; j += blockDim.x) {
             const uint32_t i = j | half;
@@ -278,9 +383,11 @@ struct Ctx {
     // projective measurement of q with the draw r: returns c = (r < p1)
     __device__ int measure(int q, double r) {
         double p0 = 0.0, p1 = 0.0;
-        for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
+        const bool dq = CL && dist(q);
+        for (uint32_t i = threadIdx.x; i < Nl; i += blockDim.x) {
             const double w = (double)re[pad(i)] * (double)re[pad(i)] + (double)im[pad(i)] * (double)im[pad(i)];
-            if ((i >> q) & 1u) p1 += w; else p0 += w;
+            const uint32_t bit = dq ? rbit(q) : ((i >> q) & 1u);
+            if (bit) p1 += w; else p0 += w;
         }
         for (int o = 16; o > 0; o >>= 1) {
             p0 += __shfl_down_sync(0xffffffffu, p0, o);
@@ -294,43 +401,78 @@ struct Ctx {
         sync();
         if (threadIdx.x == 0) {
             double a = 0.0, b = 0.0;
-            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-                a += sh->red[0][k];
-                b += sh->red[1][k];
+            for (int kk = 0; kk < (int)(blockDim.x >> 5); ++kk) {
+                a += sh->red[0][kk];
+                b += sh->red[1][kk];
             }
-            const int cc = (int)(r < b);
-            sh->bcast_i[0] = cc;
-            sh->bcast_d[0] = 1. / sqrt(cc ? b : a);
+            sh->bcast_d[2] = a;
+            sh->bcast_d[3] = b;
         }
-        sync();
+        if (CL) {
+            csync();
+            if (rank == 0 && threadIdx.x == 0) {
+                double a = 0.0, b = 0.0;
+                const uint32_t nr = 1u << k;
+                for (uint32_t rr = 0; rr < nr; ++rr) {
+                    Shared* ps = peer_sh(rr);
+                    a += ps->bcast_d[2];
+                    b += ps->bcast_d[3];
+                }
+                const int cc = (int)(r < b);
+                const double sc = 1. / sqrt(cc ? b : a);
+                for (uint32_t rr = 0; rr < nr; ++rr) {
+                    Shared* ps = peer_sh(rr);
+                    ps->bcast_i[0] = cc;
+                    ps->bcast_d[0] = sc;
+                }
+            }
+            csync();
+        } else {
+            if (threadIdx.x == 0) {
+                const double a = sh->bcast_d[2], b = sh->bcast_d[3];
+                const int cc = (int)(r < b);
+                sh->bcast_i[0] = cc;
+                sh->bcast_d[0] = 1. / sqrt(cc ? b : a);
+            }
+            sync();
+        }
         const int cc = sh->bcast_i[0];
         const T sc = (T)sh->bcast_d[0];
-        for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
-            const bool keep = (int)((i >> q) & 1u) == cc;
+        for (uint32_t i = threadIdx.x; i < Nl; i += blockDim.x) {
+            const uint32_t bit = dq ? rbit(q) : ((i >> q) & 1u);
+            const bool keep = (int)bit == cc;
             re[pad(i)] = (keep ? re[pad(i)] : (T)0) * sc;
             im[pad(i)] = (keep ? im[pad(i)] : (T)0) * sc;
         }
         sync();
         return cc;
     }
+
+    // one draw from the chain's stream (rank 0, thread 0), broadcast to every thread
+    __device__ double draw() {
+        csync();
+        if (threadIdx.x == 0 && rank == 0) {
+            const double v = pcg_doub(*sh);
+            if (CL) {
+                for (uint32_t rr = 0; rr < (1u << k); ++rr) peer_sh(rr)->bcast_d[1] = v;
+            } else {
+                sh->bcast_d[1] = v;
+            }
+        }
+        csync();
+        return sh->bcast_d[1];
+    }
 };
 
-// one draw, made by thread 0 and broadcast
-__device__ __forceinline__ double draw(Shared& sh) {
-    __syncthreads();
-    if (threadIdx.x == 0) sh.bcast_d[1] = pcg_doub(sh);
-    __syncthreads();
-    return sh.bcast_d[1];
-}
-
-template <typename T>
+template <typename T, bool CL>
 struct Qms {
-    Ctx<T> cx;
+    Ctx<T, CL> cx;
     const DevChain* P;
     int s, e, acc;
     uint32_t L;
     uint32_t E_old;
     int gCi;
+    uint32_t nphi = 0;
 
     // exp(-iHt) on the spins, controlled on bit c (a phase-estimation target)
     __device__ void evolution(double t, int c) {
@@ -353,7 +495,7 @@ struct Qms {
             xs = (T)sn;
         }
         __syncthreads();
-        for (int k = 0; k < steps; ++k) cx.trotter_step(s, c, tc, ts, xc, xs);
+        for (int kk = 0; kk < steps; ++kk) cx.trotter_step(s, c, tc, ts, xc, xs);
     }
 
     __device__ void u1(int q, double phase) {
@@ -372,20 +514,21 @@ struct Qms {
     __device__ void qft(bool inverse) {
         if (!inverse) {
             for (int o = e - 1; o >= 0; o--) {
-                cx.h(s + o, -1);
+                cx.h(s + o);
                 for (int i = o - 1; i >= 0; i--) cu1(s + i, s + o, 2.0 * M_PI / (double)(1u << (1 + (o - i))));
             }
         } else {
             for (int o = 0; o < e; o++) {
                 for (int i = 0; i < o; i++) cu1(s + i, s + o, -(2.0 * M_PI / (double)(1u << (1 + (o - i)))));
-                cx.h(s + o, -1);
+                cx.h(s + o);
             }
         }
     }
 
     __device__ void phi() {
+        nphi++;
         const double t = P->t_pe;
-        for (int k = 0; k < e; ++k) cx.h(s + k, -1);
+        for (int kk = 0; kk < e; ++kk) cx.h(s + kk);
         for (int trg = e - 1; trg > -1; --trg) {
             const double powr = (double)(1u << (e - 1 - trg));
             evolution(-powr * t, s + trg);
@@ -395,6 +538,7 @@ struct Qms {
     }
 
     __device__ void phi_inverse() {
+        nphi++;
         const double t = P->t_pe;
         qft(false);
         for (int trg = 0; trg < e; ++trg) {
@@ -402,7 +546,7 @@ struct Qms {
             evolution(powr * t, s + trg);
             u1(s + trg, powr * t * P->t_shift);
         }
-        for (int k = 0; k < e; ++k) cx.h(s + k, -1);
+        for (int kk = 0; kk < e; ++kk) cx.h(s + kk);
     }
 
     __device__ void w() {
@@ -422,7 +566,7 @@ struct Qms {
     }
 
     __device__ void apply_U() {
-        cx.h(gCi, -1);
+        cx.h(gCi);
         phi();
         w();
     }
@@ -430,20 +574,19 @@ struct Qms {
     __device__ void apply_U_inverse() {
         w();
         phi_inverse();
-        cx.h(gCi, -1);
+        cx.h(gCi);
     }
 
     __device__ void reset(int q) {
-        const double r = draw(*cx.sh);
+        const double r = cx.draw();
         if (cx.measure(q, r)) cx.x(q);
     }
 
     __device__ uint32_t read_energy() {
+        double r[8];
+        for (int kk = 0; kk < e; ++kk) r[kk] = cx.draw();
         uint32_t v = 0;
-        for (int k = 0; k < e; ++k) {
-            const double r = draw(*cx.sh);
-            v += (uint32_t)cx.measure(s + k, r) << k;
-        }
+        for (int kk = 0; kk < e; ++kk) v += (uint32_t)cx.measure(s + kk, r[kk]) << kk;
         return v;
     }
 
@@ -451,14 +594,14 @@ struct Qms {
 
     __device__ double measure_magnetisation() {
         double r[24];
-        for (int i = 0; i < s; ++i) r[i] = draw(*cx.sh);
+        for (int i = 0; i < s; ++i) r[i] = cx.draw();
         double m = 0.0;
         for (int i = 0; i < s; ++i) m += cx.measure(i, r[i]) ? -1.0 : 1.0;
         return m;
     }
 
     __device__ int draw_C() {
-        const double xr = draw(*cx.sh);
+        const double xr = cx.draw();
         for (int i = 0; i < s; ++i) {
             const double wsum = (i + 1 == s) ? 1.0 : (double)(i + 1) / (double)s;
             if (xr < wsum) return i;
@@ -469,26 +612,26 @@ struct Qms {
     // one Metropolis step; returns 1/2 accepted (not/sampled), 3/4 restored, -1 failed
     __device__ int metro_step(bool take, double* Eout, double* Aout, bool* sampled) {
         *sampled = false;
-        for (int k = 0; k < e; ++k) reset(s + k);
+        for (int kk = 0; kk < e; ++kk) reset(s + kk);
         reset(acc);
         phi();
         const uint32_t eo = read_energy();
         E_old = eo;
-        for (int k = 0; k < e; ++k)
-            if ((eo >> k) & 1u) cx.x(s + k);
+        for (int kk = 0; kk < e; ++kk)
+            if ((eo >> kk) & 1u) cx.x(s + kk);
         gCi = draw_C();
         apply_U();
-        const int c_acc = cx.measure(acc, draw(*cx.sh));
+        const int c_acc = cx.measure(acc, cx.draw());
         if (c_acc == 1) {
             const uint32_t en = read_energy();
             phi_inverse();
             if (!take) return 1;
             *Eout = energy_of(en);
-            for (int k = 0; k < e; ++k)
-                if ((en >> k) & 1u) cx.x(s + k);
+            for (int kk = 0; kk < e; ++kk)
+                if ((en >> kk) & 1u) cx.x(s + kk);
             *Aout = measure_magnetisation();
             *sampled = true;
-            for (int k = 0; k < e; ++k) reset(s + k);
+            for (int kk = 0; kk < e; ++kk) reset(s + kk);
             phi();
             read_energy();
             phi_inverse();
@@ -504,10 +647,10 @@ struct Qms {
             if (E_old == en) {
                 if (take) {
                     *Eout = energy_of(E_old);
-                    for (int k = 0; k < e; ++k) reset(s + k);
+                    for (int kk = 0; kk < e; ++kk) reset(s + kk);
                     *Aout = measure_magnetisation();
                     *sampled = true;
-                    for (int k = 0; k < e; ++k) reset(s + k);
+                    for (int kk = 0; kk < e; ++kk) reset(s + kk);
                     phi();
                     read_energy();
                     phi_inverse();
@@ -518,7 +661,7 @@ struct Qms {
                 break;
             }
             apply_U();
-            cx.measure(acc, draw(*cx.sh));
+            cx.measure(acc, cx.draw());
             apply_U_inverse();
             iters++;
         }
@@ -527,38 +670,46 @@ struct Qms {
     }
 };
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads, 2) k_qms_tfim(const DevChain* __restrict__ chains, const int* __restrict__ order,
-                                                       int nchains, unsigned int* next, sq_chain_result* res,
-                                                       double* sE, double* sA, uint32_t* sStep, T* gbuf,
-                                                       int smem_qubits, int gbuf_qubits) {
+// Persistent chain loop.  CL = cluster mode (one chain per cluster of 2^k CTAs).
+template <typename T, bool CL>
+__global__ void __launch_bounds__(kThreads, 2) k_qms_tfim(const DevChain* __restrict__ chains,
+                                                          const int* __restrict__ order, int nchains,
+                                                          unsigned int* next, sq_chain_result* res, double* sE,
+                                                          double* sA, uint32_t* sStep, int kdist) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ Shared sh;
     __shared__ int cur;
+    const uint32_t rank = CL ? cg::this_cluster().block_rank() : 0u;
     for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) cur = (int)atomicAdd(next, 1u);
-        __syncthreads();
+        if (CL) cg::this_cluster().sync(); else __syncthreads();
+        if (threadIdx.x == 0 && rank == 0) {
+            const int c = (int)atomicAdd(next, 1u);
+            if (CL) {
+                for (uint32_t rr = 0; rr < (1u << kdist); ++rr) *cg::this_cluster().map_shared_rank(&cur, rr) = c;
+            } else {
+                cur = c;
+            }
+        }
+        if (CL) cg::this_cluster().sync(); else __syncthreads();
         if (cur >= nchains) return;
         const int ci = order[cur];
         const DevChain& P = chains[ci];
-        Qms<T> q;
+        Qms<T, CL> q;
         q.P = &P;
         q.s = P.s;
         q.e = P.e;
         q.acc = P.s + P.e;
         q.L = 1u << P.e;
         q.cx.n = P.n;
-        q.cx.N = 1u << P.n;
+        q.cx.k = CL ? kdist : 0;
+        q.cx.nl = P.n - q.cx.k;
+        q.cx.Nl = 1u << q.cx.nl;
+        q.cx.rank = rank;
         q.cx.sh = &sh;
-        if (P.n <= smem_qubits) {
-            q.cx.re = reinterpret_cast<T*>(smem_raw);
-        } else {
-            const size_t cap = ((size_t)1 << gbuf_qubits) + ((size_t)1 << gbuf_qubits) / 32 + 1;
-            q.cx.re = gbuf + (size_t)blockIdx.x * 2 * cap;
-        }
-        q.cx.im = q.cx.re + (q.cx.N + q.cx.N / 32 + 1);
-        if (threadIdx.x == 0) pcg_seed(sh, P.seed);
+        q.cx.re = reinterpret_cast<T*>(smem_raw);
+        q.cx.im = q.cx.re + (q.cx.Nl + q.cx.Nl / 32 + 1);
+        if (threadIdx.x == 0 && rank == 0) pcg_seed(sh, P.seed);
+        const long long t_start = clock64();
         q.cx.init();
         uint32_t s0 = 0, accepted = 0, failures = 0, ns = 0;
         for (uint32_t st = 0; st < (uint32_t)P.steps; ++st) {
@@ -566,7 +717,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_qms_tfim(const DevChain* __rest
             double E = 0.0, A = 0.0;
             bool sampled = false;
             const int ret = q.metro_step(take, &E, &A, &sampled);
-            if (threadIdx.x == 0 && sampled) {
+            if (threadIdx.x == 0 && rank == 0 && sampled) {
                 const size_t o = (size_t)P.out_offset + ns;
                 sE[o] = E;
                 sA[o] = A;
@@ -580,11 +731,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_qms_tfim(const DevChain* __rest
             }
             if (ret == 1 || ret == 2) accepted++;
         }
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0 && rank == 0) {
             res[ci].accepted = accepted;
             res[ci].failures = failures;
             res[ci].samples = ns;
-            res[ci].pad = 0;
+            res[ci].phase_estimations = q.nphi;
+            res[ci].cycles = (uint64_t)(clock64() - t_start);
         }
     }
 }
@@ -663,10 +815,6 @@ extern "C" int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, 
         if (classes.empty() || classes.back().n != n) classes.push_back({n, (int)k, 0});
         classes.back().count++;
     }
-    int gmax_grid = 0;
-    for (const auto& c : classes)
-        if (c.n > smem_q) gmax_grid = std::max(gmax_grid, std::min(c.count, nsm * 2));
-
     cudaStream_t st = (cudaStream_t)stream;
     DevChain* d_ch = nullptr;
     int* d_order = nullptr;
@@ -674,20 +822,18 @@ extern "C" int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, 
     sq_chain_result* d_res = nullptr;
     double *d_E = nullptr, *d_A = nullptr;
     uint32_t* d_step = nullptr;
-    void* d_g = nullptr;
-    const size_t gq = nmax > smem_q ? (size_t)nmax : 0;
     auto cleanup = [&]() {
         cudaFree(d_ch); cudaFree(d_order); cudaFree(d_next); cudaFree(d_res);
-        cudaFree(d_E); cudaFree(d_A); cudaFree(d_step); cudaFree(d_g);
+        cudaFree(d_E); cudaFree(d_A); cudaFree(d_step);
     };
+    if (nmax > smem_q + 4) return fail(SQ_ERR_ARG, "chain too wide for a 16-CTA cluster");
     if (cudaMalloc(&d_ch, sizeof(DevChain) * nchains) != cudaSuccess ||
         cudaMalloc(&d_order, sizeof(int) * nchains) != cudaSuccess ||
         cudaMalloc(&d_next, sizeof(unsigned int) * classes.size()) != cudaSuccess ||
         cudaMalloc(&d_res, sizeof(sq_chain_result) * nchains) != cudaSuccess ||
         cudaMalloc(&d_E, sizeof(double) * (total + 1)) != cudaSuccess ||
         cudaMalloc(&d_A, sizeof(double) * (total + 1)) != cudaSuccess ||
-        cudaMalloc(&d_step, sizeof(uint32_t) * (total + 1)) != cudaSuccess ||
-        (gq && cudaMalloc(&d_g, (size_t)gmax_grid * 2 * padded((int)gq) * esz) != cudaSuccess)) {
+        cudaMalloc(&d_step, sizeof(uint32_t) * (total + 1)) != cudaSuccess) {
         cudaGetLastError();
         cleanup();
         return fail(SQ_ERR_NOMEM, "device allocation for the chain batch failed");
@@ -702,22 +848,51 @@ extern "C" int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, 
     cudaError_t err = cudaSuccess;
     for (size_t ci = 0; ci < classes.size() && err == cudaSuccess; ++ci) {
         const Class& c = classes[ci];
-        const bool in_smem = c.n <= smem_q;
-        const size_t smem = in_smem ? 2 * padded(c.n) * esz : 16;
+        const int kd = c.n > smem_q ? c.n - smem_q : 0;  // distributed qubits
+        const int nl = c.n - kd;
+        const int csize = 1 << kd;
+        const size_t smem = 2 * padded(nl) * esz;
         int per_sm = (int)((size_t)(228 * 1024) / (smem + static_smem + 1024));
         per_sm = std::max(1, std::min(per_sm, 8));
-        int grid = in_smem ? nsm * per_sm : std::min(c.count, nsm * 2);
-        grid = std::min(grid, c.count);
-        if (precision == SQ_F64) {
-            cudaFuncSetAttribute(k_qms_tfim<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            k_qms_tfim<double><<<grid, kThreads, smem, st>>>(d_ch, d_order + c.first, c.count, d_next + ci, d_res,
-                                                             d_E, d_A, d_step, (double*)d_g, in_smem ? c.n : -1, (int)gq);
+        int groups = std::max(1, (nsm * per_sm) / csize);
+        groups = std::min(groups, c.count);
+        const unsigned grid = (unsigned)(groups * csize);
+        const int* ord = d_order + c.first;
+        unsigned int* nxt = d_next + ci;
+        if (kd == 0) {
+            if (precision == SQ_F64) {
+                cudaFuncSetAttribute(k_qms_tfim<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                k_qms_tfim<double, false><<<grid, kThreads, smem, st>>>(d_ch, ord, c.count, nxt, d_res, d_E, d_A, d_step, 0);
+            } else {
+                cudaFuncSetAttribute(k_qms_tfim<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                k_qms_tfim<float, false><<<grid, kThreads, smem, st>>>(d_ch, ord, c.count, nxt, d_res, d_E, d_A, d_step, 0);
+            }
         } else {
-            cudaFuncSetAttribute(k_qms_tfim<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            k_qms_tfim<float><<<grid, kThreads, smem, st>>>(d_ch, d_order + c.first, c.count, d_next + ci, d_res,
-                                                            d_E, d_A, d_step, (float*)d_g, in_smem ? c.n : -1, (int)gq);
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(grid, 1, 1);
+            cfg.blockDim = dim3(kThreads, 1, 1);
+            cfg.dynamicSmemBytes = smem;
+            cfg.stream = st;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = (unsigned)csize;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            if (precision == SQ_F64) {
+                auto kf = k_qms_tfim<double, true>;
+                cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (csize > 8) cudaFuncSetAttribute(kf, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+                err = cudaLaunchKernelEx(&cfg, kf, (const DevChain*)d_ch, ord, c.count, nxt, d_res, d_E, d_A, d_step, kd);
+            } else {
+                auto kf = k_qms_tfim<float, true>;
+                cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (csize > 8) cudaFuncSetAttribute(kf, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+                err = cudaLaunchKernelEx(&cfg, kf, (const DevChain*)d_ch, ord, c.count, nxt, d_res, d_E, d_A, d_step, kd);
+            }
         }
-        err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaGetLastError();
     }
     cudaEventRecord(e1, st);
     if (err == cudaSuccess) {

@@ -56,3 +56,26 @@ def test_batch_of_mixed_chains_each_matches_its_single_run():
         alone, _ = run_tfim_batch([chains[i]], "f64")
         assert alone[0].accepted == together[i].accepted
         assert np.array_equal(alone[0].E, together[i].E) and np.array_equal(alone[0].A, together[i].A)
+
+
+@pytest.mark.parametrize("spins,ene,steps", [(8, 5, 6), (10, 5, 3)])
+def test_cluster_chains_match_host_driven_driver(spins, ene, steps, tmp_path):
+    """Chains wider than one CTA's shared memory (14 and 16 qubits in FP64) run on
+    a 2- and 8-CTA cluster; their rows equal those of the host-driven drop-in
+    driver (libsq state API) for the same chain."""
+    import os
+    import subprocess
+    from suqa_gb300.batch import TfimChain, run_tfim_batch
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    c = TfimChain(spins=spins, ene_qbits=ene, steps=steps, beta=1.1, h=0.9, thermalization=0, seed=77,
+                  ene_min=-2.0 * spins, ene_max=2.0 * spins)
+    runs, _ = run_tfim_batch([c], "f64")
+    out = str(tmp_path / "drv.txt")
+    env = dict(os.environ, TFIM_J="1.0", TFIM_H="0.9")
+    cp = subprocess.run([os.path.join(root, "suqa_gb300", "_build", f"qms_tfim_s{spins}"), "1.1", str(steps), "1",
+                         str(ene), out, "--seed", "77", "--ene-min", str(-2.0 * spins), "--ene-max", str(2.0 * spins),
+                         "--thermalization", "0"], env=env, capture_output=True, text=True, timeout=1200)
+    assert cp.returncode == 0, cp.stderr[-2000:]
+    wE, wA = parse_rows(open(out).read())
+    E, A = runs[0].reference_rows(steps)
+    assert fmt(E) == wE and fmt(A) == wA

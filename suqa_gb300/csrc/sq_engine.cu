@@ -192,11 +192,25 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         }
         o.lflip = lf;
         o.lpair = (uint8_t)(lf ? __builtin_ctz(lf) : 0);
+        uint32_t lcm = 0, lcv = 0, lzy = 0;
+        for (int b = 0; b < n; ++b) {
+            const int lb = local_of(b);
+            if (lb < 0) continue;
+            if ((h.cmask >> b) & 1ull) {
+                lcm |= 1u << lb;
+                if ((h.cval >> b) & 1ull) lcv |= 1u << lb;
+            }
+            if ((h.zy >> b) & 1ull) lzy |= 1u << lb;
+        }
+        o.lcm = lcm;
+        o.lcv = lcv;
+        o.lzy = (h.kind == sqk::OP_PAULI) ? lzy : 0u;
         o.cmask = h.cmask;
         o.cval = h.cval;
         o.ocm = h.skm & outer;
         o.ocv = h.skv & o.ocm;
-        o.zy = h.zy;
+        // Pauli: the kernel takes the outer part of the sign parity per tile
+        o.zy = (h.kind == sqk::OP_PAULI) ? (h.zy & outer) : h.zy;
         o.shift = h.shift;
         o.c = h.c;
         o.s = h.s;

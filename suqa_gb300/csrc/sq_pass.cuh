@@ -20,7 +20,7 @@
 
 namespace sqk {
 
-constexpr int kMaxOps = 24;   // gates per launch (kernel parameter space <= 4 KB)
+constexpr int kMaxOps = 48;   // gates per launch (kernel parameters, ~6.4 KB)
 constexpr int kMaxTab = 128;  // complex table entries per launch (W factors, phase lists)
 constexpr int kMaxHigh = 16;  // tile qubits above the contiguous low block
 
@@ -36,19 +36,23 @@ enum OpKind : uint8_t {
     OP_SCALE = 8      // a *= s everywhere
 };
 
-// One gate in tile-local form (64 bytes).  For pair operations the pairs are
-// (t0, t0 ^ lflip) with t0 the tile index whose bit lpair is clear; control
-// conditions are tested on g0, the global index of t0.
+// One gate in tile-local form (88 bytes).  For pair operations the pairs are
+// (t0, t0 ^ lflip) with t0 the tile index whose bit lpair is clear.  Control
+// conditions are split into the tile-local part (lcm, lcv: bits of the tile
+// index, tested per element) and the outer part (ocm, ocv: tested once per tile).
 struct Op {
     uint8_t kind;
     uint8_t lpair;   // tile-local bit that orders the pair
     uint8_t ny;      // Pauli: number of Y factors
     uint8_t fz;      // Pauli: parity of (flip & zy)
     uint32_t lflip;  // tile-local flip mask
-    uint64_t cmask, cval;  // element condition
-    uint64_t ocm, ocv;     // part of the condition on qubits outside the tile
-    uint64_t zy;           // Pauli: Y|Z mask; PLIST/W: extraction mask
+    uint32_t lcm, lcv;     // tile-local control condition
+    uint32_t lzy;          // tile-local Y|Z mask (Pauli signs)
     uint32_t shift, tab;   // PLIST/W: shift and table offset (in complex entries)
+    uint32_t pad;
+    uint64_t cmask, cval;  // global element condition (diagonal slow paths)
+    uint64_t ocm, ocv;     // part of the condition on qubits outside the tile
+    uint64_t zy;           // Pauli: global Y|Z mask; PLIST/W: extraction mask
     double c, s;
 };
 
@@ -95,6 +99,23 @@ __device__ __forceinline__ void rot_k(T ar, T ai, T br, T bi, int k, T c, T s, T
     if (k >= 2) xi = -xi;
     outr = ar * c + xr * s;
     outi = ai * c + xi * s;
+}
+
+// Deferred-scale rotation: with cbig, out = a + u*(i^k b) (u = s/c, the factor c
+// deferred); otherwise out = u*a + i^k b (u = c/s, the factor s deferred).
+template <typename T>
+__device__ __forceinline__ void rot_deferred(T ar, T ai, T br, T bi, int k, T u, bool cbig, T& outr, T& outi) {
+    T xr = (k & 1) ? bi : br;
+    T xi = (k & 1) ? br : bi;
+    if (k == 1 || k == 2) xr = -xr;
+    if (k >= 2) xi = -xi;
+    if (cbig) {
+        outr = ar + u * xr;
+        outi = ai + u * xi;
+    } else {
+        outr = u * ar + xr;
+        outi = u * ai + xi;
+    }
 }
 
 template <typename T>
@@ -184,62 +205,138 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
         }
         __syncthreads();
 
-        // ---- gates
+        // ---- gates.  sigma is a per-tile scale deferred by uniform H and Pauli
+        // rotations (gates acting on every element of the tile): H stores
+        // (a0+a1, a0-a1) and multiplies sigma by 1/sqrt(2); a rotation
+        // c + i s P stores a + (s/c) iP a (or (c/s) a + iP a) and multiplies sigma
+        // by c (or s).  Every gate is linear, so sigma commutes with the rest of
+        // the pass and is applied once, before the reduction and the store.
+        double sigma = 1.0;
         for (int k = 0; k < p.nops; ++k) {
             const Op& op = p.ops[k];
             if ((base & op.ocm) != op.ocv) continue;
             const T c = (T)op.c, s = (T)op.s;
             const int kind = op.kind;
+            const uint32_t lcm = op.lcm, lcv = op.lcv;
             if (kind <= OP_PAULI && !(kind == OP_PAULI && op.lflip == 0u) || kind == OP_W) {
                 const uint32_t lp = op.lpair, lf = op.lflip;
-                for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
-                    const uint32_t t0 = insert_zero(pp, lp);
-                    const uint32_t t1 = t0 ^ lf;
-                    const uint64_t g0 = base | offs[t0 >> L] | (t0 & lowmask);
-                    if ((g0 & op.cmask) != op.cval) continue;
-                    const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
-                    if (kind == OP_SWAPP) {
-                        // include/suqa_cpu.hpp:223-253 (MCX), :268-319 (SWAP)
-                        sre[t0] = a1r; sim[t0] = a1i; sre[t1] = a0r; sim[t1] = a0i;
-                    } else if (kind == OP_YP) {
-                        // include/suqa_cpu.hpp:96-122: a1' = i a0, a0' = -i a1
+                if (kind == OP_SWAPP) {
+                    // include/suqa_cpu.hpp:223-253 (MCX), :268-319 (SWAP)
+                    for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
+                        const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
+                        if ((t0 & lcm) != lcv) continue;
+                        const T a0r = sre[t0], a0i = sim[t0];
+                        sre[t0] = sre[t1]; sim[t0] = sim[t1]; sre[t1] = a0r; sim[t1] = a0i;
+                    }
+                } else if (kind == OP_YP) {
+                    // include/suqa_cpu.hpp:96-122: a1' = i a0, a0' = -i a1
+                    for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
+                        const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
+                        if ((t0 & lcm) != lcv) continue;
+                        const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
                         sre[t1] = -a0i; sim[t1] = a0r; sre[t0] = a1i; sim[t0] = -a1r;
-                    } else if (kind == OP_HP) {
-                        // include/suqa_cpu.hpp:150-206
+                    }
+                } else if (kind == OP_HP) {
+                    // include/suqa_cpu.hpp:150-206
+                    if (lcm == 0u) {
+                        for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
+                            const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
+                            const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
+                            sre[t0] = a0r + a1r; sim[t0] = a0i + a1i;
+                            sre[t1] = a0r - a1r; sim[t1] = a0i - a1i;
+                        }
+                        sigma *= 0.7071067811865475;
+                    } else {
                         const T h = (T)0.7071067811865475;
-                        sre[t0] = h * (a0r + a1r); sim[t0] = h * (a0i + a1i);
-                        sre[t1] = h * (a0r - a1r); sim[t1] = h * (a0i - a1i);
-                    } else if (kind == OP_PAULI) {
-                        // exp(i th P): a0' = c a0 + i s w(g1) a1, a1' = c a1 + i s w(g0) a0
-                        const int pz0 = parity64(g0 & op.zy);
-                        const int k1 = 1 + op.ny + 2 * pz0;
-                        const int k0 = 1 + op.ny + 2 * (pz0 ^ op.fz);
-                        T r0, i0, r1, i1;
-                        rot_k<T>(a0r, a0i, a1r, a1i, k0 & 3, c, s, r0, i0);
-                        rot_k<T>(a1r, a1i, a0r, a0i, k1 & 3, c, s, r1, i1);
-                        sre[t0] = r0; sim[t0] = i0; sre[t1] = r1; sim[t1] = i1;
-                    } else {  // OP_W: include/qms.cuh:245-309
+                        for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
+                            const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
+                            if ((t0 & lcm) != lcv) continue;
+                            const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
+                            sre[t0] = h * (a0r + a1r); sim[t0] = h * (a0i + a1i);
+                            sre[t1] = h * (a0r - a1r); sim[t1] = h * (a0i - a1i);
+                        }
+                    }
+                } else if (kind == OP_PAULI) {
+                    // exp(i th P): a0' = c a0 + i s w(g1) a1, a1' = c a1 + i s w(g0) a0,
+                    // w(g) = i^ny (-1)^parity(g & zy); the outer part of the parity is per tile
+                    const int tpar = parity64(base & op.zy);
+                    const uint32_t lzy = op.lzy;
+                    const int ny = op.ny, fz = op.fz;
+                    if (lcm == 0u) {
+                        const bool cbig = fabs(op.c) >= fabs(op.s);
+                        const T u = cbig ? (T)(op.s / op.c) : (T)(op.c / op.s);
+                        for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
+                            const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
+                            const int pz0 = tpar ^ (__popc(t0 & lzy) & 1);
+                            const int k1 = (1 + ny + 2 * pz0) & 3;
+                            const int k0 = (1 + ny + 2 * (pz0 ^ fz)) & 3;
+                            const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
+                            T r0, i0, r1, i1;
+                            rot_deferred<T>(a0r, a0i, a1r, a1i, k0, u, cbig, r0, i0);
+                            rot_deferred<T>(a1r, a1i, a0r, a0i, k1, u, cbig, r1, i1);
+                            sre[t0] = r0; sim[t0] = i0; sre[t1] = r1; sim[t1] = i1;
+                        }
+                        sigma *= cbig ? op.c : op.s;
+                    } else {
+                        for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
+                            const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
+                            if ((t0 & lcm) != lcv) continue;
+                            const int pz0 = tpar ^ (__popc(t0 & lzy) & 1);
+                            const int k1 = (1 + ny + 2 * pz0) & 3;
+                            const int k0 = (1 + ny + 2 * (pz0 ^ fz)) & 3;
+                            const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
+                            T r0, i0, r1, i1;
+                            rot_k<T>(a0r, a0i, a1r, a1i, k0, c, s, r0, i0);
+                            rot_k<T>(a1r, a1i, a0r, a0i, k1, c, s, r1, i1);
+                            sre[t0] = r0; sim[t0] = i0; sre[t1] = r1; sim[t1] = i1;
+                        }
+                    }
+                } else {  // OP_W: include/qms.cuh:245-309
+                    for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
+                        const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
+                        const uint64_t g0 = base | offs[t0 >> L] | (t0 & lowmask);
                         const uint32_t e = (uint32_t)((g0 & op.zy) >> op.shift);
                         const T f1 = (T)p.tab[2 * (op.tab + e)], f2 = (T)p.tab[2 * (op.tab + e) + 1];
+                        const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
                         sre[t0] = f2 * a0r + f1 * a1r; sim[t0] = f2 * a0i + f1 * a1i;
                         sre[t1] = f1 * a0r - f2 * a1r; sim[t1] = f1 * a0i - f2 * a1i;
+                    }
+                }
+            } else if (kind == OP_PHASE) {
+                // include/suqa_kernels.cuh:175-190, :209-221
+                for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
+                    if ((t & lcm) != lcv) continue;
+                    const T ar = sre[t], ai = sim[t];
+                    sre[t] = ar * c - ai * s;
+                    sim[t] = ai * c + ar * s;
+                }
+            } else if (kind == OP_PAULI) {  // all-Z string: diagonal c + i s (-1)^parity
+                const int tpar = parity64(base & op.zy);
+                const uint32_t lzy = op.lzy;
+                if (lcm == 0u) {
+                    const bool cbig = fabs(op.c) >= fabs(op.s);
+                    const T u = cbig ? (T)(op.s / op.c) : (T)(op.c / op.s);
+                    for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
+                        const T ar = sre[t], ai = sim[t];
+                        T r, i;
+                        rot_deferred<T>(ar, ai, ar, ai, (1 + 2 * (tpar ^ (__popc(t & lzy) & 1))) & 3, u, cbig, r, i);
+                        sre[t] = r; sim[t] = i;
+                    }
+                    sigma *= cbig ? op.c : op.s;
+                } else {
+                    for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
+                        if ((t & lcm) != lcv) continue;
+                        const T ar = sre[t], ai = sim[t];
+                        T r, i;
+                        rot_k<T>(ar, ai, ar, ai, (1 + 2 * (tpar ^ (__popc(t & lzy) & 1))) & 3, c, s, r, i);
+                        sre[t] = r; sim[t] = i;
                     }
                 }
             } else {
                 for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
                     const uint64_t g = base | offs[t >> L] | (t & lowmask);
                     T ar = sre[t], ai = sim[t];
-                    if (kind == OP_PHASE) {
-                        // include/suqa_kernels.cuh:175-190, :209-221
-                        if ((g & op.cmask) != op.cval) continue;
-                        sre[t] = ar * c - ai * s;
-                        sim[t] = ai * c + ar * s;
-                    } else if (kind == OP_PAULI) {  // all-Z string: diagonal
-                        if ((g & op.cmask) != op.cval) continue;
-                        T r, i;
-                        rot_k<T>(ar, ai, ar, ai, 1 + 2 * parity64(g & op.zy), c, s, r, i);
-                        sre[t] = r; sim[t] = i;
-                    } else if (kind == OP_PLIST) {
+                    if (kind == OP_PLIST) {
                         // include/suqa_kernels.cuh:246-259 (guard: any gc bit set)
                         if ((g & op.cmask) == 0ull) continue;
                         const uint32_t e = (uint32_t)((g >> op.shift) & op.zy);
@@ -257,6 +354,14 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                         sim[t] = ai * s;
                     }
                 }
+            }
+            __syncthreads();
+        }
+        if (sigma != 1.0) {
+            const T sg = (T)sigma;
+            for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
+                sre[t] *= sg;
+                sim[t] *= sg;
             }
             __syncthreads();
         }

@@ -123,7 +123,12 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     for (size_t i = i0; i < i1; ++i) need |= ops[i].flip;
     int K = s->kp;
     const int needbits = popc(need | 3ull);
-    if ((int)s->n > small_max(s) && needbits > K) K = needbits;
+    if ((int)s->n > small_max(s)) {
+        // the smallest tile (of at least 2^10 amplitudes) that holds the pass's
+        // gates: smaller tiles keep more CTAs in flight on memory-bound passes
+        K = needbits > 10 ? needbits : 10;
+        if (K > s->kp && needbits <= s->kp) K = s->kp;
+    }
     if (K > n) K = n;
     if (K > tile_cap(s)) return fail(SQ_ERR_UNSUPPORTED, "gate touches too many qubits for one tile");
     // contiguous low block L, then the high tile qubits

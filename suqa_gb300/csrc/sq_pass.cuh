@@ -90,33 +90,39 @@ __device__ __forceinline__ uint32_t insert_zero(uint32_t p, uint32_t b) {
 
 __device__ __forceinline__ int parity64(uint64_t x) { return __popcll(x) & 1; }
 
-// out = c*a + s*(i^k * b), written as the reference's rotate2 (a*c -/+ x*s)
+// out = c*a + s*(i^k * b), the reference's rotate2 form (a*c -/+ x*s).  The
+// data-dependent sign of i^k is a select between +s and -s (computed once per
+// gate), which keeps it off the FP64 pipe.
 template <typename T>
-__device__ __forceinline__ void rot_k(T ar, T ai, T br, T bi, int k, T c, T s, T& outr, T& outi) {
-    T xr = (k & 1) ? bi : br;
-    T xi = (k & 1) ? br : bi;
-    if (k == 1 || k == 2) xr = -xr;
-    if (k >= 2) xi = -xi;
-    outr = ar * c + xr * s;
-    outi = ai * c + xi * s;
+__device__ __forceinline__ void rot_k(T ar, T ai, T br, T bi, int k, T c, T sp, T sn, T& outr, T& outi) {
+    const T xr = (k & 1) ? bi : br;
+    const T xi = (k & 1) ? br : bi;
+    const T fr = (k == 1 || k == 2) ? sn : sp;
+    const T fi = (k >= 2) ? sn : sp;
+    outr = ar * c + xr * fr;
+    outi = ai * c + xi * fi;
 }
 
 // Deferred-scale rotation: with cbig, out = a + u*(i^k b) (u = s/c, the factor c
 // deferred); otherwise out = u*a + i^k b (u = c/s, the factor s deferred).
+// up = +u, un = -u.
 template <typename T>
-__device__ __forceinline__ void rot_deferred(T ar, T ai, T br, T bi, int k, T u, bool cbig, T& outr, T& outi) {
-    T xr = (k & 1) ? bi : br;
-    T xi = (k & 1) ? br : bi;
-    if (k == 1 || k == 2) xr = -xr;
-    if (k >= 2) xi = -xi;
+__device__ __forceinline__ void rot_deferred(T ar, T ai, T br, T bi, int k, T up, T un, bool cbig, T& outr,
+                                             T& outi) {
+    const T xr = (k & 1) ? bi : br;
+    const T xi = (k & 1) ? br : bi;
+    const bool nr = (k == 1 || k == 2), ni = (k >= 2);
     if (cbig) {
-        outr = ar + u * xr;
-        outi = ai + u * xi;
+        outr = ar + xr * (nr ? un : up);
+        outi = ai + xi * (ni ? un : up);
     } else {
-        outr = u * ar + xr;
-        outi = u * ai + xi;
+        outr = nr ? (ar * up - xr) : (ar * up + xr);
+        outi = ni ? (ai * up - xi) : (ai * up + xi);
     }
 }
+
+__device__ __forceinline__ void scale_vec(double2& v, double s) { v.x *= s; v.y *= s; }
+__device__ __forceinline__ void scale_vec(float4& v, float s) { v.x *= s; v.y *= s; v.z *= s; v.w *= s; }
 
 template <typename T>
 __device__ __forceinline__ double sqnorm(T r, T i) {
@@ -215,7 +221,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
         for (int k = 0; k < p.nops; ++k) {
             const Op& op = p.ops[k];
             if ((base & op.ocm) != op.ocv) continue;
-            const T c = (T)op.c, s = (T)op.s;
+            const T c = (T)op.c, s = (T)op.s, sneg = (T)(-op.s);
             const int kind = op.kind;
             const uint32_t lcm = op.lcm, lcv = op.lcv;
             if (kind <= OP_PAULI && !(kind == OP_PAULI && op.lflip == 0u) || kind == OP_W) {
@@ -264,7 +270,8 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                     const int ny = op.ny, fz = op.fz;
                     if (lcm == 0u) {
                         const bool cbig = fabs(op.c) >= fabs(op.s);
-                        const T u = cbig ? (T)(op.s / op.c) : (T)(op.c / op.s);
+                        const double ud = cbig ? op.s / op.c : op.c / op.s;
+                        const T up = (T)ud, un = (T)(-ud);
                         for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
                             const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
                             const int pz0 = tpar ^ (__popc(t0 & lzy) & 1);
@@ -272,8 +279,8 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                             const int k0 = (1 + ny + 2 * (pz0 ^ fz)) & 3;
                             const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
                             T r0, i0, r1, i1;
-                            rot_deferred<T>(a0r, a0i, a1r, a1i, k0, u, cbig, r0, i0);
-                            rot_deferred<T>(a1r, a1i, a0r, a0i, k1, u, cbig, r1, i1);
+                            rot_deferred<T>(a0r, a0i, a1r, a1i, k0, up, un, cbig, r0, i0);
+                            rot_deferred<T>(a1r, a1i, a0r, a0i, k1, up, un, cbig, r1, i1);
                             sre[t0] = r0; sim[t0] = i0; sre[t1] = r1; sim[t1] = i1;
                         }
                         sigma *= cbig ? op.c : op.s;
@@ -286,8 +293,8 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                             const int k0 = (1 + ny + 2 * (pz0 ^ fz)) & 3;
                             const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
                             T r0, i0, r1, i1;
-                            rot_k<T>(a0r, a0i, a1r, a1i, k0, c, s, r0, i0);
-                            rot_k<T>(a1r, a1i, a0r, a0i, k1, c, s, r1, i1);
+                            rot_k<T>(a0r, a0i, a1r, a1i, k0, c, s, sneg, r0, i0);
+                            rot_k<T>(a1r, a1i, a0r, a0i, k1, c, s, sneg, r1, i1);
                             sre[t0] = r0; sim[t0] = i0; sre[t1] = r1; sim[t1] = i1;
                         }
                     }
@@ -315,11 +322,12 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                 const uint32_t lzy = op.lzy;
                 if (lcm == 0u) {
                     const bool cbig = fabs(op.c) >= fabs(op.s);
-                    const T u = cbig ? (T)(op.s / op.c) : (T)(op.c / op.s);
+                    const double ud = cbig ? op.s / op.c : op.c / op.s;
+                    const T up = (T)ud, un = (T)(-ud);
                     for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
                         const T ar = sre[t], ai = sim[t];
                         T r, i;
-                        rot_deferred<T>(ar, ai, ar, ai, (1 + 2 * (tpar ^ (__popc(t & lzy) & 1))) & 3, u, cbig, r, i);
+                        rot_deferred<T>(ar, ai, ar, ai, (1 + 2 * (tpar ^ (__popc(t & lzy) & 1))) & 3, up, un, cbig, r, i);
                         sre[t] = r; sim[t] = i;
                     }
                     sigma *= cbig ? op.c : op.s;
@@ -328,7 +336,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                         if ((t & lcm) != lcv) continue;
                         const T ar = sre[t], ai = sim[t];
                         T r, i;
-                        rot_k<T>(ar, ai, ar, ai, (1 + 2 * (tpar ^ (__popc(t & lzy) & 1))) & 3, c, s, r, i);
+                        rot_k<T>(ar, ai, ar, ai, (1 + 2 * (tpar ^ (__popc(t & lzy) & 1))) & 3, c, s, sneg, r, i);
                         sre[t] = r; sim[t] = i;
                     }
                 }
@@ -357,20 +365,14 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
             }
             __syncthreads();
         }
-        if (sigma != 1.0) {
-            const T sg = (T)sigma;
-            for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
-                sre[t] *= sg;
-                sim[t] *= sg;
-            }
-            __syncthreads();
-        }
+        const T sg = (T)sigma;
+        const double sg2 = sigma * sigma;
 
         // ---- reduction contribution and store
         if (p.red) {
             for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
                 const uint64_t g = base | offs[t >> L] | (t & lowmask);
-                const double w = sqnorm<T>(sre[t], sim[t]);
+                const double w = sqnorm<T>(sre[t], sim[t]) * sg2;
                 if (p.red == 1) {
                     if (g & p.rmask) acc1 += w; else acc0 += w;
                 } else if ((g & p.rmask) == p.rval) {
@@ -383,14 +385,20 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                 for (uint32_t v = threadIdx.x; v < TS / W; v += blockDim.x) {
                     const uint32_t t = v * W;
                     const uint64_t g = base | offs[t >> L] | (t & lowmask);
-                    __stcs(reinterpret_cast<V*>(gre + g), *reinterpret_cast<const V*>(sre + t));
-                    __stcs(reinterpret_cast<V*>(gim + g), *reinterpret_cast<const V*>(sim + t));
+                    V vr = *reinterpret_cast<const V*>(sre + t);
+                    V vi = *reinterpret_cast<const V*>(sim + t);
+                    if (sigma != 1.0) {
+                        scale_vec(vr, sg);
+                        scale_vec(vi, sg);
+                    }
+                    __stcs(reinterpret_cast<V*>(gre + g), vr);
+                    __stcs(reinterpret_cast<V*>(gim + g), vi);
                 }
             } else {
                 for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
                     const uint64_t g = base | offs[t >> L] | (t & lowmask);
-                    gre[g] = sre[t];
-                    gim[g] = sim[t];
+                    gre[g] = sre[t] * sg;
+                    gim[g] = sim[t] * sg;
                 }
             }
         }

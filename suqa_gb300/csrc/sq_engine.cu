@@ -123,12 +123,7 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     for (size_t i = i0; i < i1; ++i) need |= ops[i].flip;
     int K = s->kp;
     const int needbits = popc(need | 3ull);
-    if ((int)s->n > small_max(s)) {
-        // the smallest tile (of at least 2^10 amplitudes) that holds the pass's
-        // gates: smaller tiles keep more CTAs in flight on memory-bound passes
-        K = needbits > 10 ? needbits : 10;
-        if (K > s->kp && needbits <= s->kp) K = s->kp;
-    }
+    if ((int)s->n > small_max(s) && needbits > K) K = needbits;
     if (K > n) K = n;
     if (K > tile_cap(s)) return fail(SQ_ERR_UNSUPPORTED, "gate touches too many qubits for one tile");
     // contiguous low block L, then the high tile qubits
@@ -178,6 +173,7 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     static thread_local sqk::Prog p;
     p.nops = (int)(i1 - i0);
     p.red = red;
+    p.defer = 0;
     p.rmask = rmask;
     p.rval = rval;
     uint32_t tabpos = 0;
@@ -209,6 +205,7 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         }
         o.lcm = lcm;
         o.lcv = lcv;
+        if ((h.kind == sqk::OP_HP || h.kind == sqk::OP_PAULI) && lcm == 0u) p.defer++;
         o.lzy = (h.kind == sqk::OP_PAULI) ? lzy : 0u;
         o.cmask = h.cmask;
         o.cval = h.cval;
@@ -226,6 +223,7 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         }
     }
 
+    p.defer = p.defer >= 2 ? 1 : 0;  // deferring one factor costs as much as it saves
     const bool single = (K == n);
     const int block = single ? (K >= 10 ? 1024 : (K >= 8 ? 256 : 128)) : 256;
     int grid = (int)std::min<uint64_t>(a.ntiles, (uint64_t)s->max_grid);

@@ -59,6 +59,8 @@ struct Op {
 struct Prog {
     int nops;
     int red;             // 0 none, 1 measurement split by rmask, 2 filter (g & rmask) == rval
+    int defer;           // 1: uniform H / rotations defer their scale factor
+    int pad;
     uint64_t rmask, rval;
     Op ops[kMaxOps];
     double tab[2 * kMaxTab];
@@ -244,7 +246,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                     }
                 } else if (kind == OP_HP) {
                     // include/suqa_cpu.hpp:150-206
-                    if (lcm == 0u) {
+                    if (lcm == 0u && p.defer) {
                         for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
                             const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
                             const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                     const int tpar = parity64(base & op.zy);
                     const uint32_t lzy = op.lzy;
                     const int ny = op.ny, fz = op.fz;
-                    if (lcm == 0u) {
+                    if (lcm == 0u && p.defer) {
                         const bool cbig = fabs(op.c) >= fabs(op.s);
                         const double ud = cbig ? op.s / op.c : op.c / op.s;
                         const T up = (T)ud, un = (T)(-ud);
@@ -320,7 +322,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
             } else if (kind == OP_PAULI) {  // all-Z string: diagonal c + i s (-1)^parity
                 const int tpar = parity64(base & op.zy);
                 const uint32_t lzy = op.lzy;
-                if (lcm == 0u) {
+                if (lcm == 0u && p.defer) {
                     const bool cbig = fabs(op.c) >= fabs(op.s);
                     const double ud = cbig ? op.s / op.c : op.c / op.s;
                     const T up = (T)ud, un = (T)(-ud);

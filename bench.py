@@ -43,6 +43,9 @@ def parse():
     ap.add_argument("--no-fusion", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-qms", action="store_true")
+    ap.add_argument("--qms-chains", type=int, default=1024)
+    ap.add_argument("--qms-steps", type=int, default=3)
     return ap.parse_args()
 
 
@@ -133,6 +136,53 @@ def cpu_baseline(n, gates, seconds, bytes_per_amp):
     ost.close()
     alg = algorithmic_bytes(gates[:done], n, bytes_per_amp)
     return alg / dt / 1e9, done, threads, dt
+
+
+def qms_section(n_chains, steps, seed=2024):
+    """Batched quantum Metropolis sampling of TFIM rings: a sample of the
+    4096-chain workload (spins 4-10, energy register 4-6 qubits, J = 1,
+    h ~ U[0.5, 1.5], beta ~ U[0.2, 2.0], dt = 0.1, one PCG32 stream per chain),
+    run as FP32 and FP64 batches, against the host-driven plain GPU chain (the
+    drop-in qms driver on the libsq state API) on a 7-spin, 5-energy-qubit ring."""
+    import numpy as np
+    from suqa_gb300.batch import TfimChain, run_tfim_batch
+    rng = np.random.default_rng(seed)
+    chains = [TfimChain(spins=int(rng.integers(4, 11)), ene_qbits=int(rng.integers(4, 7)), steps=steps,
+                        beta=float(rng.uniform(0.2, 2.0)), h=float(rng.uniform(0.5, 1.5)), thermalization=0,
+                        seed=1 + i) for i in range(n_chains)]
+    out = {"workload": f"{n_chains} TFIM-ring chains x {steps} Metropolis steps (8-17 qubits)"}
+    runs = {}
+    for prec in ("f32", "f64"):
+        t0 = time.perf_counter()
+        r, ms = run_tfim_batch(chains, prec)
+        runs[prec] = r
+        out[prec] = {"chain_steps_per_s": n_chains * steps / (ms / 1e3), "device_ms": ms,
+                     "wall_s": time.perf_counter() - t0,
+                     "phase_estimations_per_step": float(np.mean([x.phase_estimations for x in r])) / steps}
+    # FP32 vs FP64 on identical chains and draws: identical measured sequences and energies
+    same = sum(1 for a, b in zip(runs["f32"], runs["f64"])
+               if a.accepted == b.accepted and np.array_equal(a.E, b.E) and np.array_equal(a.A, b.A))
+    e32 = np.concatenate([x.E for x in runs["f32"]])
+    e64 = np.concatenate([x.E for x in runs["f64"]])
+    out["fp32_vs_fp64"] = {"chains_identical": same, "chains": n_chains,
+                           "mean_E_f32": float(e32.mean()) if len(e32) else None,
+                           "mean_E_f64": float(e64.mean()) if len(e64) else None,
+                           "stderr_E_f64": float(e64.std() / max(1, len(e64)) ** 0.5) if len(e64) else None}
+    # plain GPU chain: one chain, one launch per fused gate group, host sync per measurement
+    exe = os.path.join(ROOT, "suqa_gb300", "_build", "qms_tfim_s7")
+    plain_steps = 4
+    env = dict(os.environ, TFIM_J="1.0", TFIM_H="1.0")
+    t0 = time.perf_counter()
+    cp = subprocess.run([exe, "1.0", str(plain_steps), "1", "5", "/tmp/suqa_plain_chain.txt", "--seed", "5",
+                         "--ene-min", "-14", "--ene-max", "14", "--thermalization", "0"], env=env,
+                        capture_output=True, text=True)
+    dt = time.perf_counter() - t0
+    if os.path.exists("/tmp/suqa_plain_chain.txt"):
+        os.remove("/tmp/suqa_plain_chain.txt")
+    plain = plain_steps / dt if cp.returncode == 0 else None
+    out["plain_gpu_chain"] = {"steps_per_s": plain, "config": "7 spins, 5 energy qubits (13 qubits), FP64"}
+    out["batched_f32_over_plain"] = (out["f32"]["chain_steps_per_s"] / plain) if plain else None
+    return out
 
 
 def run_reference_arm(args, rank, world):
@@ -260,6 +310,10 @@ def main():
                 "bytes_per_launch": kbytes / klaunch if klaunch else None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"}
 
+    qms = None
+    if rank == 0 and not args.skip_qms:
+        qms = qms_section(args.qms_chains, args.qms_steps)
+
     if rank == 0:
         cpu = None
         if not args.skip_cpu:
@@ -281,7 +335,8 @@ def main():
                 "e2e": {"value": e2e_value, "unit": "GB/s", "ms_per_step": ms_e2e,
                         "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes},
                 "roofline": roofline,
-                "cpu_baseline": cpu}
+                "cpu_baseline": cpu,
+                "qms_batched": qms}
         print(json.dumps(line), flush=True)
     st.close()
     if dist is not None:

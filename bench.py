@@ -180,8 +180,17 @@ def qms_section(n_chains, steps, seed=2024):
     if os.path.exists("/tmp/suqa_plain_chain.txt"):
         os.remove("/tmp/suqa_plain_chain.txt")
     plain = plain_steps / dt if cp.returncode == 0 else None
-    out["plain_gpu_chain"] = {"steps_per_s": plain, "config": "7 spins, 5 energy qubits (13 qubits), FP64"}
-    out["batched_f32_over_plain"] = (out["f32"]["chain_steps_per_s"] / plain) if plain else None
+    # the same chain run by the batch engine has identical outcomes, hence the same
+    # number of phase estimations: the per-estimation rate removes the seed-dependent
+    # length of the restoration loops from the comparison
+    same, _ = run_tfim_batch([TfimChain(spins=7, ene_qbits=5, steps=plain_steps, beta=1.0, h=1.0, ene_min=-14.0,
+                                        ene_max=14.0, thermalization=0, seed=5)], "f64")
+    plain_pe = same[0].phase_estimations / dt if cp.returncode == 0 else None
+    f32_pe = out["f32"]["phase_estimations_per_step"] * out["f32"]["chain_steps_per_s"]
+    out["plain_gpu_chain"] = {"steps_per_s": plain, "phase_estimations_per_s": plain_pe,
+                              "config": "7 spins, 5 energy qubits (13 qubits), FP64, host-driven (libsq state API)"}
+    out["batched_f32_over_plain_steps"] = (out["f32"]["chain_steps_per_s"] / plain) if plain else None
+    out["batched_f32_over_plain_phase_estimations"] = (f32_pe / plain_pe) if plain_pe else None
     return out
 
 
@@ -295,6 +304,26 @@ def main():
     e2e_value = alg * world / (ms_e2e / 1e3) / 1e9
     state_bytes = (1 << n) * bpa  # re + im
 
+    # FP64 peak of this GPU, measured here with cuBLAS DGEMM (the pass kernel's
+    # arithmetic bound in FP64)
+    fp64_peak = None
+    try:
+        xa = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+        xb = torch.randn_like(xa)
+        torch.matmul(xa, xb)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(3):
+            torch.matmul(xa, xb)
+        ev1.record()
+        torch.cuda.synchronize()
+        fp64_peak = 3 * 2 * 8192 ** 3 / (ev0.elapsed_time(ev1) / 1e3) / 1e12
+        del xa, xb
+        torch.cuda.empty_cache()
+    except Exception:
+        pass
+
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -308,7 +337,43 @@ def main():
                 "kernel": "sqk::k_pass<%s>" % ("double" if args.precision == "f64" else "float"),
                 "launches": klaunch, "avg_launch_ms": kms / klaunch if klaunch else None,
                 "bytes_per_launch": kbytes / klaunch if klaunch else None,
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"}
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback",
+                "fp64_tflops_achieved": stats["flops"] / (kms / 1e3) / 1e12 if kms > 0 else None,
+                "fp64_tflops_peak": fp64_peak,
+                "fp64_frac": (stats["flops"] / (kms / 1e3) / 1e12 / fp64_peak) if (kms > 0 and fp64_peak) else None,
+                "fp64_peak_source": "cuBLAS DGEMM 8192^3 measured in this run"}
+
+    # secondary: the same circuit with FP32 amplitudes (FP64 reductions)
+    fp32_line = None
+    if args.precision == "f64" and rank == 0:
+        st.close()
+        st32 = State(n, "f32")
+        st32.set_stream(stream.cuda_stream)
+        r32, i32 = random_state(n, 7, np.float32)
+        h32r = torch.from_numpy(r32).pin_memory()
+        h32i = torch.from_numpy(i32).pin_memory()
+        st32.upload(h32r.data_ptr(), h32i.data_ptr())
+        apply_circuit(st32, gates)
+        st32.flush()
+        torch.cuda.synchronize()
+        st32.set_timing(True)
+        st32.kernel_time()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.steps):
+            apply_circuit(st32, gates)
+        st32.flush()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ms32 = f0.elapsed_time(f1) / args.steps
+        k32, l32, b32 = st32.kernel_time()
+        alg32 = algorithmic_bytes(gates, n, 8)
+        fp32_line = {"value": alg32 / (ms32 / 1e3) / 1e9, "unit": "GB/s", "ms_per_step": ms32,
+                     "gates_per_s": len([g for g in gates if g[0] != "measure"]) / (ms32 / 1e3),
+                     "pass_kernel_gbs": b32 / (k32 / 1e3) / 1e9 if k32 > 0 else None}
+        st32.close()
+        del h32r, h32i
+        st = None
 
     qms = None
     if rank == 0 and not args.skip_qms:
@@ -336,9 +401,11 @@ def main():
                         "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes},
                 "roofline": roofline,
                 "cpu_baseline": cpu,
+                "fp32_same_circuit": fp32_line,
                 "qms_batched": qms}
         print(json.dumps(line), flush=True)
-    st.close()
+    if st is not None:
+        st.close()
     if dist is not None:
         dist.destroy_process_group()
 

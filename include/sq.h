@@ -125,6 +125,9 @@ typedef struct sq_stats {
     uint64_t launches;     /* kernel launches */
     uint64_t reductions;   /* measurement / filter reductions */
     uint64_t bytes_moved;  /* bytes read + written by executed passes (algorithmic) */
+    uint64_t flops;        /* floating-point operations of the executed gates and reductions
+                              (reference formulas: 4/amplitude for H, 6 for a phase or a
+                              Pauli rotation on the amplitudes it touches, 0 for X/CX/MCX/SWAP) */
 } sq_stats;
 int sq_get_stats(const sq_state* s, sq_stats* out);
 int sq_reset_stats(sq_state* s);

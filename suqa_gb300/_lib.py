@@ -25,7 +25,7 @@ class SqUnsupported(SqError):
 
 class SqStats(C.Structure):
     _fields_ = [("gates", C.c_uint64), ("passes", C.c_uint64), ("launches", C.c_uint64),
-                ("reductions", C.c_uint64), ("bytes_moved", C.c_uint64)]
+                ("reductions", C.c_uint64), ("bytes_moved", C.c_uint64), ("flops", C.c_uint64)]
 
 
 class SqTfimChain(C.Structure):

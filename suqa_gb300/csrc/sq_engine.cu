@@ -250,6 +250,26 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         s->ev_open.push_back({e0, e1});
         s->ev_bytes.push_back(moved);
     }
+    // algorithmic flops: per amplitude the gate touches (tiles enumerated x 2^K x fraction)
+    {
+        const double amps = (double)a.ntiles * (double)((uint64_t)1 << K);
+        double fl = 0.0;
+        for (size_t i = i0; i < i1; ++i) {
+            const HostOp& h = ops[i];
+            const double frac = 1.0 / (double)(1ull << popc(h.cmask & ~h.flip));
+            switch (h.kind) {
+                case sqk::OP_HP: fl += 4.0 * amps * frac; break;
+                case sqk::OP_PAULI: fl += 6.0 * amps * frac; break;
+                case sqk::OP_PHASE: fl += 6.0 * amps * frac; break;
+                case sqk::OP_PLIST: fl += 6.0 * amps; break;
+                case sqk::OP_W: fl += 6.0 * amps; break;
+                case sqk::OP_COLLAPSE: case sqk::OP_SCALE: fl += 2.0 * amps; break;
+                default: break;
+            }
+        }
+        if (red) fl += 4.0 * amps;
+        s->stats.flops += (uint64_t)fl;
+    }
     s->stats.passes++;
     s->stats.launches++;
     s->stats.bytes_moved += moved;

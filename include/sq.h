@@ -156,6 +156,10 @@ typedef struct sq_tfim_chain {
     double ene_min, ene_max;  /* phase-estimation window */
     double dt;                /* Trotter step width */
     uint64_t seed;            /* PCG32 seed, stream 1 (as pcg::set_seed) */
+    uint32_t warm_start;      /* 1: the initial state is RY(ry[i]) on spin i applied to |0...0>
+                                 (also after a failed restoration); 0: |0...0> */
+    uint32_t pad;
+    double ry[20];
 } sq_tfim_chain;
 
 typedef struct sq_chain_result {
@@ -173,6 +177,25 @@ typedef struct sq_chain_result {
  * index).  kernel_ms (may be NULL) receives the device time of the launches. */
 int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, int precision, sq_chain_result* results,
                       double* samples_E, double* samples_A, uint32_t* samples_step, void* stream, float* kernel_ms);
+
+/* --- learned warm start: a small MLP with BF16 weights/activations, FP32 sums ---
+ * No reference counterpart.  in -> `layers` hidden layers of `hidden` GELU units
+ * -> out.  Parameters are one flat FP32 array (W_l row-major, then b_l, layer by
+ * layer).  Host arrays throughout: x[batch][in], y/targets/mask[batch][out].
+ * Loss: mean over rows of sum_k mask*(y - t)^2.  train_step = forward, backward
+ * and one Adam update (beta 0.9/0.999, eps 1e-8) on the FP32 master weights. */
+typedef struct sq_mlp sq_mlp;
+int sq_mlp_create(sq_mlp** out, uint32_t in, uint32_t hidden, uint32_t layers, uint32_t out_dim, uint64_t seed);
+int sq_mlp_destroy(sq_mlp* n);
+int sq_mlp_num_params(const sq_mlp* n, uint32_t* count);
+int sq_mlp_get_params(sq_mlp* n, float* flat);
+int sq_mlp_set_params(sq_mlp* n, const float* flat);
+int sq_mlp_forward(sq_mlp* n, const float* x, uint32_t batch, float* y);
+/* gradient of the loss w.r.t. the flat parameters (for checks against a CPU reference) */
+int sq_mlp_gradients(sq_mlp* n, const float* x, const float* targets, const float* mask, uint32_t batch,
+                     float* grad, float* loss);
+int sq_mlp_train_step(sq_mlp* n, const float* x, const float* targets, const float* mask, uint32_t batch, float lr,
+                      float* loss);
 
 /* --- allocation-free measurement probabilities (no counterpart in the reference) ---
  * For callers that may not allocate device memory on the call path: their host

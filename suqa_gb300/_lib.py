@@ -32,7 +32,8 @@ class SqTfimChain(C.Structure):
     _fields_ = [("spins", C.c_uint32), ("ene_qbits", C.c_uint32), ("steps", C.c_uint32),
                 ("thermalization", C.c_uint32), ("reset_each", C.c_uint32), ("max_reverse", C.c_uint32),
                 ("J", C.c_double), ("h", C.c_double), ("beta", C.c_double), ("ene_min", C.c_double),
-                ("ene_max", C.c_double), ("dt", C.c_double), ("seed", C.c_uint64)]
+                ("ene_max", C.c_double), ("dt", C.c_double), ("seed", C.c_uint64),
+                ("warm_start", C.c_uint32), ("pad", C.c_uint32), ("ry", C.c_double * 20)]
 
 
 class SqChainResult(C.Structure):
@@ -79,6 +80,16 @@ _SIGS = {
     "sq_kernel_time": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "sq_qms_tfim_batch": (C.c_int, [C.POINTER(SqTfimChain), C.c_uint32, C.c_int, C.POINTER(SqChainResult),
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_float)]),
+    "sq_mlp_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64]),
+    "sq_mlp_destroy": (C.c_int, [C.c_void_p]),
+    "sq_mlp_num_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
+    "sq_mlp_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sq_mlp_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sq_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "sq_mlp_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                   C.POINTER(C.c_float)]),
+    "sq_mlp_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_float,
+                                    C.POINTER(C.c_float)]),
     "sq_qubit_probs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_uint32, C.c_void_p,
                                          C.c_void_p]),
 }

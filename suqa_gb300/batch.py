@@ -27,6 +27,7 @@ class TfimChain:
     max_reverse: int = 100
     dt: float = 0.1
     seed: int = 1
+    warm_angles: list | None = None  # per-spin RY angles of a learned warm start
 
     def window(self):
         """Phase-estimation window; by default +-s(|J|+|h|), a bound of the spectrum."""
@@ -69,6 +70,10 @@ def run_tfim_batch(chains: list[TfimChain], precision: str = "f32", stream: int 
         lo, hi = c.window()
         arr[i] = SqTfimChain(c.spins, c.ene_qbits, c.steps, c.thermalization, c.reset_each, c.max_reverse,
                              c.J, c.h, c.beta, lo, hi, c.dt, c.seed)
+        if c.warm_angles is not None:
+            arr[i].warm_start = 1
+            for k, a in enumerate(c.warm_angles[:20]):
+                arr[i].ry[k] = float(a)
     res = (SqChainResult * n)()
     total = sum(c.steps for c in chains)
     E = np.zeros(max(total, 1), dtype=np.float64)

@@ -46,6 +46,8 @@ struct DevChain {
     double t_pe, t_shift, pe_factor, c_factor;  // as the reference driver computes them
     uint64_t seed;
     int out_offset;  // first sample slot of this chain
+    int warm;
+    double ry[20];   // warm-start RY angles per spin
 };
 
 struct Shared {
@@ -195,6 +197,19 @@ struct Ctx {
             im[pad(i0)] = im[pad(i1)];
             re[pad(i1)] = r;
             im[pad(i1)] = i;
+        }
+        sync();
+    }
+
+    // RY(theta) on a local qubit: a0' = c a0 - s a1, a1' = s a0 + c a1 (c, s of theta/2)
+    __device__ void ry(int q, T cs, T sn) {
+        for (uint32_t p = threadIdx.x; p < Nl / 2; p += blockDim.x) {
+            const uint32_t i0 = ins0(p, (uint32_t)q), i1 = i0 | (1u << q);
+            const T a0r = re[pad(i0)], a0i = im[pad(i0)], a1r = re[pad(i1)], a1i = im[pad(i1)];
+            re[pad(i0)] = cs * a0r - sn * a1r;
+            im[pad(i0)] = cs * a0i - sn * a1i;
+            re[pad(i1)] = sn * a0r + cs * a1r;
+            im[pad(i1)] = sn * a0i + cs * a1i;
         }
         sync();
     }
@@ -592,6 +607,19 @@ struct Qms {
 
     __device__ double energy_of(uint32_t v) const { return P->t_shift + v / (double)(P->pe_factor * L); }
 
+    // the system's initial state: |0...0>, or the learned warm start RY(ry_i) per spin
+    __device__ void init_state() {
+        cx.init();
+        if (P->warm) {
+            for (int i = 0; i < s; ++i) {
+                double sn, cs;
+                sincos(0.5 * P->ry[i], &sn, &cs);
+                cx.ry(i, (T)cs, (T)sn);
+            }
+            cx.csync();
+        }
+    }
+
     __device__ double measure_magnetisation() {
         double r[24];
         for (int i = 0; i < s; ++i) r[i] = cx.draw();
@@ -710,7 +738,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_qms_tfim(const DevChain* __rest
         q.cx.im = q.cx.re + (q.cx.Nl + q.cx.Nl / 32 + 1);
         if (threadIdx.x == 0 && rank == 0) pcg_seed(sh, P.seed);
         const long long t_start = clock64();
-        q.cx.init();
+        q.init_state();
         uint32_t s0 = 0, accepted = 0, failures = 0, ns = 0;
         for (uint32_t st = 0; st < (uint32_t)P.steps; ++st) {
             const bool take = (st > s0 + (uint32_t)P.therm) && ((st - s0) % (uint32_t)P.reset_each == 0u);
@@ -725,7 +753,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_qms_tfim(const DevChain* __rest
             }
             if (sampled) ns++;
             if (ret < 0) {
-                q.cx.init();
+                q.init_state();
                 s0 = st + 1;
                 failures++;
             }
@@ -791,6 +819,8 @@ extern "C" int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, 
         d.c_factor = c.beta / (d.pe_factor * L);
         d.seed = c.seed;
         d.out_offset = (int)total;
+        d.warm = c.warm_start ? 1 : 0;
+        for (int k = 0; k < 20; ++k) d.ry[k] = c.ry[k];
         total += c.steps;
         if (d.n > nmax) nmax = d.n;
     }

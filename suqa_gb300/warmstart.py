@@ -1,0 +1,139 @@
+"""Learned warm start for QMS chains of transverse-field Ising rings.
+
+A small network (inputs: spin count, J, h, beta; 3 hidden layers of 128 GELU
+units; outputs: one RY angle per spin, up to 12) is trained on the GPU by the
+libsq kernels (sq_mlp_*) on data produced by plain cold-start chains, and its
+angles prepare the chains' initial product state RY(theta_i)|0> in place of
+|0...0>.  The Metropolis steps themselves are unchanged; the cold start stays
+the fallback and the judge of the thermal averages.
+
+Training target: the chains' equilibrium energy E of a parameter set is turned
+into the angle of the product state with that energy,
+    E(theta) = -J s cos(theta)^2 - h s sin(theta)   (all spins at theta),
+solved on the branch theta in [-pi/2, theta_min] that runs from E = +h s down to
+the product-state minimum (bisection; energies outside the range are clamped).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+MAX_SPINS = 12
+
+
+def features(spins, J, h, beta):
+    return np.array([spins / 12.0, J, h, beta], dtype=np.float32)
+
+
+def product_energy(theta, spins, J, h):
+    return -J * spins * math.cos(theta) ** 2 - h * spins * math.sin(theta)
+
+
+def angle_for_energy(E, spins, J, h):
+    """Product-state angle whose energy is E (see the module docstring)."""
+    # minimum of E(theta) on [-pi/2, pi/2]: sin(theta*) = h / (2J) if h < 2J else pi/2
+    tmin = math.asin(min(1.0, h / (2.0 * J))) if J > 0 else math.pi / 2
+    lo, hi = -math.pi / 2, tmin  # E decreases from +h s at lo to its minimum at hi
+    if E >= product_energy(lo, spins, J, h):
+        return lo
+    if E <= product_energy(hi, spins, J, h):
+        return hi
+    for _ in range(80):
+        mid = 0.5 * (lo + hi)
+        if product_energy(mid, spins, J, h) > E:
+            lo = mid
+        else:
+            hi = mid
+    return 0.5 * (lo + hi)
+
+
+class WarmStartNet:
+    def __init__(self, hidden=128, layers=3, seed=1):
+        self.L = _lib.load()
+        h = C.c_void_p()
+        check(self.L.sq_mlp_create(C.byref(h), 4, hidden, layers, MAX_SPINS, seed))
+        self.h = h
+        n = C.c_uint32()
+        check(self.L.sq_mlp_num_params(self.h, C.byref(n)))
+        self.nparams = n.value
+        self.dims = [4] + [hidden] * layers + [MAX_SPINS]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sq_mlp_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def params(self):
+        p = np.empty(self.nparams, dtype=np.float32)
+        check(self.L.sq_mlp_get_params(self.h, p.ctypes.data_as(C.c_void_p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(self.L.sq_mlp_set_params(self.h, p.ctypes.data_as(C.c_void_p)))
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.empty((x.shape[0], MAX_SPINS), dtype=np.float32)
+        check(self.L.sq_mlp_forward(self.h, x.ctypes.data_as(C.c_void_p), x.shape[0], y.ctypes.data_as(C.c_void_p)))
+        return y
+
+    def gradients(self, x, t, mask=None):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+        g = np.empty(self.nparams, dtype=np.float32)
+        loss = C.c_float()
+        check(self.L.sq_mlp_gradients(self.h, x.ctypes.data_as(C.c_void_p), t.ctypes.data_as(C.c_void_p),
+                                      None if m is None else m.ctypes.data_as(C.c_void_p), x.shape[0],
+                                      g.ctypes.data_as(C.c_void_p), C.byref(loss)))
+        return g, loss.value
+
+    def train_step(self, x, t, mask=None, lr=1e-3):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+        loss = C.c_float()
+        check(self.L.sq_mlp_train_step(self.h, x.ctypes.data_as(C.c_void_p), t.ctypes.data_as(C.c_void_p),
+                                       None if m is None else m.ctypes.data_as(C.c_void_p), x.shape[0], lr,
+                                       C.byref(loss)))
+        return loss.value
+
+    def fit(self, x, t, mask, iters=2000, batch=256, lr=2e-3, seed=0):
+        rng = np.random.default_rng(seed)
+        losses = []
+        for it in range(iters):
+            idx = rng.integers(0, x.shape[0], size=min(batch, x.shape[0]))
+            losses.append(self.train_step(x[idx], t[idx], mask[idx], lr))
+        return losses
+
+    def angles(self, spins, J, h, beta):
+        y = self.forward(features(spins, J, h, beta)[None, :])[0]
+        return [float(a) for a in y[:spins]]
+
+
+def training_set(chains, runs, burn_in):
+    """(x, target angles, mask) from plain chains: the mean energy of each chain's
+    samples after burn_in steps gives its parameter set's target angle."""
+    xs, ts, ms = [], [], []
+    for c, r in zip(chains, runs):
+        keep = r.step >= burn_in
+        if not np.any(keep):
+            continue
+        E = float(np.mean(r.E[keep]))
+        th = angle_for_energy(E, c.spins, c.J, c.h)
+        xs.append(features(c.spins, c.J, c.h, c.beta))
+        t = np.zeros(MAX_SPINS, np.float32)
+        m = np.zeros(MAX_SPINS, np.float32)
+        t[:c.spins] = th
+        m[:c.spins] = 1.0
+        ts.append(t)
+        ms.append(m)
+    return np.array(xs), np.array(ts), np.array(ms)

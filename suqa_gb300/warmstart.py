@@ -137,3 +137,58 @@ def training_set(chains, runs, burn_in):
         ts.append(t)
         ms.append(m)
     return np.array(xs), np.array(ts), np.array(ms)
+
+
+def burn_in_experiment(spins=(4, 5, 6), ene_qbits=4, train_chains=512, train_steps=12, train_burn=6,
+                       eval_groups=((6, 1.0, 0.3), (6, 1.0, 1.0), (6, 0.7, 1.8)), eval_chains=96, eval_steps=8,
+                       precision="f32", iters=1500, seed=7):
+    """Trains the network on plain cold-start chains and compares warm- and
+    cold-started chains of held-out parameter sets.  Returns a dict with, per
+    group, the equilibrium energy (cold chains after burn-in), the mean energy
+    error of the first samples for cold and warm starts, and the number of steps
+    each start needs before its step-averaged energy stays within two standard
+    errors of equilibrium."""
+    from .batch import TfimChain, run_tfim_batch
+    rng = np.random.default_rng(seed)
+    chains = [TfimChain(spins=int(rng.choice(spins)), ene_qbits=ene_qbits, steps=train_steps,
+                        beta=float(rng.uniform(0.2, 2.0)), h=float(rng.uniform(0.5, 1.5)), thermalization=0,
+                        seed=10_000 + i) for i in range(train_chains)]
+    runs, ms_data = run_tfim_batch(chains, precision)
+    x, t, m = training_set(chains, runs, train_burn)
+    net = WarmStartNet(seed=seed)
+    losses = net.fit(x, t, m, iters=iters, batch=256, lr=2e-3, seed=seed)
+    out = {"train_samples": int(sum(len(r.E) for r in runs)), "train_rows": int(x.shape[0]),
+           "data_device_ms": ms_data, "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-20:])),
+           "groups": []}
+    for gi, (s, h, beta) in enumerate(eval_groups):
+        base = dict(spins=s, ene_qbits=ene_qbits, steps=eval_steps, beta=beta, h=h, thermalization=0)
+        cold = [TfimChain(seed=50_000 + 1000 * gi + k, **base) for k in range(eval_chains)]
+        ang = net.angles(s, 1.0, h, beta)
+        warm = [TfimChain(seed=50_000 + 1000 * gi + k, warm_angles=ang, **base) for k in range(eval_chains)]
+        rc, _ = run_tfim_batch(cold, precision)
+        rw, _ = run_tfim_batch(warm, precision)
+
+        def per_step(rr):
+            mat = np.full((len(rr), eval_steps), np.nan)
+            for i, r in enumerate(rr):
+                mat[i, r.step.astype(int)] = r.E
+            return np.nanmean(mat, axis=0), np.nanstd(mat, axis=0) / np.sqrt(np.sum(~np.isnan(mat), axis=0))
+
+        mc, sc = per_step(rc)
+        mw, _ = per_step(rw)
+        eq = float(np.nanmean(mc[eval_steps // 2:]))
+        err = float(np.nanmean(sc[eval_steps // 2:]))
+        first = slice(0, 3)
+
+        def burn(mean):
+            for k in range(eval_steps):
+                if np.all(np.abs(mean[k:] - eq) <= 2 * err + 1e-12):
+                    return k
+            return eval_steps
+
+        out["groups"].append({"spins": s, "h": h, "beta": beta, "E_eq": eq, "E_eq_err": err,
+                              "warm_angle": ang[0], "cold_first_err": float(np.mean(np.abs(mc[first] - eq))),
+                              "warm_first_err": float(np.mean(np.abs(mw[first] - eq))),
+                              "cold_burn_in_steps": burn(mc), "warm_burn_in_steps": burn(mw)})
+    net.close()
+    return out

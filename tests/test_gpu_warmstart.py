@@ -38,3 +38,15 @@ def test_training_reduces_loss():
     mask = np.ones_like(target)
     losses = net.fit(x, target, mask, iters=400, batch=128, lr=2e-3)
     assert np.mean(losses[-20:]) < 0.1 * np.mean(losses[:20])
+
+
+def test_warm_start_shortens_burn_in():
+    """Chains started from the trained network's product state are closer to the
+    equilibrium energy in their first steps than cold-started chains."""
+    from suqa_gb300.warmstart import burn_in_experiment
+    res = burn_in_experiment()
+    print(res)
+    assert res["loss_last"] < res["loss_first"]
+    cold = np.mean([g["cold_first_err"] for g in res["groups"]])
+    warm = np.mean([g["warm_first_err"] for g in res["groups"]])
+    assert warm < cold, (warm, cold)

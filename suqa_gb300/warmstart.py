@@ -178,17 +178,17 @@ def burn_in_experiment(spins=(4, 5, 6), ene_qbits=4, train_chains=512, train_ste
         mw, _ = per_step(rw)
         eq = float(np.nanmean(mc[eval_steps // 2:]))
         err = float(np.nanmean(sc[eval_steps // 2:]))
-        first = slice(0, 3)
+        first = slice(1, 4)  # step 0 is never sampled (the driver samples from step 1 on)
 
         def burn(mean):
-            for k in range(eval_steps):
+            for k in range(1, eval_steps):
                 if np.all(np.abs(mean[k:] - eq) <= 2 * err + 1e-12):
                     return k
             return eval_steps
 
         out["groups"].append({"spins": s, "h": h, "beta": beta, "E_eq": eq, "E_eq_err": err,
-                              "warm_angle": ang[0], "cold_first_err": float(np.mean(np.abs(mc[first] - eq))),
-                              "warm_first_err": float(np.mean(np.abs(mw[first] - eq))),
+                              "warm_angle": ang[0], "cold_first_err": float(np.nanmean(np.abs(mc[first] - eq))),
+                              "warm_first_err": float(np.nanmean(np.abs(mw[first] - eq))),
                               "cold_burn_in_steps": burn(mc), "warm_burn_in_steps": burn(mw)})
     net.close()
     return out

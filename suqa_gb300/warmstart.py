@@ -172,7 +172,14 @@ def burn_in_experiment(spins=(4, 5, 6), ene_qbits=4, train_chains=512, train_ste
             mat = np.full((len(rr), eval_steps), np.nan)
             for i, r in enumerate(rr):
                 mat[i, r.step.astype(int)] = r.E
-            return np.nanmean(mat, axis=0), np.nanstd(mat, axis=0) / np.sqrt(np.sum(~np.isnan(mat), axis=0))
+            cnt = np.sum(~np.isnan(mat), axis=0)
+            mean = np.full(eval_steps, np.nan)
+            sem = np.full(eval_steps, np.nan)
+            for k in np.nonzero(cnt)[0]:  # steps without a single sample stay NaN
+                col = mat[~np.isnan(mat[:, k]), k]
+                mean[k] = col.mean()
+                sem[k] = col.std() / np.sqrt(len(col))
+            return mean, sem
 
         mc, sc = per_step(rc)
         mw, _ = per_step(rw)

@@ -168,6 +168,7 @@ typedef struct sq_chain_result {
     uint32_t samples;         /* (E, A) samples written */
     uint32_t phase_estimations; /* energy phase estimations (forward and inverse) applied */
     uint64_t cycles;          /* SM clock cycles the chain took */
+    uint64_t evolution_cycles; /* ... of which in the controlled time evolutions (Trotter steps) */
 } sq_chain_result;
 
 /* Runs every chain to completion on the current device (one persistent launch per
@@ -177,6 +178,55 @@ typedef struct sq_chain_result {
  * index).  kernel_ms (may be NULL) receives the device time of the launches. */
 int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, int precision, sq_chain_result* results,
                       double* samples_E, double* samples_A, uint32_t* samples_step, void* stream, float* kernel_ms);
+
+/* --- resumable chain batches ---
+ * A batch keeps every chain's amplitudes, random stream (PCG32 state and
+ * increment) and counters on the device between calls, so a run can be
+ * advanced in pieces, read out, checkpointed to host memory and resumed; the
+ * results are identical to one uninterrupted run.  Calls are blocking and use
+ * the batch's own stream on the device current at creation. */
+typedef struct sq_batch sq_batch;
+
+typedef struct sq_batch_opts {
+    uint32_t segment_steps;    /* steps per segment (0: a run call is one segment) */
+    uint32_t use_graph;        /* 1 (with segment_steps > 0): the launches of one segment are
+                                  captured once in a CUDA graph and replayed */
+    uint32_t autotune;         /* 1 (with threads == 0): per chain-width class, time one step of
+                                  a sample of its chains at each CTA size and keep the fastest */
+    uint32_t threads;          /* CTA size 128, 256 or 512 (FP64: at most 256); 0: 256 or tuned */
+    uint64_t l2_budget_bytes;  /* live-state bound for chains run from global memory (0: 64 MiB) */
+    uint32_t cta_qubits;       /* most qubits one CTA holds in shared memory (0: as many as fit);
+                                  wider chains are spread over a cluster */
+    uint32_t global_qubits;    /* chains of at least this many qubits run from global memory
+                                  (0: only chains too wide for a 16-CTA cluster) */
+} sq_batch_opts;
+
+typedef struct sq_batch_class {
+    uint32_t n, count;         /* qubits per chain, chains of this width */
+    uint32_t mode;             /* 0: one CTA, state in shared memory; 1: cluster, state in the
+                                  CTAs' shared memory; 2: cluster, state in global memory */
+    uint32_t cluster, threads, grid, smem_bytes;
+    float probe_ms;            /* autotuner's time for the chosen size (-1: not tuned) */
+} sq_batch_class;
+
+int sq_batch_create(sq_batch** out, const sq_tfim_chain* chains, uint32_t nchains, int precision,
+                    const sq_batch_opts* opts);
+int sq_batch_destroy(sq_batch* b);
+/* advance every unfinished chain by up to `steps` steps; kernel_ms (may be NULL) = device time */
+int sq_batch_run(sq_batch* b, uint32_t steps, float* kernel_ms);
+/* counters and all samples written so far (layout as sq_qms_tfim_batch) */
+int sq_batch_results(sq_batch* b, sq_chain_result* results, double* samples_E, double* samples_A,
+                     uint32_t* samples_step);
+/* steps completed per chain (host array of nchains) */
+int sq_batch_progress(sq_batch* b, uint32_t* steps_done);
+/* current amplitudes of one chain (2^n each, converted to double) */
+int sq_batch_state(sq_batch* b, uint32_t chain, double* re, double* im);
+int sq_batch_checkpoint_size(const sq_batch* b, uint64_t* bytes);
+int sq_batch_checkpoint(sq_batch* b, void* host, uint64_t bytes);
+/* only into a batch created with the same chains and precision */
+int sq_batch_restore(sq_batch* b, const void* host, uint64_t bytes);
+/* the launch plan: one entry per chain-width class (widest first) */
+int sq_batch_plan(const sq_batch* b, sq_batch_class* info, uint32_t max, uint32_t* nclasses);
 
 /* --- learned warm start: a small MLP with BF16 weights/activations, FP32 sums ---
  * No reference counterpart.  in -> `layers` hidden layers of `hidden` GELU units

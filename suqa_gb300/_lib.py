@@ -38,7 +38,18 @@ class SqTfimChain(C.Structure):
 
 class SqChainResult(C.Structure):
     _fields_ = [("accepted", C.c_uint32), ("failures", C.c_uint32), ("samples", C.c_uint32),
-                ("phase_estimations", C.c_uint32), ("cycles", C.c_uint64)]
+                ("phase_estimations", C.c_uint32), ("cycles", C.c_uint64), ("evolution_cycles", C.c_uint64)]
+
+
+class SqBatchOpts(C.Structure):
+    _fields_ = [("segment_steps", C.c_uint32), ("use_graph", C.c_uint32), ("autotune", C.c_uint32),
+                ("threads", C.c_uint32), ("l2_budget_bytes", C.c_uint64), ("cta_qubits", C.c_uint32),
+                ("global_qubits", C.c_uint32)]
+
+
+class SqBatchClass(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("count", C.c_uint32), ("mode", C.c_uint32), ("cluster", C.c_uint32),
+                ("threads", C.c_uint32), ("grid", C.c_uint32), ("smem_bytes", C.c_uint32), ("probe_ms", C.c_float)]
 
 
 _lib = None
@@ -80,6 +91,17 @@ _SIGS = {
     "sq_kernel_time": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "sq_qms_tfim_batch": (C.c_int, [C.POINTER(SqTfimChain), C.c_uint32, C.c_int, C.POINTER(SqChainResult),
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_float)]),
+    "sq_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(SqTfimChain), C.c_uint32, C.c_int,
+                                  C.POINTER(SqBatchOpts)]),
+    "sq_batch_destroy": (C.c_int, [C.c_void_p]),
+    "sq_batch_run": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_float)]),
+    "sq_batch_results": (C.c_int, [C.c_void_p, C.POINTER(SqChainResult), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sq_batch_progress": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sq_batch_state": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "sq_batch_checkpoint_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "sq_batch_checkpoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "sq_batch_restore": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "sq_batch_plan": (C.c_int, [C.c_void_p, C.POINTER(SqBatchClass), C.c_uint32, C.POINTER(C.c_uint32)]),
     "sq_mlp_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64]),
     "sq_mlp_destroy": (C.c_int, [C.c_void_p]),
     "sq_mlp_num_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),

@@ -1,6 +1,7 @@
 """Batched quantum Metropolis sampling of transverse-field Ising rings on the GPU
-(libsq sq_qms_tfim_batch): thousands of independent chains, one PCG32 stream
-each, run to completion in persistent kernels."""
+(libsq sq_qms_tfim_batch / sq_batch_*): thousands of independent chains, one
+PCG32 stream each, run in persistent kernels; a Batch can be advanced in
+segments (replayed from a captured CUDA graph), checkpointed and resumed."""
 from __future__ import annotations
 
 import ctypes as C
@@ -9,7 +10,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import SQ_F32, SQ_F64, SqChainResult, SqTfimChain, check
+from ._lib import SQ_F32, SQ_F64, SqBatchClass, SqBatchOpts, SqChainResult, SqTfimChain, check
 
 
 @dataclass
@@ -50,6 +51,7 @@ class ChainRun:
     step: np.ndarray = field(default_factory=lambda: np.zeros(0, np.uint32))
     phase_estimations: int = 0
     cycles: int = 0
+    evolution_cycles: int = 0
 
     def reference_rows(self, steps: int):
         """Rows the reference qms driver would have written to its output file: it
@@ -61,9 +63,7 @@ class ChainRun:
         return self.E[keep], self.A[keep]
 
 
-def run_tfim_batch(chains: list[TfimChain], precision: str = "f32", stream: int | None = None):
-    """Runs all chains; returns ([ChainRun], device milliseconds)."""
-    L = _lib.load()
+def _chain_array(chains):
     n = len(chains)
     arr = (SqTfimChain * n)()
     for i, c in enumerate(chains):
@@ -74,20 +74,120 @@ def run_tfim_batch(chains: list[TfimChain], precision: str = "f32", stream: int 
             arr[i].warm_start = 1
             for k, a in enumerate(c.warm_angles[:20]):
                 arr[i].ry[k] = float(a)
+    return arr
+
+
+def _precision(p):
+    return SQ_F64 if p in ("f64", "fp64") else SQ_F32
+
+
+def _split_runs(chains, res, E, A, S):
+    out = []
+    off = 0
+    for i, c in enumerate(chains):
+        k = res[i].samples
+        out.append(ChainRun(res[i].accepted, res[i].failures, E[off:off + k].copy(), A[off:off + k].copy(),
+                            S[off:off + k].copy(), res[i].phase_estimations, res[i].cycles,
+                            res[i].evolution_cycles))
+        off += c.steps
+    return out
+
+
+def run_tfim_batch(chains: list[TfimChain], precision: str = "f32", stream: int | None = None):
+    """Runs all chains; returns ([ChainRun], device milliseconds)."""
+    L = _lib.load()
+    n = len(chains)
+    arr = _chain_array(chains)
     res = (SqChainResult * n)()
     total = sum(c.steps for c in chains)
     E = np.zeros(max(total, 1), dtype=np.float64)
     A = np.zeros(max(total, 1), dtype=np.float64)
     S = np.zeros(max(total, 1), dtype=np.uint32)
     ms = C.c_float()
-    prec = SQ_F64 if precision in ("f64", "fp64") else SQ_F32
-    check(L.sq_qms_tfim_batch(arr, n, prec, res, E.ctypes.data_as(C.c_void_p), A.ctypes.data_as(C.c_void_p),
-                              S.ctypes.data_as(C.c_void_p), C.c_void_p(stream) if stream else None, C.byref(ms)))
-    out = []
-    off = 0
-    for i, c in enumerate(chains):
-        k = res[i].samples
-        out.append(ChainRun(res[i].accepted, res[i].failures, E[off:off + k].copy(), A[off:off + k].copy(),
-                            S[off:off + k].copy(), res[i].phase_estimations, res[i].cycles))
-        off += c.steps
-    return out, ms.value
+    check(L.sq_qms_tfim_batch(arr, n, _precision(precision), res, E.ctypes.data_as(C.c_void_p),
+                              A.ctypes.data_as(C.c_void_p), S.ctypes.data_as(C.c_void_p),
+                              C.c_void_p(stream) if stream else None, C.byref(ms)))
+    return _split_runs(chains, res, E, A, S), ms.value
+
+
+MODES = {0: "shared", 1: "cluster-shared", 2: "cluster-global"}
+
+
+class Batch:
+    """A resumable batch of chains (sq_batch_*).
+
+    segment_steps / use_graph: run() advances in segments of that many steps,
+    replaying one captured CUDA graph per segment; autotune: time the CTA sizes
+    per chain-width class on a sample of its chains and keep the fastest."""
+
+    def __init__(self, chains: list[TfimChain], precision: str = "f32", segment_steps: int = 0,
+                 use_graph: bool = False, autotune: bool = False, threads: int = 0, l2_budget_bytes: int = 0,
+                 cta_qubits: int = 0, global_qubits: int = 0):
+        self._L = _lib.load()
+        self.chains = list(chains)
+        self._arr = _chain_array(self.chains)
+        opts = SqBatchOpts(segment_steps, 1 if use_graph else 0, 1 if autotune else 0, threads, l2_budget_bytes,
+                           cta_qubits, global_qubits)
+        h = C.c_void_p()
+        check(self._L.sq_batch_create(C.byref(h), self._arr, len(self.chains), _precision(precision), C.byref(opts)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            self._L.sq_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, steps: int) -> float:
+        """Advance every unfinished chain by up to `steps` steps; returns device ms."""
+        ms = C.c_float()
+        check(self._L.sq_batch_run(self._h, steps, C.byref(ms)))
+        return ms.value
+
+    def results(self):
+        n = len(self.chains)
+        res = (SqChainResult * n)()
+        total = max(sum(c.steps for c in self.chains), 1)
+        E = np.zeros(total, dtype=np.float64)
+        A = np.zeros(total, dtype=np.float64)
+        S = np.zeros(total, dtype=np.uint32)
+        check(self._L.sq_batch_results(self._h, res, E.ctypes.data_as(C.c_void_p), A.ctypes.data_as(C.c_void_p),
+                                       S.ctypes.data_as(C.c_void_p)))
+        return _split_runs(self.chains, res, E, A, S)
+
+    def progress(self) -> np.ndarray:
+        out = np.zeros(len(self.chains), dtype=np.uint32)
+        check(self._L.sq_batch_progress(self._h, out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def state(self, chain: int) -> np.ndarray:
+        N = 1 << self.chains[chain].nqubits
+        re = np.zeros(N, dtype=np.float64)
+        im = np.zeros(N, dtype=np.float64)
+        check(self._L.sq_batch_state(self._h, chain, re.ctypes.data_as(C.c_void_p), im.ctypes.data_as(C.c_void_p)))
+        return re + 1j * im
+
+    def checkpoint(self) -> bytes:
+        size = C.c_uint64()
+        check(self._L.sq_batch_checkpoint_size(self._h, C.byref(size)))
+        buf = (C.c_char * size.value)()
+        check(self._L.sq_batch_checkpoint(self._h, buf, size.value))
+        return bytes(buf)
+
+    def restore(self, blob: bytes):
+        buf = C.create_string_buffer(blob, len(blob))
+        check(self._L.sq_batch_restore(self._h, buf, len(blob)))
+
+    def plan(self) -> list[dict]:
+        cnt = C.c_uint32()
+        check(self._L.sq_batch_plan(self._h, None, 0, C.byref(cnt)))
+        info = (SqBatchClass * max(cnt.value, 1))()
+        check(self._L.sq_batch_plan(self._h, info, cnt.value, C.byref(cnt)))
+        return [{"n": c.n, "chains": c.count, "mode": MODES.get(c.mode, c.mode), "cluster": c.cluster,
+                 "threads": c.threads, "grid": c.grid, "smem_bytes": c.smem_bytes,
+                 "probe_ms": round(float(c.probe_ms), 3)} for c in info[:cnt.value]]

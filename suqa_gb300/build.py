@@ -26,7 +26,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                      "-I" + INCLUDE, "-I" + CSRC]
 
-LIB_SOURCES = ["sq_engine.cu", "sq_noalloc.cu", "sq_batch.cu", "sq_mlp.cu"]
+LIB_SOURCES = ["sq_engine.cu", "sq_noalloc.cu", "sq_batch.cu", "sq_mlp.cu"] + [
+    "sq_batch_%s_m%d.cu" % (t, m) for t in ("f32", "f64") for m in (0, 1, 2)]
 
 
 def nvcc():
@@ -62,7 +63,7 @@ def build_libsq(force=False):
         objs.append(o)
         if force or not _newer(o, [s] + headers):
             jobs.append([nvcc()] + NVCC_FLAGS + ["-c", s, "-o", o])
-    with cf.ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1))) as ex:
         list(ex.map(_run, jobs))
     lib = os.path.join(BUILD, "libsq.so")
     if force or jobs or not os.path.exists(lib):
@@ -106,7 +107,7 @@ def build_dropin(force=False):
     return outs
 
 
-TFIM_SPINS = range(4, 11)
+TFIM_SPINS = range(4, 13)
 
 
 def build_tfim_drivers(force=False):

@@ -1,797 +1,374 @@
-// Batched quantum Metropolis sampling of transverse-field Ising rings, one chain
-// per CTA, entirely on the device.
+// Host side of the batched QMS engine: resumable chain batches (sq_batch_*) and
+// the one-shot sq_qms_tfim_batch.  Device code: sq_batch_dev.cuh.
 //
-// System: H = -J sum_i Z_i Z_{i+1} - h sum_i X_i on a ring of s spins; exp(-iHt)
-// as ceil(|t|/dt) first-order Trotter steps of width d = t/steps, each the ZZ
-// bond phases exp(i J d Z_i Z_{i+1}) then exp(i h d X_i) on every spin; moves:
-// Hadamard on spin i with probability 1/s; observable: magnetisation read in
-// the Z basis.  The register layout, the QMS step (reset, phase estimation,
-// move, acceptance oracle W, accept / restore loop, sampling branch) and the
-// order of every PCG32 draw restate the reference's include/qms.cuh:128-545 and
-// the driver loop of src/qms.cu:114-149, so each chain reproduces the reference
-// CPU `qms` binary built with the same system (measured outcomes identical,
-// amplitudes to rounding).
-//
-// GB300 mapping: a persistent grid of CTAs pulls chains from an atomic work
-// counter (largest first); a chain's 2^n amplitudes stay in shared memory for
-// its whole run (n <= 13 FP64 / 14 FP32; larger chains use a per-CTA buffer in
-// global memory that stays L2-resident); gates are CTA-wide sweeps with no
-// kernel launches and no host round trips; measurement probabilities are FP64
-// block reductions; the bond phases of a Trotter step are applied as one
-// diagonal (their product depends only on the number of domain walls).
+// A batch sorts its chains into width classes (same qubit count n).  Each class
+// gets a storage mode (one CTA with the state in shared memory; a cluster with
+// the state spread over its CTAs' shared memory; a cluster working on the state
+// in L2-resident global memory), a CTA size and a grid.  One launch per class
+// advances every unfinished chain of the class by a quota of steps; a segment
+// (the launches of all classes plus the work-counter reset) is captured once in
+// a CUDA graph and replayed.  Optionally an autotuner times the candidate CTA
+// sizes of each class on a sample of its chains (the same chains and seeds for
+// every candidate, so every candidate does identical work) and keeps the
+// fastest.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
-#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
 
-#include <cooperative_groups.h>
-
 #include "sq.h"
-
-namespace cg = cooperative_groups;
+#include "sq_batch_dev.cuh"
 
 namespace sqi {
 void set_error(const char* msg);
 }
 
-namespace sqb {
-
-constexpr int kThreads = 256;
-
-struct DevChain {
-    int s, e, n, steps, therm, reset_each, max_reverse;
-    double J, h, beta, dt;
-    double t_pe, t_shift, pe_factor, c_factor;  // as the reference driver computes them
-    uint64_t seed;
-    int out_offset;  // first sample slot of this chain
-    int warm;
-    double ry[20];   // warm-start RY angles per spin
-};
-
-struct Shared {
-    double red[2][32];
-    double bcast_d[4];
-    int bcast_i[4];
-    uint64_t rng_state, rng_inc;
-};
-
-__device__ __forceinline__ uint32_t pcg_next(Shared& sh) {
-    const uint64_t old = sh.rng_state;
-    sh.rng_state = old * 6364136223846793005ULL + sh.rng_inc;
-    const uint32_t x = (uint32_t)(((old >> 18u) ^ old) >> 27u);
-    const uint32_t rot = (uint32_t)(old >> 59u);
-    return (x >> rot) | (x << ((0u - rot) & 31u));
-}
-
-__device__ __forceinline__ double pcg_doub(Shared& sh) {
-    const uint64_t bits = ((uint64_t)pcg_next(sh) << 20) | 0x3ff0000000000000ULL;
-    return __longlong_as_double((long long)bits) - 1.0;
-}
-
-__device__ __forceinline__ void pcg_seed(Shared& sh, uint64_t s) {
-    sh.rng_state = 0U;
-    sh.rng_inc = (1ull << 1u) | 1u;
-    pcg_next(sh);
-    sh.rng_state += s;
-    pcg_next(sh);
-}
-
-__device__ __forceinline__ uint32_t ins0(uint32_t p, uint32_t b) {
-    return ((p >> b) << (b + 1u)) | (p & ((1u << b) - 1u));
-}
-
-// index p of the subspace with bit q = 0 and (if c >= 0) bit c = 1
-__device__ __forceinline__ uint32_t pair_idx(uint32_t p, int q, int c) {
-    if (c < 0) return ins0(p, (uint32_t)q);
-    const uint32_t lo = q < c ? (uint32_t)q : (uint32_t)c, hi = q < c ? (uint32_t)c : (uint32_t)q;
-    return ins0(ins0(p, lo), hi) | (1u << c);
-}
-
-// Shared-memory layout: element i lives at i + i/32 (one pad word per 32), which
-// makes the strided group loads of the fused Trotter sweeps bank-conflict free.
-__device__ __forceinline__ uint32_t pad(uint32_t i) { return i + (i >> 5); }
-
-// A chain's state.  Chains wider than one CTA's shared memory run on a cluster
-// of 2^k CTAs: the k most significant qubits (the acceptance qubit and the top
-// energy qubits) are distributed, CTA rank r holding the slice whose top bits
-// equal r.  Gates on local qubits never leave the CTA; a distributed qubit used
-// as a control is a per-CTA predicate; only H/X/W on a distributed qubit and the
-// measurement reductions exchange data through distributed shared memory.
-// Rank 0 owns the chain's random stream and broadcasts every decision, so all
-// ranks follow the same control flow.
-template <typename T, bool CL>
-struct Ctx {
-    T* re;
-    T* im;
-    int n, k, nl;      // total, distributed, local qubits
-    uint32_t Nl;       // local amplitudes
-    uint32_t rank;
-    Shared* sh;
-
-    __device__ void sync() const { __syncthreads(); }
-    __device__ void csync() const {
-        if (CL) cg::this_cluster().sync(); else __syncthreads();
-    }
-    __device__ bool dist(int q) const { return q >= nl; }
-    __device__ uint32_t rbit(int q) const { return (rank >> (q - nl)) & 1u; }
-    __device__ T* peer_re(uint32_t r) const { return cg::this_cluster().map_shared_rank(re, r); }
-    __device__ T* peer_im(uint32_t r) const { return cg::this_cluster().map_shared_rank(im, r); }
-    __device__ Shared* peer_sh(uint32_t r) const { return cg::this_cluster().map_shared_rank(sh, r); }
-
-    __device__ void init() {
-        for (uint32_t i = threadIdx.x; i < Nl; i += blockDim.x) {
-            re[pad(i)] = (T)0;
-            im[pad(i)] = (T)0;
-        }
-        sync();
-        if (threadIdx.x == 0 && rank == 0) re[pad(0)] = (T)1;
-        csync();
-    }
-
-    // 2x2 update of a pair across the cluster: this CTA holds the element with
-    // bit value `mine` of the distributed qubit q, the partner CTA the other.
-    // op: 0 = X (swap), 1 = H
-    __device__ void cross_pair(int q, int op) {
-        const uint32_t partner = rank ^ (1u << (q - nl));
-        const uint32_t mine = rbit(q);
-        T* pre = peer_re(partner);
-        T* pim = peer_im(partner);
-        csync();  // partner's previous writes are visible
-        const T kh = (T)0.7071067811865475;
-        // read phase into registers (at most Nl/blockDim elements per thread)
-        for (uint32_t base = 0; base < Nl; base += blockDim.x * 8u) {
-            T nr[8], ni[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const uint32_t i = base + threadIdx.x + u * blockDim.x;
-                if (i < Nl) {
-                    const T ar = re[pad(i)], ai = im[pad(i)], br = pre[pad(i)], bi = pim[pad(i)];
-                    if (op == 0) {
-                        nr[u] = br;
-                        ni[u] = bi;
-                    } else if (mine == 0) {
-                        nr[u] = kh * (ar + br);
-                        ni[u] = kh * (ai + bi);
-                    } else {
-                        nr[u] = kh * (br - ar);
-                        ni[u] = kh * (bi - ai);
-                    }
-                }
-            }
-            csync();  // everyone has read before anyone writes
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const uint32_t i = base + threadIdx.x + u * blockDim.x;
-                if (i < Nl) {
-                    re[pad(i)] = nr[u];
-                    im[pad(i)] = ni[u];
-                }
-            }
-            csync();
-        }
-    }
-
-    // Hadamard on q (uncontrolled)
-    __device__ void h(int q) {
-        if (CL && dist(q)) { cross_pair(q, 1); return; }
-        const T kk = (T)0.7071067811865475;
-        for (uint32_t p = threadIdx.x; p < Nl / 2; p += blockDim.x) {
-            const uint32_t i0 = ins0(p, (uint32_t)q), i1 = i0 | (1u << q);
-            const T a0r = re[pad(i0)], a0i = im[pad(i0)], a1r = re[pad(i1)], a1i = im[pad(i1)];
-            re[pad(i0)] = kk * (a0r + a1r);
-            im[pad(i0)] = kk * (a0i + a1i);
-            re[pad(i1)] = kk * (a0r - a1r);
-            im[pad(i1)] = kk * (a0i - a1i);
-        }
-        sync();
-    }
-
-    __device__ void x(int q) {
-        if (CL && dist(q)) { cross_pair(q, 0); return; }
-        for (uint32_t p = threadIdx.x; p < Nl / 2; p += blockDim.x) {
-            const uint32_t i0 = ins0(p, (uint32_t)q), i1 = i0 | (1u << q);
-            const T r = re[pad(i0)], i = im[pad(i0)];
-            re[pad(i0)] = re[pad(i1)];
-            im[pad(i0)] = im[pad(i1)];
-            re[pad(i1)] = r;
-            im[pad(i1)] = i;
-        }
-        sync();
-    }
-
-    // RY(theta) on a local qubit: a0' = c a0 - s a1, a1' = s a0 + c a1 (c, s of theta/2)
-    __device__ void ry(int q, T cs, T sn) {
-        for (uint32_t p = threadIdx.x; p < Nl / 2; p += blockDim.x) {
-            const uint32_t i0 = ins0(p, (uint32_t)q), i1 = i0 | (1u << q);
-            const T a0r = re[pad(i0)], a0i = im[pad(i0)], a1r = re[pad(i1)], a1i = im[pad(i1)];
-            re[pad(i0)] = cs * a0r - sn * a1r;
-            im[pad(i0)] = cs * a0i - sn * a1i;
-            re[pad(i1)] = sn * a0r + cs * a1r;
-            im[pad(i1)] = sn * a0i + cs * a1i;
-        }
-        sync();
-    }
-
-    // phase (cs + i sn) on the elements with bit q == val (U1 with q_mask = val)
-    __device__ void u1(int q, int val, T cs, T sn) {
-        if (CL && dist(q)) {
-            if (rbit(q) == (uint32_t)val) {
-                for (uint32_t i = threadIdx.x; i < Nl; i += blockDim.x) {
-                    const T a = re[pad(i)];
-                    re[pad(i)] = a * cs - im[pad(i)] * sn;
-                    im[pad(i)] = im[pad(i)] * cs + a * sn;
-                }
-            }
-            sync();
-            return;
-        }
-        for (uint32_t p = threadIdx.x; p < Nl / 2; p += blockDim.x) {
-            const uint32_t i = ins0(p, (uint32_t)q) | ((uint32_t)val << q);
-            const T a = re[pad(i)];
-            re[pad(i)] = a * cs - im[pad(i)] * sn;
-            im[pad(i)] = im[pad(i)] * cs + a * sn;
-        }
-        sync();
-    }
-
-    // controlled phase: both bits set
-    __device__ void cu1(int qc, int qt, T cs, T sn) {
-        int fixed[2];
-        int nf = 0;
-        bool skip = false;
-        for (int q : {qc, qt}) {
-            if (CL && dist(q)) {
-                if (!rbit(q)) skip = true;
-            } else {
-                fixed[nf++] = q;
-            }
-        }
-        if (!skip) {
-            const uint32_t cnt = Nl >> nf;
-            for (uint32_t p = threadIdx.x; p < cnt; p += blockDim.x) {
-                uint32_t i = p;
-                if (nf == 2) {
-                    const int lo = fixed[0] < fixed[1] ? fixed[0] : fixed[1], hi = fixed[0] < fixed[1] ? fixed[1] : fixed[0];
-                    i = ins0(ins0(i, lo), hi);
-                } else if (nf == 1) {
-                    i = ins0(i, fixed[0]);
-                }
-                for (int f = 0; f < nf; ++f) i |= 1u << fixed[f];
-                const T a = re[pad(i)];
-                re[pad(i)] = a * cs - im[pad(i)] * sn;
-                im[pad(i)] = im[pad(i)] * cs + a * sn;
-            }
-        }
-        sync();
-    }
-
-    // One Trotter step on the half with bit c set: the ZZ bond phases (a diagonal
-    // indexed by the number of domain walls), then exp(i h d X_i) on every spin.
-    // Spins are processed M at a time: a thread loads the 2^M amplitudes that
-    // differ only in those spins into registers, applies the M rotations there
-    // (they commute) and stores them back, so a step costs ceil(s/4) sweeps.
-    template <int M>
-    __device__ void trotter_group(int s, int g0, int c, bool with_zz, const T* tc, const T* ts, T xc, T xs) {
-        constexpr int G = 1 << M;
-        const uint32_t smask = (1u << s) - 1u;
-        const bool local_c = !(CL && dist(c));
-        if (!local_c && !rbit(c)) { sync(); return; }
-        const uint32_t ngroups = local_c ? (Nl >> (M + 1)) : (Nl >> M);
-        for (uint32_t gi = threadIdx.x; gi < ngroups; gi += blockDim.x) {
-            // insert M zero bits at g0, then the control bit (c > every spin bit)
-            uint32_t base = ((gi >> g0) << (g0 + M)) | (gi & ((1u << g0) - 1u));
-            if (local_c) base = ins0(base, (uint32_t)c) | (1u << c);
-            T ar[G], ai[G];
-#pragma unroll
-            for (int r = 0; r < G; ++r) {
-                const uint32_t i = base | ((uint32_t)r << g0);
-                ar[r] = re[pad(i)];
-                ai[r] = im[pad(i)];
-            }
-            if (with_zz) {
-#pragma unroll
-                for (int r = 0; r < G; ++r) {
-                    const uint32_t xsb = (base | ((uint32_t)r << g0)) & smask;
-                    const uint32_t rot = ((xsb >> 1) | ((xsb & 1u) << (s - 1))) & smask;
-                    const int w = __popc(xsb ^ rot);
-                    const T cs = tc[w], sn = ts[w];
-                    const T a = ar[r];
-                    ar[r] = a * cs - ai[r] * sn;
-                    ai[r] = ai[r] * cs + a * sn;
-                }
-            }
-#pragma unroll
-            for (int kq = 0; kq < M; ++kq) {
-#pragma unroll
-                for (int r = 0; r < G; ++r) {
-                    if (r & (1 << kq)) continue;
-                    const int r1 = r | (1 << kq);
-                    const T a0r = ar[r], a0i = ai[r], a1r = ar[r1], a1i = ai[r1];
-                    ar[r] = a0r * xc - a1i * xs;
-                    ai[r] = a0i * xc + a1r * xs;
-                    ar[r1] = a1r * xc - a0i * xs;
-                    ai[r1] = a1i * xc + a0r * xs;
-                }
-            }
-#pragma unroll
-            for (int r = 0; r < G; ++r) {
-                const uint32_t i = base | ((uint32_t)r << g0);
-                re[pad(i)] = ar[r];
-                im[pad(i)] = ai[r];
-            }
-        }
-        sync();
-    }
-
-    __device__ void trotter_step(int s, int c, const T* tc, const T* ts, T xc, T xs) {
-        for (int g0 = 0; g0 < s; g0 += 4) {
-            const int m = s - g0 < 4 ? s - g0 : 4;
-            const bool zz = (g0 == 0);
-            switch (m) {
-                case 4: trotter_group<4>(s, g0, c, zz, tc, ts, xc, xs); break;
-                case 3: trotter_group<3>(s, g0, c, zz, tc, ts, xc, xs); break;
-                case 2: trotter_group<2>(s, g0, c, zz, tc, ts, xc, xs); break;
-                default: trotter_group<1>(s, g0, c, zz, tc, ts, xc, xs); break;
-            }
-        }
-    }
-
-    // QMS acceptance rotation W on the acceptance qubit (the MSB), factors per
-    // energy reading Enew = (j >> shift) & (L-1), j the element with acc = 0
-    __device__ void w_oracle(int qacc, int shift, uint32_t L, const double* f1, const double* f2) {
-        if (CL && dist(qacc)) {
-            const uint32_t accbit = 1u << (qacc - nl);
-            const uint32_t partner = rank ^ accbit;
-            const bool is_j = (rank & accbit) == 0u;
-            const uint32_t jrank = rank & ~accbit;
-            T* pre = peer_re(partner);
-            T* pim = peer_im(partner);
-            csync();
-            for (uint32_t base = 0; base < Nl; base += blockDim.x * 8u) {
-                T nr[8], ni[8];
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const uint32_t l = base + threadIdx.x + u * blockDim.x;
-                    if (l < Nl) {
-                        const uint32_t gj = l | (jrank << nl);
-                        const uint32_t e = (gj >> shift) & (L - 1u);
-                        const T a = (T)f1[e], b = (T)f2[e];
-                        const T mr = re[pad(l)], mi = im[pad(l)], pr = pre[pad(l)], pi = pim[pad(l)];
-                        if (is_j) {
-                            nr[u] = b * mr + a * pr;
-                            ni[u] = b * mi + a * pi;
-                        } else {
-                            nr[u] = a * pr - b * mr;
-                            ni[u] = a * pi - b * mi;
-                        }
-                    }
-                }
-                csync();
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const uint32_t l = base + threadIdx.x + u * blockDim.x;
-                    if (l < Nl) {
-                        re[pad(l)] = nr[u];
-                        im[pad(l)] = ni[u];
-                    }
-                }
-                csync();
-            }
-            return;
-        }
-        const uint32_t half = 1u << qacc;
-        for (uint32_t j = threadIdx.x; j < half; j += blockDim.x) {
-            const uint32_t i = j | half;
-            const uint32_t e = (j >> shift) & (L - 1u);
-            const T a = (T)f1[e], b = (T)f2[e];
-            const T jr = re[pad(j)], ji = im[pad(j)], ir = re[pad(i)], ii = im[pad(i)];
-            re[pad(j)] = b * jr + a * ir;
-            im[pad(j)] = b * ji + a * ii;
-            re[pad(i)] = a * jr - b * ir;
-            im[pad(i)] = a * ji - b * ii;
-        }
-        sync();
-    }
-
-    // projective measurement of q with the draw r: returns c = (r < p1)
-    __device__ int measure(int q, double r) {
-        double p0 = 0.0, p1 = 0.0;
-        const bool dq = CL && dist(q);
-        for (uint32_t i = threadIdx.x; i < Nl; i += blockDim.x) {
-            const double w = (double)re[pad(i)] * (double)re[pad(i)] + (double)im[pad(i)] * (double)im[pad(i)];
-            const uint32_t bit = dq ? rbit(q) : ((i >> q) & 1u);
-            if (bit) p1 += w; else p0 += w;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            p0 += __shfl_down_sync(0xffffffffu, p0, o);
-            p1 += __shfl_down_sync(0xffffffffu, p1, o);
-        }
-        const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        if (lane == 0) {
-            sh->red[0][wid] = p0;
-            sh->red[1][wid] = p1;
-        }
-        sync();
-        if (threadIdx.x == 0) {
-            double a = 0.0, b = 0.0;
-            for (int kk = 0; kk < (int)(blockDim.x >> 5); ++kk) {
-                a += sh->red[0][kk];
-                b += sh->red[1][kk];
-            }
-            sh->bcast_d[2] = a;
-            sh->bcast_d[3] = b;
-        }
-        if (CL) {
-            csync();
-            if (rank == 0 && threadIdx.x == 0) {
-                double a = 0.0, b = 0.0;
-                const uint32_t nr = 1u << k;
-                for (uint32_t rr = 0; rr < nr; ++rr) {
-                    Shared* ps = peer_sh(rr);
-                    a += ps->bcast_d[2];
-                    b += ps->bcast_d[3];
-                }
-                const int cc = (int)(r < b);
-                const double sc = 1. / sqrt(cc ? b : a);
-                for (uint32_t rr = 0; rr < nr; ++rr) {
-                    Shared* ps = peer_sh(rr);
-                    ps->bcast_i[0] = cc;
-                    ps->bcast_d[0] = sc;
-                }
-            }
-            csync();
-        } else {
-            if (threadIdx.x == 0) {
-                const double a = sh->bcast_d[2], b = sh->bcast_d[3];
-                const int cc = (int)(r < b);
-                sh->bcast_i[0] = cc;
-                sh->bcast_d[0] = 1. / sqrt(cc ? b : a);
-            }
-            sync();
-        }
-        const int cc = sh->bcast_i[0];
-        const T sc = (T)sh->bcast_d[0];
-        for (uint32_t i = threadIdx.x; i < Nl; i += blockDim.x) {
-            const uint32_t bit = dq ? rbit(q) : ((i >> q) & 1u);
-            const bool keep = (int)bit == cc;
-            re[pad(i)] = (keep ? re[pad(i)] : (T)0) * sc;
-            im[pad(i)] = (keep ? im[pad(i)] : (T)0) * sc;
-        }
-        sync();
-        return cc;
-    }
-
-    // one draw from the chain's stream (rank 0, thread 0), broadcast to every thread
-    __device__ double draw() {
-        csync();
-        if (threadIdx.x == 0 && rank == 0) {
-            const double v = pcg_doub(*sh);
-            if (CL) {
-                for (uint32_t rr = 0; rr < (1u << k); ++rr) peer_sh(rr)->bcast_d[1] = v;
-            } else {
-                sh->bcast_d[1] = v;
-            }
-        }
-        csync();
-        return sh->bcast_d[1];
-    }
-};
-
-template <typename T, bool CL>
-struct Qms {
-    Ctx<T, CL> cx;
-    const DevChain* P;
-    int s, e, acc;
-    uint32_t L;
-    uint32_t E_old;
-    int gCi;
-    uint32_t nphi = 0;
-
-    // exp(-iHt) on the spins, controlled on bit c (a phase-estimation target)
-    __device__ void evolution(double t, int c) {
-        const double at = fabs(t);
-        int steps = (int)ceil(at / P->dt - 1e-9);
-        if (steps < 1) steps = 1;
-        const double d = t / (double)steps;
-        __shared__ T tc[24], ts[24];
-        __shared__ T xc, xs;
-        if (threadIdx.x <= (unsigned)s) {
-            double sn, cs;
-            sincos(P->J * d * (double)(s - 2 * (int)threadIdx.x), &sn, &cs);
-            tc[threadIdx.x] = (T)cs;
-            ts[threadIdx.x] = (T)sn;
-        }
-        if (threadIdx.x == 32) {
-            double sn, cs;
-            sincos(P->h * d, &sn, &cs);
-            xc = (T)cs;
-            xs = (T)sn;
-        }
-        __syncthreads();
-        for (int kk = 0; kk < steps; ++kk) cx.trotter_step(s, c, tc, ts, xc, xs);
-    }
-
-    __device__ void u1(int q, double phase) {
-        double sn, cs;
-        sincos(phase, &sn, &cs);
-        cx.u1(q, 1, (T)cs, (T)sn);
-    }
-
-    __device__ void cu1(int qc, int qt, double phase) {
-        double sn, cs;
-        sincos(phase, &sn, &cs);
-        cx.cu1(qc, qt, (T)cs, (T)sn);
-    }
-
-    // QFT over the energy register (phases 2 pi / 2^m, the reference's table)
-    __device__ void qft(bool inverse) {
-        if (!inverse) {
-            for (int o = e - 1; o >= 0; o--) {
-                cx.h(s + o);
-                for (int i = o - 1; i >= 0; i--) cu1(s + i, s + o, 2.0 * M_PI / (double)(1u << (1 + (o - i))));
-            }
-        } else {
-            for (int o = 0; o < e; o++) {
-                for (int i = 0; i < o; i++) cu1(s + i, s + o, -(2.0 * M_PI / (double)(1u << (1 + (o - i)))));
-                cx.h(s + o);
-            }
-        }
-    }
-
-    __device__ void phi() {
-        nphi++;
-        const double t = P->t_pe;
-        for (int kk = 0; kk < e; ++kk) cx.h(s + kk);
-        for (int trg = e - 1; trg > -1; --trg) {
-            const double powr = (double)(1u << (e - 1 - trg));
-            evolution(-powr * t, s + trg);
-            u1(s + trg, -powr * t * P->t_shift);
-        }
-        qft(true);
-    }
-
-    __device__ void phi_inverse() {
-        nphi++;
-        const double t = P->t_pe;
-        qft(false);
-        for (int trg = 0; trg < e; ++trg) {
-            const double powr = (double)(1u << (e - 1 - trg));
-            evolution(powr * t, s + trg);
-            u1(s + trg, powr * t * P->t_shift);
-        }
-        for (int kk = 0; kk < e; ++kk) cx.h(s + kk);
-    }
-
-    __device__ void w() {
-        __shared__ double f1[128], f2[128];
-        for (uint32_t en = threadIdx.x; en < L; en += blockDim.x) {
-            const double dE = (en * P->c_factor - E_old * P->c_factor);
-            if (dE > 0) {
-                f1[en] = exp(-dE / 2.0);
-                f2[en] = sqrt(1.0 - f1[en] * f1[en]);
-            } else {
-                f1[en] = 1.0;
-                f2[en] = 0.0;
-            }
-        }
-        __syncthreads();
-        cx.w_oracle(acc, s, L, f1, f2);
-    }
-
-    __device__ void apply_U() {
-        cx.h(gCi);
-        phi();
-        w();
-    }
-
-    __device__ void apply_U_inverse() {
-        w();
-        phi_inverse();
-        cx.h(gCi);
-    }
-
-    __device__ void reset(int q) {
-        const double r = cx.draw();
-        if (cx.measure(q, r)) cx.x(q);
-    }
-
-    __device__ uint32_t read_energy() {
-        double r[8];
-        for (int kk = 0; kk < e; ++kk) r[kk] = cx.draw();
-        uint32_t v = 0;
-        for (int kk = 0; kk < e; ++kk) v += (uint32_t)cx.measure(s + kk, r[kk]) << kk;
-        return v;
-    }
-
-    __device__ double energy_of(uint32_t v) const { return P->t_shift + v / (double)(P->pe_factor * L); }
-
-    // the system's initial state: |0...0>, or the learned warm start RY(ry_i) per spin
-    __device__ void init_state() {
-        cx.init();
-        if (P->warm) {
-            for (int i = 0; i < s; ++i) {
-                double sn, cs;
-                sincos(0.5 * P->ry[i], &sn, &cs);
-                cx.ry(i, (T)cs, (T)sn);
-            }
-            cx.csync();
-        }
-    }
-
-    __device__ double measure_magnetisation() {
-        double r[24];
-        for (int i = 0; i < s; ++i) r[i] = cx.draw();
-        double m = 0.0;
-        for (int i = 0; i < s; ++i) m += cx.measure(i, r[i]) ? -1.0 : 1.0;
-        return m;
-    }
-
-    __device__ int draw_C() {
-        const double xr = cx.draw();
-        for (int i = 0; i < s; ++i) {
-            const double wsum = (i + 1 == s) ? 1.0 : (double)(i + 1) / (double)s;
-            if (xr < wsum) return i;
-        }
-        return s;
-    }
-
-    // one Metropolis step; returns 1/2 accepted (not/sampled), 3/4 restored, -1 failed
-    __device__ int metro_step(bool take, double* Eout, double* Aout, bool* sampled) {
-        *sampled = false;
-        for (int kk = 0; kk < e; ++kk) reset(s + kk);
-        reset(acc);
-        phi();
-        const uint32_t eo = read_energy();
-        E_old = eo;
-        for (int kk = 0; kk < e; ++kk)
-            if ((eo >> kk) & 1u) cx.x(s + kk);
-        gCi = draw_C();
-        apply_U();
-        const int c_acc = cx.measure(acc, cx.draw());
-        if (c_acc == 1) {
-            const uint32_t en = read_energy();
-            phi_inverse();
-            if (!take) return 1;
-            *Eout = energy_of(en);
-            for (int kk = 0; kk < e; ++kk)
-                if ((en >> kk) & 1u) cx.x(s + kk);
-            *Aout = measure_magnetisation();
-            *sampled = true;
-            for (int kk = 0; kk < e; ++kk) reset(s + kk);
-            phi();
-            read_energy();
-            phi_inverse();
-            return 2;
-        }
-        apply_U_inverse();
-        int ret = 0;
-        int iters = 0;
-        while (iters < P->max_reverse) {
-            phi();
-            const uint32_t en = read_energy();
-            phi_inverse();
-            if (E_old == en) {
-                if (take) {
-                    *Eout = energy_of(E_old);
-                    for (int kk = 0; kk < e; ++kk) reset(s + kk);
-                    *Aout = measure_magnetisation();
-                    *sampled = true;
-                    for (int kk = 0; kk < e; ++kk) reset(s + kk);
-                    phi();
-                    read_energy();
-                    phi_inverse();
-                    ret = 4;
-                } else {
-                    ret = 3;
-                }
-                break;
-            }
-            apply_U();
-            cx.measure(acc, cx.draw());
-            apply_U_inverse();
-            iters++;
-        }
-        if (iters == P->max_reverse) return -1;
-        return ret;
-    }
-};
-
-// Persistent chain loop.  CL = cluster mode (one chain per cluster of 2^k CTAs).
-template <typename T, bool CL>
-__global__ void __launch_bounds__(kThreads, 2) k_qms_tfim(const DevChain* __restrict__ chains,
-                                                          const int* __restrict__ order, int nchains,
-                                                          unsigned int* next, sq_chain_result* res, double* sE,
-                                                          double* sA, uint32_t* sStep, int kdist) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ Shared sh;
-    __shared__ int cur;
-    const uint32_t rank = CL ? cg::this_cluster().block_rank() : 0u;
-    for (;;) {
-        if (CL) cg::this_cluster().sync(); else __syncthreads();
-        if (threadIdx.x == 0 && rank == 0) {
-            const int c = (int)atomicAdd(next, 1u);
-            if (CL) {
-                for (uint32_t rr = 0; rr < (1u << kdist); ++rr) *cg::this_cluster().map_shared_rank(&cur, rr) = c;
-            } else {
-                cur = c;
-            }
-        }
-        if (CL) cg::this_cluster().sync(); else __syncthreads();
-        if (cur >= nchains) return;
-        const int ci = order[cur];
-        const DevChain& P = chains[ci];
-        Qms<T, CL> q;
-        q.P = &P;
-        q.s = P.s;
-        q.e = P.e;
-        q.acc = P.s + P.e;
-        q.L = 1u << P.e;
-        q.cx.n = P.n;
-        q.cx.k = CL ? kdist : 0;
-        q.cx.nl = P.n - q.cx.k;
-        q.cx.Nl = 1u << q.cx.nl;
-        q.cx.rank = rank;
-        q.cx.sh = &sh;
-        q.cx.re = reinterpret_cast<T*>(smem_raw);
-        q.cx.im = q.cx.re + (q.cx.Nl + q.cx.Nl / 32 + 1);
-        if (threadIdx.x == 0 && rank == 0) pcg_seed(sh, P.seed);
-        const long long t_start = clock64();
-        q.init_state();
-        uint32_t s0 = 0, accepted = 0, failures = 0, ns = 0;
-        for (uint32_t st = 0; st < (uint32_t)P.steps; ++st) {
-            const bool take = (st > s0 + (uint32_t)P.therm) && ((st - s0) % (uint32_t)P.reset_each == 0u);
-            double E = 0.0, A = 0.0;
-            bool sampled = false;
-            const int ret = q.metro_step(take, &E, &A, &sampled);
-            if (threadIdx.x == 0 && rank == 0 && sampled) {
-                const size_t o = (size_t)P.out_offset + ns;
-                sE[o] = E;
-                sA[o] = A;
-                sStep[o] = st;
-            }
-            if (sampled) ns++;
-            if (ret < 0) {
-                q.init_state();
-                s0 = st + 1;
-                failures++;
-            }
-            if (ret == 1 || ret == 2) accepted++;
-        }
-        if (threadIdx.x == 0 && rank == 0) {
-            res[ci].accepted = accepted;
-            res[ci].failures = failures;
-            res[ci].samples = ns;
-            res[ci].phase_estimations = q.nphi;
-            res[ci].cycles = (uint64_t)(clock64() - t_start);
-        }
-    }
-}
-
-}  // namespace sqb
+using namespace sqb;
 
 namespace {
+
 int fail(int code, const std::string& m) {
     sqi::set_error(m.c_str());
     return code;
 }
+
 #define SQB_CUDA(call)                                                                              \
     do {                                                                                            \
         cudaError_t e_ = (call);                                                                    \
         if (e_ != cudaSuccess) return fail(SQ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
+
+const void* kernel_of(int precision, int mode) {
+    if (precision == SQ_F64) {
+        if (mode == 0) return kernel_for<double, 0>();
+        if (mode == 1) return kernel_for<double, 1>();
+        return kernel_for<double, 2>();
+    }
+    if (mode == 0) return kernel_for<float, 0>();
+    if (mode == 1) return kernel_for<float, 1>();
+    return kernel_for<float, 2>();
+}
+
+size_t padded(int q) { return ((size_t)1 << q) + ((size_t)1 << q) / 32 + 1; }
+
+struct Class {
+    int n, first, count;
+    int smax;  // longest ring of the class
+    int mode, kd, threads;
+    unsigned grid;
+    size_t smem;
+    float probe_ms;
+};
+
+uint64_t fnv1a(const void* p, size_t n, uint64_t h = 1469598103934665603ULL) {
+    const unsigned char* b = (const unsigned char*)p;
+    for (size_t i = 0; i < n; ++i) {
+        h ^= b[i];
+        h *= 1099511628211ULL;
+    }
+    return h;
+}
+
+struct CkptHeader {
+    char magic[8];
+    uint32_t version, nchains, precision, pad;
+    uint64_t state_elems, total_samples, chain_hash;
+};
+
 }  // namespace
 
-extern "C" int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, int precision, sq_chain_result* results,
-                                 double* samples_E, double* samples_A, uint32_t* samples_step, void* stream,
-                                 float* kernel_ms) {
-    using namespace sqb;
-    if (!chains || !results || nchains == 0) return fail(SQ_ERR_ARG, "null or empty chain list");
+struct sq_batch {
+    int precision = SQ_F64;
+    size_t esz = 8;
+    int dev = 0, nsm = 1, optin = 0;
+    cudaStream_t st = nullptr;
+    sq_batch_opts opts{};
+    uint32_t nchains = 0;
+    std::vector<DevChain> dc;
+    std::vector<int> order;
+    std::vector<Class> classes;
+    size_t total_samples = 0, state_elems = 0;
+    uint64_t chain_hash = 0;
+    DevChain* d_ch = nullptr;
+    int* d_order = nullptr;
+    unsigned int* d_next = nullptr;
+    ChainRec* d_rec = nullptr;
+    double* d_E = nullptr;
+    double* d_A = nullptr;
+    uint32_t* d_step = nullptr;
+    void* d_states = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    // one stream per width class: the classes run concurrently, so the tail of
+    // one class (its last, longest chains) overlaps the others' work
+    std::vector<cudaStream_t> cst;
+    std::vector<cudaEvent_t> cev;
+    cudaEvent_t fork = nullptr;
+
+    ~sq_batch() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        for (cudaStream_t x : cst) cudaStreamDestroy(x);
+        for (cudaEvent_t x : cev) cudaEventDestroy(x);
+        if (fork) cudaEventDestroy(fork);
+        cudaFree(d_ch); cudaFree(d_order); cudaFree(d_next); cudaFree(d_rec);
+        cudaFree(d_E); cudaFree(d_A); cudaFree(d_step); cudaFree(d_states);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    // dynamic shared memory of class c at a CTA size: the state slice (modes 0,
+    // 1) or the staging area of the warp-group exchange for rings longer than
+    // 10 spins (mode 2)
+    size_t smem_of(const Class& c, int threads) const {
+        if (c.mode != 2) return 2 * padded(c.n - c.kd) * esz;
+        return c.smax > 10 ? 2 * (size_t)threads * 32 * esz : 0;
+    }
+
+    // grid (in CTAs) for class c at a CTA size, or 0 if it cannot launch
+    int grid_for(const Class& c, int threads, unsigned* grid) const {
+        const void* k = kernel_of(precision, c.mode);
+        const size_t smem = smem_of(c, threads);
+        *grid = 0;
+        if (c.mode == 0) {
+            int bps = 0;
+            SQB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, threads, smem));
+            if (bps <= 0) return SQ_OK;
+            *grid = (unsigned)std::min<long long>((long long)bps * nsm, c.count);
+            return SQ_OK;
+        }
+        const unsigned csize = 1u << c.kd;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(csize * 64u, 1, 1);
+        cfg.blockDim = dim3((unsigned)threads, 1, 1);
+        cfg.dynamicSmemBytes = smem;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = csize;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int ncl = 0;
+        SQB_CUDA(cudaOccupancyMaxActiveClusters(&ncl, k, &cfg));
+        if (ncl <= 0) return SQ_OK;
+        long long live = std::min<long long>(ncl, c.count);
+        if (c.mode == 2) {
+            const uint64_t budget = opts.l2_budget_bytes ? opts.l2_budget_bytes : (64ull << 20);
+            const uint64_t chain_bytes = ((uint64_t)2 << c.n) * esz;
+            live = std::min<long long>(live, std::max<long long>(1, (long long)(budget / chain_bytes)));
+        }
+        *grid = (unsigned)(live * csize);
+        return SQ_OK;
+    }
+
+    int launch_class(const Class& c, const KArgs& a, int threads, unsigned grid, cudaStream_t stream) {
+        const void* k = kernel_of(precision, c.mode);
+        KArgs karg = a;
+        void* args[] = {(void*)&karg};
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid, 1, 1);
+        cfg.blockDim = dim3((unsigned)threads, 1, 1);
+        cfg.dynamicSmemBytes = smem_of(c, threads);
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        if (c.mode != 0) {
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = 1u << c.kd;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+        }
+        SQB_CUDA(cudaLaunchKernelExC(&cfg, k, args));
+        return SQ_OK;
+    }
+
+    KArgs args_for(size_t ci, uint32_t quota) const {
+        const Class& c = classes[ci];
+        KArgs a;
+        a.chains = d_ch;
+        a.order = d_order + c.first;
+        a.count = c.count;
+        a.next = d_next + ci;
+        a.recs = d_rec;
+        a.sE = d_E;
+        a.sA = d_A;
+        a.sStep = d_step;
+        a.states = d_states;
+        a.quota = quota;
+        a.kdist = c.kd;
+        return a;
+    }
+
+    // one segment: reset the work counters, launch every class on its own
+    // stream (widest first), join
+    int enqueue_segment(uint32_t quota) {
+        SQB_CUDA(cudaMemsetAsync(d_next, 0, sizeof(unsigned int) * classes.size(), st));
+        SQB_CUDA(cudaEventRecord(fork, st));
+        for (size_t ci = 0; ci < classes.size(); ++ci) {
+            SQB_CUDA(cudaStreamWaitEvent(cst[ci], fork, 0));
+            const int rc = launch_class(classes[ci], args_for(ci, quota), classes[ci].threads, classes[ci].grid, cst[ci]);
+            if (rc != SQ_OK) return rc;
+            SQB_CUDA(cudaEventRecord(cev[ci], cst[ci]));
+        }
+        for (size_t ci = 0; ci < classes.size(); ++ci) SQB_CUDA(cudaStreamWaitEvent(st, cev[ci], 0));
+        return SQ_OK;
+    }
+
+    int build_graph(uint32_t quota) {
+        if (gexec) {
+            cudaGraphExecDestroy(gexec);
+            gexec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        SQB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_segment(quota);
+        const cudaError_t ce = cudaStreamEndCapture(st, &g);
+        if (rc != SQ_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (ce != cudaSuccess) return fail(SQ_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+        const cudaError_t ie = cudaGraphInstantiate(&gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            gexec = nullptr;
+            return fail(SQ_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+        }
+        return SQ_OK;
+    }
+
+    // Time each candidate CTA size of class ci on one step of the same sample of
+    // its chains (scratch copies: the batch's own chains are not advanced).
+    int autotune_class(size_t ci) {
+        Class& c = classes[ci];
+        const int cands64[] = {128, 256};
+        const int cands32[] = {128, 256, 512};
+        const int* cands = precision == SQ_F64 ? cands64 : cands32;
+        const int ncand = precision == SQ_F64 ? 2 : 3;
+        unsigned cap = 0;
+        for (int k = 0; k < ncand; ++k) {
+            unsigned g = 0;
+            const int rc = grid_for(c, cands[k], &g);
+            if (rc != SQ_OK) return rc;
+            const unsigned chains_live = c.mode == 0 ? g : (g >> c.kd);
+            cap = std::max(cap, chains_live);
+        }
+        const int S = (int)std::min<unsigned>(cap, (unsigned)c.count);
+        if (S <= 0) return fail(SQ_ERR_ARG, "chain class cannot be launched");
+        const size_t per = ((size_t)2 << c.n);
+        std::vector<DevChain> pc(S);
+        for (int k = 0; k < S; ++k) {
+            pc[k] = dc[order[c.first + k]];
+            pc[k].state_off = (uint64_t)k * per;
+            pc[k].out_offset = k;
+            pc[k].steps = 1;
+        }
+        std::vector<int> po(S);
+        for (int k = 0; k < S; ++k) po[k] = k;
+        DevChain* d_pc = nullptr;
+        int* d_po = nullptr;
+        ChainRec* d_pr = nullptr;
+        double *d_pE = nullptr, *d_pA = nullptr;
+        uint32_t* d_pS = nullptr;
+        void* d_ps = nullptr;
+        unsigned int* d_pn = nullptr;
+        auto done = [&]() {
+            cudaFree(d_pc); cudaFree(d_po); cudaFree(d_pr); cudaFree(d_pE);
+            cudaFree(d_pA); cudaFree(d_pS); cudaFree(d_ps); cudaFree(d_pn);
+        };
+        if (cudaMalloc(&d_pc, sizeof(DevChain) * S) != cudaSuccess || cudaMalloc(&d_po, sizeof(int) * S) != cudaSuccess ||
+            cudaMalloc(&d_pr, sizeof(ChainRec) * S) != cudaSuccess || cudaMalloc(&d_pE, sizeof(double) * S) != cudaSuccess ||
+            cudaMalloc(&d_pA, sizeof(double) * S) != cudaSuccess || cudaMalloc(&d_pS, sizeof(uint32_t) * S) != cudaSuccess ||
+            cudaMalloc(&d_ps, per * esz * S) != cudaSuccess || cudaMalloc(&d_pn, sizeof(unsigned int)) != cudaSuccess) {
+            cudaGetLastError();
+            done();
+            return fail(SQ_ERR_NOMEM, "autotuner scratch allocation failed");
+        }
+        cudaMemcpyAsync(d_pc, pc.data(), sizeof(DevChain) * S, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(d_po, po.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st);
+        float best = -1.f;
+        int best_t = c.threads;
+        for (int k = 0; k < ncand; ++k) {
+            unsigned g = 0;
+            int rc = grid_for(c, cands[k], &g);
+            if (rc != SQ_OK) { done(); return rc; }
+            if (g == 0) continue;
+            if (c.mode != 0) g = std::min<unsigned>(g, (unsigned)S << c.kd);
+            else g = std::min<unsigned>(g, (unsigned)S);
+            KArgs a;
+            a.chains = d_pc;
+            a.order = d_po;
+            a.count = S;
+            a.next = d_pn;
+            a.recs = d_pr;
+            a.sE = d_pE;
+            a.sA = d_pA;
+            a.sStep = d_pS;
+            a.states = d_ps;
+            a.quota = 1;
+            a.kdist = c.kd;
+            cudaMemsetAsync(d_pr, 0, sizeof(ChainRec) * S, st);
+            cudaMemsetAsync(d_pn, 0, sizeof(unsigned int), st);
+            cudaEventRecord(e0, st);
+            rc = launch_class(c, a, cands[k], g, st);
+            if (rc != SQ_OK) { done(); return rc; }
+            cudaEventRecord(e1, st);
+            std::vector<ChainRec> pr(S);
+            cudaMemcpyAsync(pr.data(), d_pr, sizeof(ChainRec) * S, cudaMemcpyDeviceToHost, st);
+            const cudaError_t se = cudaStreamSynchronize(st);
+            if (se != cudaSuccess) {
+                done();
+                return fail(SQ_ERR_CUDA, std::string("autotune probe: ") + cudaGetErrorString(se));
+            }
+            float wall = 0.f;
+            cudaEventElapsedTime(&wall, e0, e1);
+            // Throughput measure: the summed per-chain SM time over the number of
+            // chains resident at once (the time a perfectly balanced queue would
+            // take), scaled to milliseconds by the probe's own wall clock so the
+            // clock rate cancels.  The probe's wall time alone is set by its
+            // single longest chain, which every candidate shares.
+            double sum_cyc = 0.0, max_cyc = 1.0;
+            for (const ChainRec& r : pr) {
+                sum_cyc += (double)r.cycles;
+                max_cyc = std::max(max_cyc, (double)r.cycles);
+            }
+            const unsigned live = c.mode == 0 ? g : (g >> c.kd);
+            const float ms = (float)(sum_cyc / std::max(1u, live) / max_cyc * wall);
+            if (best < 0.f || ms < best) {
+                best = ms;
+                best_t = cands[k];
+            }
+        }
+        done();
+        c.threads = best_t;
+        unsigned g = 0;
+        const int rc = grid_for(c, best_t, &g);
+        if (rc != SQ_OK) return rc;
+        if (g == 0) return fail(SQ_ERR_ARG, "chain class cannot be launched");
+        c.grid = g;
+        c.smem = smem_of(c, best_t);
+        c.probe_ms = best;
+        return SQ_OK;
+    }
+};
+
+extern "C" int sq_batch_create(sq_batch** out, const sq_tfim_chain* chains, uint32_t nchains, int precision,
+                               const sq_batch_opts* opts) {
+    if (!out) return fail(SQ_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    if (!chains || nchains == 0) return fail(SQ_ERR_ARG, "null or empty chain list");
     if (precision != SQ_F64 && precision != SQ_F32) return fail(SQ_ERR_ARG, "unknown precision");
-    std::vector<DevChain> dc(nchains);
-    size_t total = 0;
-    int nmax = 0;
+    sq_batch_opts o{};
+    if (opts) o = *opts;
+    if (o.threads != 0 && o.threads != 128 && o.threads != 256 && o.threads != 512)
+        return fail(SQ_ERR_ARG, "threads must be 0, 128, 256 or 512");
+    if (precision == SQ_F64 && o.threads == 512) return fail(SQ_ERR_ARG, "FP64 batches run at most 256 threads per CTA");
+    std::vector<DevChain> dcs(nchains);
+    size_t total_samples = 0, state_elems = 0;
     for (uint32_t i = 0; i < nchains; ++i) {
         const sq_tfim_chain& c = chains[i];
         if (c.spins < 2 || c.spins > 20 || c.ene_qbits < 1 || c.ene_qbits > 7)
@@ -799,7 +376,8 @@ extern "C" int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, 
         if (c.spins + c.ene_qbits + 1 > 22) return fail(SQ_ERR_ARG, "chain wider than 22 qubits");
         if (c.reset_each == 0 || c.max_reverse == 0 || !(c.ene_max > c.ene_min) || !(c.dt > 0))
             return fail(SQ_ERR_ARG, "invalid chain parameters");
-        DevChain& d = dc[i];
+        DevChain& d = dcs[i];
+        std::memset(&d, 0, sizeof(d));
         d.s = (int)c.spins;
         d.e = (int)c.ene_qbits;
         d.n = d.s + d.e + 1;
@@ -818,126 +396,334 @@ extern "C" int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, 
         d.t_pe = d.pe_factor * 8. * atan(1.0);
         d.c_factor = c.beta / (d.pe_factor * L);
         d.seed = c.seed;
-        d.out_offset = (int)total;
+        d.out_offset = (int)total_samples;
+        d.state_off = state_elems;
         d.warm = c.warm_start ? 1 : 0;
         for (int k = 0; k < 20; ++k) d.ry[k] = c.ry[k];
-        total += c.steps;
-        if (d.n > nmax) nmax = d.n;
+        total_samples += c.steps;
+        state_elems += (size_t)2 << d.n;
     }
-    // chains grouped by width; each class is one persistent launch sized for it
-    int dev = 0, nsm = 1, optin = 0;
-    SQB_CUDA(cudaGetDevice(&dev));
-    SQB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    SQB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const size_t esz = precision == SQ_F64 ? 8 : 4;
-    const size_t static_smem = 4096;
-    int smem_q = 0;
-    auto padded = [](int q) { return (size_t)(((size_t)1 << q) + ((size_t)1 << q) / 32 + 1); };
-    while (smem_q < 22 && 2 * padded(smem_q + 1) * esz + static_smem <= (size_t)optin) ++smem_q;
+    sq_batch* b = new sq_batch();
+    b->precision = precision;
+    b->esz = precision == SQ_F64 ? 8 : 4;
+    b->opts = o;
+    b->nchains = nchains;
+    b->dc.swap(dcs);
+    b->total_samples = total_samples;
+    b->state_elems = state_elems;
+    b->chain_hash = fnv1a(b->dc.data(), sizeof(DevChain) * nchains);
+    int rc = SQ_OK;
+    do {
+        cudaError_t ce = cudaGetDevice(&b->dev);
+        if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, b->dev);
+        if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&b->optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->dev);
+        if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+        if (ce == cudaSuccess) ce = cudaEventCreate(&b->e0);
+        if (ce == cudaSuccess) ce = cudaEventCreate(&b->e1);
+        cudaFuncAttributes fa;
+        if (ce == cudaSuccess) ce = cudaFuncGetAttributes(&fa, kernel_of(precision, 1));
+        if (ce != cudaSuccess) {
+            rc = fail(SQ_ERR_CUDA, std::string("chain batch set-up: ") + cudaGetErrorString(ce));
+            break;
+        }
+        // every kernel may use all the opt-in shared memory beside its static part;
+        // clusters of 16 CTAs are allowed
+        for (int md = 0; md < 3 && ce == cudaSuccess; ++md) {
+            cudaFuncAttributes fm;
+            ce = cudaFuncGetAttributes(&fm, kernel_of(precision, md));
+            if (ce == cudaSuccess)
+                ce = cudaFuncSetAttribute(kernel_of(precision, md), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          b->optin - (int)fm.sharedSizeBytes);
+            if (ce == cudaSuccess && md != 0)
+                ce = cudaFuncSetAttribute(kernel_of(precision, md), cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        }
+        if (ce != cudaSuccess) {
+            rc = fail(SQ_ERR_CUDA, std::string("kernel attributes: ") + cudaGetErrorString(ce));
+            break;
+        }
+        // widest chain whose state fits one CTA's shared memory
+        const size_t static_smem = fa.sharedSizeBytes + 1024;
+        int smem_q = 0;
+        while (smem_q < 22 && 2 * padded(smem_q + 1) * b->esz + static_smem <= (size_t)b->optin) ++smem_q;
+        if (o.cta_qubits) smem_q = std::min(smem_q, (int)o.cta_qubits);
 
-    std::vector<int> order(nchains);
-    for (uint32_t i = 0; i < nchains; ++i) order[i] = (int)i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return dc[a].n > dc[b].n; });
-    struct Class { int n, first, count; };
-    std::vector<Class> classes;
-    for (uint32_t k = 0; k < nchains; ++k) {
-        const int n = dc[order[k]].n;
-        if (classes.empty() || classes.back().n != n) classes.push_back({n, (int)k, 0});
-        classes.back().count++;
-    }
-    cudaStream_t st = (cudaStream_t)stream;
-    DevChain* d_ch = nullptr;
-    int* d_order = nullptr;
-    unsigned int* d_next = nullptr;
-    sq_chain_result* d_res = nullptr;
-    double *d_E = nullptr, *d_A = nullptr;
-    uint32_t* d_step = nullptr;
-    auto cleanup = [&]() {
-        cudaFree(d_ch); cudaFree(d_order); cudaFree(d_next); cudaFree(d_res);
-        cudaFree(d_E); cudaFree(d_A); cudaFree(d_step);
-    };
-    if (nmax > smem_q + 4) return fail(SQ_ERR_ARG, "chain too wide for a 16-CTA cluster");
-    if (cudaMalloc(&d_ch, sizeof(DevChain) * nchains) != cudaSuccess ||
-        cudaMalloc(&d_order, sizeof(int) * nchains) != cudaSuccess ||
-        cudaMalloc(&d_next, sizeof(unsigned int) * classes.size()) != cudaSuccess ||
-        cudaMalloc(&d_res, sizeof(sq_chain_result) * nchains) != cudaSuccess ||
-        cudaMalloc(&d_E, sizeof(double) * (total + 1)) != cudaSuccess ||
-        cudaMalloc(&d_A, sizeof(double) * (total + 1)) != cudaSuccess ||
-        cudaMalloc(&d_step, sizeof(uint32_t) * (total + 1)) != cudaSuccess) {
-        cudaGetLastError();
-        cleanup();
-        return fail(SQ_ERR_NOMEM, "device allocation for the chain batch failed");
-    }
-    cudaMemcpyAsync(d_ch, dc.data(), sizeof(DevChain) * nchains, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(d_order, order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, st);
-    cudaMemsetAsync(d_next, 0, sizeof(unsigned int) * classes.size(), st);
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaEventRecord(e0, st);
-    cudaError_t err = cudaSuccess;
-    for (size_t ci = 0; ci < classes.size() && err == cudaSuccess; ++ci) {
-        const Class& c = classes[ci];
-        const int kd = c.n > smem_q ? c.n - smem_q : 0;  // distributed qubits
-        const int nl = c.n - kd;
-        const int csize = 1 << kd;
-        const size_t smem = 2 * padded(nl) * esz;
-        int per_sm = (int)((size_t)(228 * 1024) / (smem + static_smem + 1024));
-        per_sm = std::max(1, std::min(per_sm, 8));
-        int groups = std::max(1, (nsm * per_sm) / csize);
-        groups = std::min(groups, c.count);
-        const unsigned grid = (unsigned)(groups * csize);
-        const int* ord = d_order + c.first;
-        unsigned int* nxt = d_next + ci;
-        if (kd == 0) {
-            if (precision == SQ_F64) {
-                cudaFuncSetAttribute(k_qms_tfim<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                k_qms_tfim<double, false><<<grid, kThreads, smem, st>>>(d_ch, ord, c.count, nxt, d_res, d_E, d_A, d_step, 0);
-            } else {
-                cudaFuncSetAttribute(k_qms_tfim<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                k_qms_tfim<float, false><<<grid, kThreads, smem, st>>>(d_ch, ord, c.count, nxt, d_res, d_E, d_A, d_step, 0);
+        b->order.resize(nchains);
+        for (uint32_t i = 0; i < nchains; ++i) b->order[i] = (int)i;
+        std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) { return b->dc[x].n > b->dc[y].n; });
+        std::vector<int> max_spins;
+        for (uint32_t k = 0; k < nchains; ++k) {
+            const DevChain& d = b->dc[b->order[k]];
+            if (b->classes.empty() || b->classes.back().n != d.n) {
+                b->classes.push_back({d.n, (int)k, 0, 0, 0, 0, 256, 0, 0, -1.f});
+                max_spins.push_back(0);
             }
-        } else {
-            cudaLaunchConfig_t cfg = {};
-            cfg.gridDim = dim3(grid, 1, 1);
-            cfg.blockDim = dim3(kThreads, 1, 1);
-            cfg.dynamicSmemBytes = smem;
-            cfg.stream = st;
-            cudaLaunchAttribute attr[1];
-            attr[0].id = cudaLaunchAttributeClusterDimension;
-            attr[0].val.clusterDim.x = (unsigned)csize;
-            attr[0].val.clusterDim.y = 1;
-            attr[0].val.clusterDim.z = 1;
-            cfg.attrs = attr;
-            cfg.numAttrs = 1;
-            if (precision == SQ_F64) {
-                auto kf = k_qms_tfim<double, true>;
-                cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                if (csize > 8) cudaFuncSetAttribute(kf, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-                err = cudaLaunchKernelEx(&cfg, kf, (const DevChain*)d_ch, ord, c.count, nxt, d_res, d_E, d_A, d_step, kd);
+            b->classes.back().count++;
+            max_spins.back() = std::max(max_spins.back(), d.s);
+            b->classes.back().smax = max_spins.back();
+        }
+        const int def_threads = o.threads ? (int)o.threads : 256;
+        for (size_t ci = 0; ci < b->classes.size(); ++ci) {
+            Class& c = b->classes[ci];
+            // the spins and at least one more qubit always stay local to a CTA
+            const int kmax = std::min(4, c.n - max_spins[ci] - 1);
+            const bool global = o.global_qubits && c.n >= (int)o.global_qubits;
+            if (c.n <= smem_q && !global) {
+                c.mode = 0;
+                c.kd = 0;
+            } else if (c.n - smem_q <= kmax && !global) {
+                c.mode = 1;
+                c.kd = c.n - smem_q;
             } else {
-                auto kf = k_qms_tfim<float, true>;
-                cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                if (csize > 8) cudaFuncSetAttribute(kf, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-                err = cudaLaunchKernelEx(&cfg, kf, (const DevChain*)d_ch, ord, c.count, nxt, d_res, d_E, d_A, d_step, kd);
+                c.mode = 2;
+                c.kd = kmax;
+            }
+            if (c.kd < 0 || (c.mode == 1 && c.kd < 1)) {
+                rc = fail(SQ_ERR_ARG, "a chain class cannot be laid out (too few qubits outside the spins)");
+                break;
+            }
+            c.threads = def_threads;
+            c.smem = b->smem_of(c, c.threads);
+            if (ce != cudaSuccess) {
+                rc = fail(SQ_ERR_CUDA, std::string("kernel attributes: ") + cudaGetErrorString(ce));
+                break;
+            }
+            rc = b->grid_for(c, c.threads, &c.grid);
+            if (rc != SQ_OK) break;
+            if (c.grid == 0) {
+                rc = fail(SQ_ERR_ARG, "a chain class cannot be launched (shared memory or cluster size)");
+                break;
             }
         }
-        if (err == cudaSuccess) err = cudaGetLastError();
+        if (rc != SQ_OK) break;
+        if (cudaMalloc(&b->d_ch, sizeof(DevChain) * nchains) != cudaSuccess ||
+            cudaMalloc(&b->d_order, sizeof(int) * nchains) != cudaSuccess ||
+            cudaMalloc(&b->d_next, sizeof(unsigned int) * b->classes.size()) != cudaSuccess ||
+            cudaMalloc(&b->d_rec, sizeof(ChainRec) * nchains) != cudaSuccess ||
+            cudaMalloc(&b->d_E, sizeof(double) * (b->total_samples + 1)) != cudaSuccess ||
+            cudaMalloc(&b->d_A, sizeof(double) * (b->total_samples + 1)) != cudaSuccess ||
+            cudaMalloc(&b->d_step, sizeof(uint32_t) * (b->total_samples + 1)) != cudaSuccess ||
+            cudaMalloc(&b->d_states, b->state_elems * b->esz) != cudaSuccess) {
+            cudaGetLastError();
+            rc = fail(SQ_ERR_NOMEM, "device allocation for the chain batch failed");
+            break;
+        }
+        ce = cudaMemcpyAsync(b->d_ch, b->dc.data(), sizeof(DevChain) * nchains, cudaMemcpyHostToDevice, b->st);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(b->d_order, b->order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, b->st);
+        if (ce == cudaSuccess) ce = cudaMemsetAsync(b->d_rec, 0, sizeof(ChainRec) * nchains, b->st);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(b->st);
+        if (ce != cudaSuccess) {
+            rc = fail(SQ_ERR_CUDA, std::string("chain batch upload: ") + cudaGetErrorString(ce));
+            break;
+        }
+        b->cst.resize(b->classes.size(), nullptr);
+        b->cev.resize(b->classes.size(), nullptr);
+        for (size_t ci = 0; ci < b->classes.size() && ce == cudaSuccess; ++ci) {
+            ce = cudaStreamCreateWithFlags(&b->cst[ci], cudaStreamNonBlocking);
+            if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&b->cev[ci], cudaEventDisableTiming);
+        }
+        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+        if (ce != cudaSuccess) {
+            rc = fail(SQ_ERR_CUDA, std::string("class streams: ") + cudaGetErrorString(ce));
+            break;
+        }
+        if (o.autotune && o.threads == 0)
+            for (size_t ci = 0; ci < b->classes.size() && rc == SQ_OK; ++ci) rc = b->autotune_class(ci);
+        if (rc != SQ_OK) break;
+        if (o.use_graph && o.segment_steps > 0) rc = b->build_graph(o.segment_steps);
+    } while (false);
+    if (rc != SQ_OK) {
+        delete b;
+        return rc;
     }
-    cudaEventRecord(e1, st);
-    if (err == cudaSuccess) {
-        cudaMemcpyAsync(results, d_res, sizeof(sq_chain_result) * nchains, cudaMemcpyDeviceToHost, st);
-        if (samples_E) cudaMemcpyAsync(samples_E, d_E, sizeof(double) * total, cudaMemcpyDeviceToHost, st);
-        if (samples_A) cudaMemcpyAsync(samples_A, d_A, sizeof(double) * total, cudaMemcpyDeviceToHost, st);
-        if (samples_step) cudaMemcpyAsync(samples_step, d_step, sizeof(uint32_t) * total, cudaMemcpyDeviceToHost, st);
-        err = cudaStreamSynchronize(st);
-    }
-    float ms = 0.f;
-    if (err == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
-    if (kernel_ms) *kernel_ms = ms;
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cleanup();
-    if (err != cudaSuccess) return fail(SQ_ERR_CUDA, std::string("chain batch: ") + cudaGetErrorString(err));
+    *out = b;
     return SQ_OK;
+}
+
+extern "C" int sq_batch_destroy(sq_batch* b) {
+    delete b;
+    return SQ_OK;
+}
+
+extern "C" int sq_batch_run(sq_batch* b, uint32_t steps, float* kernel_ms) {
+    if (!b) return fail(SQ_ERR_ARG, "null batch");
+    if (kernel_ms) *kernel_ms = 0.f;
+    if (steps == 0) return SQ_OK;
+    const uint32_t seg = b->opts.segment_steps ? b->opts.segment_steps : steps;
+    SQB_CUDA(cudaEventRecord(b->e0, b->st));
+    uint32_t left = steps;
+    while (left > 0) {
+        const uint32_t q = std::min(left, seg);
+        if (b->gexec && q == b->opts.segment_steps) {
+            SQB_CUDA(cudaGraphLaunch(b->gexec, b->st));
+        } else {
+            const int rc = b->enqueue_segment(q);
+            if (rc != SQ_OK) return rc;
+        }
+        left -= q;
+    }
+    SQB_CUDA(cudaEventRecord(b->e1, b->st));
+    const cudaError_t se = cudaStreamSynchronize(b->st);
+    if (se != cudaSuccess) return fail(SQ_ERR_CUDA, std::string("chain batch: ") + cudaGetErrorString(se));
+    if (kernel_ms) SQB_CUDA(cudaEventElapsedTime(kernel_ms, b->e0, b->e1));
+    return SQ_OK;
+}
+
+extern "C" int sq_batch_results(sq_batch* b, sq_chain_result* results, double* samples_E, double* samples_A,
+                                uint32_t* samples_step) {
+    if (!b) return fail(SQ_ERR_ARG, "null batch");
+    if (results) {
+        std::vector<ChainRec> rec(b->nchains);
+        SQB_CUDA(cudaMemcpyAsync(rec.data(), b->d_rec, sizeof(ChainRec) * b->nchains, cudaMemcpyDeviceToHost, b->st));
+        SQB_CUDA(cudaStreamSynchronize(b->st));
+        for (uint32_t i = 0; i < b->nchains; ++i) {
+            results[i].accepted = rec[i].accepted;
+            results[i].failures = rec[i].failures;
+            results[i].samples = rec[i].samples;
+            results[i].phase_estimations = rec[i].nphi;
+            results[i].cycles = rec[i].cycles;
+            results[i].evolution_cycles = rec[i].evo_cycles;
+        }
+    }
+    const size_t T = b->total_samples;
+    if (samples_E) SQB_CUDA(cudaMemcpyAsync(samples_E, b->d_E, sizeof(double) * T, cudaMemcpyDeviceToHost, b->st));
+    if (samples_A) SQB_CUDA(cudaMemcpyAsync(samples_A, b->d_A, sizeof(double) * T, cudaMemcpyDeviceToHost, b->st));
+    if (samples_step) SQB_CUDA(cudaMemcpyAsync(samples_step, b->d_step, sizeof(uint32_t) * T, cudaMemcpyDeviceToHost, b->st));
+    SQB_CUDA(cudaStreamSynchronize(b->st));
+    return SQ_OK;
+}
+
+extern "C" int sq_batch_progress(sq_batch* b, uint32_t* steps_done) {
+    if (!b || !steps_done) return fail(SQ_ERR_ARG, "null argument");
+    std::vector<ChainRec> rec(b->nchains);
+    SQB_CUDA(cudaMemcpyAsync(rec.data(), b->d_rec, sizeof(ChainRec) * b->nchains, cudaMemcpyDeviceToHost, b->st));
+    SQB_CUDA(cudaStreamSynchronize(b->st));
+    for (uint32_t i = 0; i < b->nchains; ++i) steps_done[i] = rec[i].step;
+    return SQ_OK;
+}
+
+extern "C" int sq_batch_state(sq_batch* b, uint32_t chain, double* re, double* im) {
+    if (!b || !re || !im) return fail(SQ_ERR_ARG, "null argument");
+    if (chain >= b->nchains) return fail(SQ_ERR_ARG, "chain index out of range");
+    ChainRec rec;
+    SQB_CUDA(cudaMemcpyAsync(&rec, b->d_rec + chain, sizeof(ChainRec), cudaMemcpyDeviceToHost, b->st));
+    SQB_CUDA(cudaStreamSynchronize(b->st));
+    if (!rec.started) return fail(SQ_ERR_ARG, "chain has not run yet");
+    const DevChain& d = b->dc[chain];
+    const size_t N = (size_t)1 << d.n;
+    std::vector<unsigned char> buf(2 * N * b->esz);
+    SQB_CUDA(cudaMemcpyAsync(buf.data(), (unsigned char*)b->d_states + d.state_off * b->esz, buf.size(),
+                             cudaMemcpyDeviceToHost, b->st));
+    SQB_CUDA(cudaStreamSynchronize(b->st));
+    if (b->precision == SQ_F64) {
+        const double* p = (const double*)buf.data();
+        std::copy(p, p + N, re);
+        std::copy(p + N, p + 2 * N, im);
+    } else {
+        const float* p = (const float*)buf.data();
+        for (size_t i = 0; i < N; ++i) {
+            re[i] = p[i];
+            im[i] = p[N + i];
+        }
+    }
+    return SQ_OK;
+}
+
+extern "C" int sq_batch_checkpoint_size(const sq_batch* b, uint64_t* bytes) {
+    if (!b || !bytes) return fail(SQ_ERR_ARG, "null argument");
+    *bytes = sizeof(CkptHeader) + sizeof(ChainRec) * (uint64_t)b->nchains + b->state_elems * b->esz +
+             b->total_samples * (2 * sizeof(double) + sizeof(uint32_t));
+    return SQ_OK;
+}
+
+extern "C" int sq_batch_checkpoint(sq_batch* b, void* host, uint64_t bytes) {
+    uint64_t need = 0;
+    const int rc = sq_batch_checkpoint_size(b, &need);
+    if (rc != SQ_OK) return rc;
+    if (!host || bytes < need) return fail(SQ_ERR_ARG, "checkpoint buffer too small");
+    unsigned char* p = (unsigned char*)host;
+    CkptHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, "SQBATCH1", 8);
+    h.version = 1;
+    h.nchains = b->nchains;
+    h.precision = (uint32_t)b->precision;
+    h.state_elems = b->state_elems;
+    h.total_samples = b->total_samples;
+    h.chain_hash = b->chain_hash;
+    std::memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    const size_t T = b->total_samples;
+    SQB_CUDA(cudaMemcpyAsync(p, b->d_rec, sizeof(ChainRec) * b->nchains, cudaMemcpyDeviceToHost, b->st));
+    p += sizeof(ChainRec) * b->nchains;
+    SQB_CUDA(cudaMemcpyAsync(p, b->d_states, b->state_elems * b->esz, cudaMemcpyDeviceToHost, b->st));
+    p += b->state_elems * b->esz;
+    SQB_CUDA(cudaMemcpyAsync(p, b->d_E, sizeof(double) * T, cudaMemcpyDeviceToHost, b->st));
+    p += sizeof(double) * T;
+    SQB_CUDA(cudaMemcpyAsync(p, b->d_A, sizeof(double) * T, cudaMemcpyDeviceToHost, b->st));
+    p += sizeof(double) * T;
+    SQB_CUDA(cudaMemcpyAsync(p, b->d_step, sizeof(uint32_t) * T, cudaMemcpyDeviceToHost, b->st));
+    SQB_CUDA(cudaStreamSynchronize(b->st));
+    return SQ_OK;
+}
+
+extern "C" int sq_batch_restore(sq_batch* b, const void* host, uint64_t bytes) {
+    uint64_t need = 0;
+    const int rc = sq_batch_checkpoint_size(b, &need);
+    if (rc != SQ_OK) return rc;
+    if (!host || bytes < need) return fail(SQ_ERR_ARG, "checkpoint too short");
+    const unsigned char* p = (const unsigned char*)host;
+    CkptHeader h;
+    std::memcpy(&h, p, sizeof(h));
+    if (std::memcmp(h.magic, "SQBATCH1", 8) != 0 || h.version != 1) return fail(SQ_ERR_ARG, "not a chain-batch checkpoint");
+    if (h.nchains != b->nchains || h.precision != (uint32_t)b->precision || h.state_elems != b->state_elems ||
+        h.total_samples != b->total_samples || h.chain_hash != b->chain_hash)
+        return fail(SQ_ERR_ARG, "checkpoint was written by a batch with different chains or precision");
+    p += sizeof(h);
+    const size_t T = b->total_samples;
+    SQB_CUDA(cudaMemcpyAsync(b->d_rec, p, sizeof(ChainRec) * b->nchains, cudaMemcpyHostToDevice, b->st));
+    p += sizeof(ChainRec) * b->nchains;
+    SQB_CUDA(cudaMemcpyAsync(b->d_states, p, b->state_elems * b->esz, cudaMemcpyHostToDevice, b->st));
+    p += b->state_elems * b->esz;
+    SQB_CUDA(cudaMemcpyAsync(b->d_E, p, sizeof(double) * T, cudaMemcpyHostToDevice, b->st));
+    p += sizeof(double) * T;
+    SQB_CUDA(cudaMemcpyAsync(b->d_A, p, sizeof(double) * T, cudaMemcpyHostToDevice, b->st));
+    p += sizeof(double) * T;
+    SQB_CUDA(cudaMemcpyAsync(b->d_step, p, sizeof(uint32_t) * T, cudaMemcpyHostToDevice, b->st));
+    SQB_CUDA(cudaStreamSynchronize(b->st));
+    return SQ_OK;
+}
+
+extern "C" int sq_batch_plan(const sq_batch* b, sq_batch_class* info, uint32_t max, uint32_t* nclasses) {
+    if (!b || !nclasses) return fail(SQ_ERR_ARG, "null argument");
+    *nclasses = (uint32_t)b->classes.size();
+    for (uint32_t i = 0; info && i < max && i < b->classes.size(); ++i) {
+        const Class& c = b->classes[i];
+        info[i].n = (uint32_t)c.n;
+        info[i].count = (uint32_t)c.count;
+        info[i].mode = (uint32_t)c.mode;
+        info[i].cluster = 1u << c.kd;
+        info[i].threads = (uint32_t)c.threads;
+        info[i].grid = c.grid;
+        info[i].smem_bytes = (uint32_t)c.smem;
+        info[i].probe_ms = c.probe_ms;
+    }
+    return SQ_OK;
+}
+
+extern "C" int sq_qms_tfim_batch(const sq_tfim_chain* chains, uint32_t nchains, int precision, sq_chain_result* results,
+                                 double* samples_E, double* samples_A, uint32_t* samples_step, void* stream,
+                                 float* kernel_ms) {
+    if (!results) return fail(SQ_ERR_ARG, "null results");
+    // the batch runs on its own stream: order it after the caller's work
+    if (stream) SQB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    sq_batch* b = nullptr;
+    int rc = sq_batch_create(&b, chains, nchains, precision, nullptr);
+    if (rc != SQ_OK) return rc;
+    uint32_t maxs = 0;
+    for (uint32_t i = 0; i < nchains; ++i) maxs = std::max(maxs, chains[i].steps);
+    rc = sq_batch_run(b, maxs, kernel_ms);
+    if (rc == SQ_OK) rc = sq_batch_results(b, results, samples_E, samples_A, samples_step);
+    sq_batch_destroy(b);
+    return rc;
 }

@@ -1,0 +1,10 @@
+// Batched QMS kernel, float amplitudes, storage mode 0 (one translation unit
+// per instantiation so they compile in parallel).
+#include "sq_batch_dev.cuh"
+
+namespace sqb {
+template <>
+const void* kernel_for<float, 0>() {
+    return (const void*)&k_qms_tfim<float, 0>;
+}
+}  // namespace sqb

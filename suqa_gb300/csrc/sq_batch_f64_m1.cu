@@ -1,0 +1,10 @@
+// Batched QMS kernel, double amplitudes, storage mode 1 (one translation unit
+// per instantiation so they compile in parallel).
+#include "sq_batch_dev.cuh"
+
+namespace sqb {
+template <>
+const void* kernel_for<double, 1>() {
+    return (const void*)&k_qms_tfim<double, 1>;
+}
+}  // namespace sqb

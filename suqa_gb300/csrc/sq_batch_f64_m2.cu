@@ -1,0 +1,10 @@
+// Batched QMS kernel, double amplitudes, storage mode 2 (one translation unit
+// per instantiation so they compile in parallel).
+#include "sq_batch_dev.cuh"
+
+namespace sqb {
+template <>
+const void* kernel_for<double, 2>() {
+    return (const void*)&k_qms_tfim<double, 2>;
+}
+}  // namespace sqb

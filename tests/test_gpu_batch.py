@@ -79,3 +79,130 @@ def test_cluster_chains_match_host_driven_driver(spins, ene, steps, tmp_path):
     wE, wA = parse_rows(open(out).read())
     E, A = runs[0].reference_rows(steps)
     assert fmt(E) == wE and fmt(A) == wA
+
+
+def _golden_rows(name):
+    wE, wA = parse_rows(golden_io.run_output(name))
+    return wE, wA
+
+
+@pytest.mark.parametrize("name", ["tfim_s4", "tfim_s6"])
+@pytest.mark.parametrize("layout", ["cluster", "global", "threads128"])
+def test_golden_chains_in_every_storage_mode(name, layout):
+    """The reference rows come out identical whether a chain's state sits in one
+    CTA's shared memory, is spread over a cluster's shared memory, or is worked
+    on in global memory by a cluster, and at any CTA size."""
+    from suqa_gb300.batch import Batch
+    c = chain_from_manifest(name)
+    kw = {"cluster": dict(cta_qubits=c.nqubits - 2), "global": dict(global_qubits=1),
+          "threads128": dict(threads=128)}[layout]
+    b = Batch([c], "f64", **kw)
+    plan = b.plan()
+    want_mode = {"cluster": "cluster-shared", "global": "cluster-global", "threads128": "shared"}[layout]
+    assert plan[0]["mode"] == want_mode, plan
+    b.run(c.steps)
+    E, A = b.results()[0].reference_rows(c.steps)
+    b.close()
+    wE, wA = _golden_rows(name)
+    assert fmt(E) == wE and fmt(A) == wA
+
+
+def _mixed(n, steps, seed=5, spins=(3, 7), ene=(3, 5)):
+    from suqa_gb300.batch import TfimChain
+    rng = np.random.default_rng(seed)
+    return [TfimChain(spins=int(rng.integers(*spins)), ene_qbits=int(rng.integers(*ene)), steps=steps,
+                      beta=float(rng.uniform(0.2, 2.0)), h=float(rng.uniform(0.5, 1.5)), thermalization=1,
+                      seed=500 + i) for i in range(n)]
+
+
+def _same(r1, r2):
+    for a, b in zip(r1, r2):
+        assert (a.accepted, a.failures, a.phase_estimations) == (b.accepted, b.failures, b.phase_estimations)
+        assert np.array_equal(a.E, b.E) and np.array_equal(a.A, b.A) and np.array_equal(a.step, b.step)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_segments_graph_checkpoint_resume(precision):
+    """A batch advanced in graph-replayed segments, checkpointed half-way and
+    resumed in a fresh batch gives exactly the one-shot results and states."""
+    from suqa_gb300.batch import Batch, run_tfim_batch
+    chains = _mixed(40, 9)
+    ref, _ = run_tfim_batch(chains, precision)
+    b = Batch(chains, precision, segment_steps=2, use_graph=True)
+    b.run(4)
+    assert (b.progress() == 4).all()
+    blob = b.checkpoint()
+    b.run(5)
+    seg = b.results()
+    _same(ref, seg)
+    b2 = Batch(chains, precision, segment_steps=3, use_graph=True)
+    b2.restore(blob)
+    assert (b2.progress() == 4).all()
+    b2.run(100)  # runs to the end of every chain
+    assert (b2.progress() == 9).all()
+    _same(ref, b2.results())
+    for i in (0, 17, 39):
+        assert np.array_equal(b.state(i), b2.state(i))
+    with pytest.raises(Exception):
+        Batch(chains[:-1], precision).restore(blob)
+    b.close()
+    b2.close()
+
+
+def test_autotuned_batch_same_results():
+    from suqa_gb300.batch import Batch, run_tfim_batch
+    chains = _mixed(64, 4, seed=9, spins=(4, 9), ene=(4, 6))
+    ref, _ = run_tfim_batch(chains, "f32")
+    b = Batch(chains, "f32", autotune=True)
+    plan = b.plan()
+    assert all(p["threads"] in (128, 256, 512) and p["probe_ms"] > 0 for p in plan), plan
+    b.run(4)
+    _same(ref, b.results())
+    b.close()
+
+
+@pytest.mark.parametrize("layout", ["cluster", "global"])
+def test_long_ring_matches_host_driven_driver(layout, tmp_path):
+    """12-spin rings (longer than a warp-group chunk of 10 spins: the extra spin
+    bits rotate between warps through shared memory) match the host-driven
+    drop-in driver; FP64, 17 qubits."""
+    import os
+    import subprocess
+    from suqa_gb300.batch import Batch, TfimChain
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spins, ene, steps = 12, 4, 2
+    c = TfimChain(spins=spins, ene_qbits=ene, steps=steps, beta=0.9, h=1.1, thermalization=0, seed=31,
+                  ene_min=-2.0 * spins, ene_max=2.0 * spins)
+    kw = dict(global_qubits=17) if layout == "global" else {}
+    b = Batch([c], "f64", **kw)
+    assert b.plan()[0]["mode"] == ("cluster-global" if layout == "global" else "cluster-shared")
+    b.run(steps)
+    run = b.results()[0]
+    b.close()
+    out = str(tmp_path / "drv.txt")
+    env = dict(os.environ, TFIM_J="1.0", TFIM_H="1.1")
+    cp = subprocess.run([os.path.join(root, "suqa_gb300", "_build", f"qms_tfim_s{spins}"), "0.9", str(steps), "1",
+                         str(ene), out, "--seed", "31", "--ene-min", str(-2.0 * spins), "--ene-max", str(2.0 * spins),
+                         "--thermalization", "0"], env=env, capture_output=True, text=True, timeout=1200)
+    assert cp.returncode == 0, cp.stderr[-2000:]
+    wE, wA = parse_rows(open(out).read())
+    E, A = run.reference_rows(steps)
+    assert fmt(E) == wE and fmt(A) == wA
+
+
+def test_wide_fp32_chains_in_global_memory_match_fp64():
+    """19-qubit chains (12 spins, 6 energy qubits: the warm-start evaluation
+    width) run from L2-resident global memory; FP32 takes the same path as FP64."""
+    from suqa_gb300.batch import Batch, TfimChain
+    chains = [TfimChain(spins=12, ene_qbits=6, steps=2, beta=b_, h=h_, thermalization=0, seed=70 + i)
+              for i, (b_, h_) in enumerate([(0.5, 0.7), (1.5, 1.2), (1.0, 1.0)])]
+    res = {}
+    for p in ("f32", "f64"):
+        b = Batch(chains, p)
+        assert b.plan()[0]["mode"] == "cluster-global"
+        b.run(2)
+        res[p] = b.results()
+        st = b.state(0)
+        assert abs(np.vdot(st, st).real - 1.0) < 1e-4
+        b.close()
+    _same(res["f32"], res["f64"])

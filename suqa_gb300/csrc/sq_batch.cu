@@ -124,7 +124,7 @@ struct sq_batch {
     // 10 spins (mode 2)
     size_t smem_of(const Class& c, int threads) const {
         if (c.mode != 2) return 2 * padded(c.n - c.kd) * esz;
-        return c.smax > 10 ? 2 * (size_t)threads * 32 * esz : 0;
+        return c.smax > kChunkSpins ? 2 * (size_t)threads * kStageR * esz : 0;
     }
 
     // grid (in CTAs) for class c at a CTA size, or 0 if it cannot launch
@@ -200,6 +200,7 @@ struct sq_batch {
         a.states = d_states;
         a.quota = quota;
         a.kdist = c.kd;
+        a.stage_elems = c.mode == 2 ? (uint32_t)(smem_of(c, c.threads) / esz) : 0u;
         return a;
     }
 
@@ -311,6 +312,7 @@ struct sq_batch {
             a.states = d_ps;
             a.quota = 1;
             a.kdist = c.kd;
+            a.stage_elems = c.mode == 2 ? (uint32_t)(smem_of(c, cands[k]) / esz) : 0u;
             cudaMemsetAsync(d_pr, 0, sizeof(ChainRec) * S, st);
             cudaMemsetAsync(d_pn, 0, sizeof(unsigned int), st);
             cudaEventRecord(e0, st);

@@ -68,7 +68,14 @@ struct KArgs {
     void* states;         // saved states (T elements)
     uint32_t quota;       // steps per chain in this launch
     int kdist;            // distributed qubits (MODE 1, 2)
+    uint32_t stage_elems; // MODE 2: elements of dynamic shared memory for the Trotter exchange
 };
+
+// Longer rings than this keep their top spin bits across a warp group
+// (evolve_regs); the staging area of mode 2 then needs kStageR elements per
+// thread for re and for im.
+constexpr int kChunkSpins = 9;
+constexpr int kStageR = 1 << (kChunkSpins - 5);
 
 struct Shared {
     double red[2][32];
@@ -87,6 +94,10 @@ struct Tables {
     int steps[2][8], regs[2][8];   // Trotter steps of the controlled power; register path usable
     T u1c[2][8], u1s[2][8];        // phase-estimation shift on energy qubit trg
     T qc[2][8], qs[2][8];          // QFT controlled phase at distance k (forward / inverse)
+    T rtc[128], rts[128];          // e^{i 2 pi k / 2^e}
+    T u1v_c[2][128], u1v_s[2][128];  // all phase-estimation shifts as one phase per register value
+    T dc[128], ds[128];            // the diagonal of the current fused QFT step
+    double hist[256];              // register histogram (measurements)
 };
 
 __device__ __forceinline__ uint32_t pcg_next(Shared& sh) {
@@ -131,7 +142,8 @@ struct Ctx {
     T* im;
     T* gre;       // MODE 2: the whole state's re / im blocks
     T* gim;
-    T* stage;     // MODE 2: shared-memory staging for the Trotter exchange (2 * threads * 32 elements)
+    T* stage;     // MODE 2: shared-memory staging for the Trotter exchange
+    uint32_t stage_elems;
     int n, k, nl;      // total, distributed, local qubits
     uint32_t Nl;       // local amplitudes
     uint32_t rank;
@@ -515,6 +527,287 @@ struct Ctx {
         sync();
     }
 
+    // value of the k-qubit register starting at q0 for local element i (the
+    // distributed top qubits come from the CTA's rank)
+    __device__ __forceinline__ uint32_t regval(uint32_t i, int q0, int k) const {
+        const uint32_t g = CL ? (i | (rank << nl)) : i;
+        return (g >> q0) & ((1u << k) - 1u);
+    }
+
+    // Hadamards on the local qubits q0..q0+CNT-1 in one sweep (groups of 2^CNT
+    // amplitudes in registers), each the reference's H: sum and difference
+    // times 0.7071067811865475
+    template <int CNT>
+    __device__ __noinline__ void h_group(int q0) {
+        constexpr int G = 1 << CNT;
+        const T kk = (T)0.7071067811865475;
+        const uint32_t ng = Nl >> CNT;
+        for (uint32_t gi = threadIdx.x; gi < ng; gi += blockDim.x) {
+            const uint32_t base = ((gi >> q0) << (q0 + CNT)) | (gi & ((1u << q0) - 1u));
+            T ar[G], ai[G];
+#pragma unroll
+            for (int r = 0; r < G; ++r) {
+                ar[r] = re[at(base | ((uint32_t)r << q0))];
+                ai[r] = im[at(base | ((uint32_t)r << q0))];
+            }
+#pragma unroll
+            for (int b = 0; b < CNT; ++b) {
+#pragma unroll
+                for (int r = 0; r < G; ++r) {
+                    if (r & (1 << b)) continue;
+                    const int r1 = r | (1 << b);
+                    const T xr = ar[r], xi = ai[r], yr = ar[r1], yi = ai[r1];
+                    ar[r] = kk * (xr + yr);
+                    ai[r] = kk * (xi + yi);
+                    ar[r1] = kk * (xr - yr);
+                    ai[r1] = kk * (xi - yi);
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < G; ++r) {
+                re[at(base | ((uint32_t)r << q0))] = ar[r];
+                im[at(base | ((uint32_t)r << q0))] = ai[r];
+            }
+        }
+        sync();
+    }
+
+    // H on every qubit of q0..q0+k-1: local ones up to four per sweep, distributed
+    // ones through the cluster
+    __device__ void h_layer(int q0, int k) {
+        int q = q0;
+        const int qe = q0 + k;
+        while (q < qe && !dist(q)) {
+            int cnt = qe - q;
+            int room = nl - q;
+            if (cnt > room) cnt = room;
+            if (cnt > 4) cnt = 4;
+            switch (cnt) {
+                case 4: h_group<4>(q); break;
+                case 3: h_group<3>(q); break;
+                case 2: h_group<2>(q); break;
+                default: h_group<1>(q); break;
+            }
+            q += cnt;
+        }
+        for (; q < qe; ++q) cross_pair(q, 1);
+    }
+
+    // element phase (dc, ds)[v], v the value of the e-qubit register at q0
+    __device__ __noinline__ void diag(int q0, int e, const T* dcr, const T* dsr) {
+        for (uint32_t i = threadIdx.x; i < Nl; i += blockDim.x) {
+            const uint32_t v = regval(i, q0, e);
+            const T cs = dcr[v], sn = dsr[v];
+            const T a = re[at(i)];
+            re[at(i)] = a * cs - im[at(i)] * sn;
+            im[at(i)] = im[at(i)] * cs + a * sn;
+        }
+        sync();
+    }
+
+    // the diagonal and H on the local qubit q in one sweep (DIAG_FIRST: diagonal
+    // then H, else H then diagonal)
+    template <bool DIAG_FIRST>
+    __device__ __noinline__ void diag_h_local(int q, int q0, int e, const T* dcr, const T* dsr) {
+        const T kk = (T)0.7071067811865475;
+        for (uint32_t p = threadIdx.x; p < Nl / 2; p += blockDim.x) {
+            const uint32_t i0 = ins0(p, (uint32_t)q), i1 = i0 | (1u << q);
+            T a0r = re[at(i0)], a0i = im[at(i0)], a1r = re[at(i1)], a1i = im[at(i1)];
+            const uint32_t v0 = regval(i0, q0, e), v1 = regval(i1, q0, e);
+            if (DIAG_FIRST) {
+                T c = dcr[v0], sn = dsr[v0], t = a0r;
+                a0r = t * c - a0i * sn;
+                a0i = a0i * c + t * sn;
+                c = dcr[v1], sn = dsr[v1], t = a1r;
+                a1r = t * c - a1i * sn;
+                a1i = a1i * c + t * sn;
+            }
+            T b0r = kk * (a0r + a1r), b0i = kk * (a0i + a1i), b1r = kk * (a0r - a1r), b1i = kk * (a0i - a1i);
+            if (!DIAG_FIRST) {
+                T c = dcr[v0], sn = dsr[v0], t = b0r;
+                b0r = t * c - b0i * sn;
+                b0i = b0i * c + t * sn;
+                c = dcr[v1], sn = dsr[v1], t = b1r;
+                b1r = t * c - b1i * sn;
+                b1i = b1i * c + t * sn;
+            }
+            re[at(i0)] = b0r;
+            im[at(i0)] = b0i;
+            re[at(i1)] = b1r;
+            im[at(i1)] = b1i;
+        }
+        sync();
+    }
+
+    __device__ void diag_h(bool diag_first, int q, int q0, int e, const T* dcr, const T* dsr) {
+        if (!dist(q)) {
+            if (diag_first) diag_h_local<true>(q, q0, e, dcr, dsr);
+            else diag_h_local<false>(q, q0, e, dcr, dsr);
+            return;
+        }
+        if (diag_first) {
+            diag(q0, e, dcr, dsr);
+            cross_pair(q, 1);
+        } else {
+            cross_pair(q, 1);
+            diag(q0, e, dcr, dsr);
+        }
+    }
+
+    // X on the register qubits set in c: element i takes the value of i ^ (c << q0).
+    // The local qubits swap pairs inside the CTA; the distributed ones then swap
+    // whole slices with the partner CTA at equal local indices (so the batched
+    // exchange below never reads an element the partner has already rewritten).
+    __device__ __noinline__ void xor_register(int q0, int k, uint32_t c) {
+        if (c == 0u) return;
+        const uint32_t full = c << q0;
+        const uint32_t mloc = full & (Nl - 1u);
+        const uint32_t rx = CL ? (full >> nl) : 0u;
+        if (mloc != 0u) {
+            for (uint32_t i = threadIdx.x; i < Nl; i += blockDim.x) {
+                const uint32_t j = i ^ mloc;
+                if (j > i) {
+                    const T r = re[at(i)], m = im[at(i)];
+                    re[at(i)] = re[at(j)];
+                    im[at(i)] = im[at(j)];
+                    re[at(j)] = r;
+                    im[at(j)] = m;
+                }
+            }
+            sync();
+        }
+        if (rx == 0u) return;
+        const uint32_t partner = rank ^ rx;
+        T* pre = peer_re(partner);
+        T* pim = peer_im(partner);
+        csync();
+        for (uint32_t base = 0; base < Nl; base += blockDim.x * 8u) {
+            T nr[8], ni[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t i = base + threadIdx.x + u * blockDim.x;
+                if (i < Nl) {
+                    nr[u] = pre[at(i)];
+                    ni[u] = pim[at(i)];
+                }
+            }
+            csync();
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t i = base + threadIdx.x + u * blockDim.x;
+                if (i < Nl) {
+                    re[at(i)] = nr[u];
+                    im[at(i)] = ni[u];
+                }
+            }
+            csync();
+        }
+    }
+
+    // Measures the k-qubit register at q0 (k <= 8) qubit by qubit, lowest first,
+    // with k fresh draws of the chain's stream, exactly as k successive
+    // measure_qbit calls of the reference (each outcome c_j = r_j < p1 given the
+    // earlier outcomes), but with one histogram pass and one collapse pass:
+    // the histogram P[v] (FP64, each warp summing whole bins in a fixed order)
+    // gives every conditional p1; the collapse keeps the elements of the outcome
+    // v = c scaled by 1/sqrt(P[c]), and with `flip` also applies X to every qubit
+    // read as 1 (moves them to v = 0), as the reference's apply_reset.
+    __device__ __noinline__ uint32_t measure_register(int q0, int k, bool flip, double* hist) {
+        const uint32_t nb = 1u << k;
+        // register qubits held locally, and the rank bits of the distributed ones
+        int kl = nl - q0;
+        if (kl > k) kl = k;
+        if (kl < 0) kl = 0;
+        const uint32_t nbl = 1u << kl;
+        const uint32_t vhi = (CL && kl < k) ? ((rank >> (q0 + kl - nl)) & ((1u << (k - kl)) - 1u)) : 0u;
+        const int lane = threadIdx.x & 31;
+        const uint32_t nw = blockDim.x >> 5;
+        // local bins: warp w sums bins w, w + nw, ...; bin vl holds the elements
+        // (low q0 bits) | vl << q0 | (high bits) << (q0 + kl)
+        const uint32_t per = Nl >> kl;
+        for (uint32_t vl = threadIdx.x >> 5; vl < nbl; vl += nw) {
+            double acc = 0.0;
+            for (uint32_t j = lane; j < per; j += 32) {
+                const uint32_t i = (j & ((1u << q0) - 1u)) | (vl << q0) | ((j >> q0) << (q0 + kl));
+                acc += (double)re[at(i)] * (double)re[at(i)] + (double)im[at(i)] * (double)im[at(i)];
+            }
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+            if (lane == 0) hist[vl] = acc;
+        }
+        csync();
+        if (threadIdx.x == 0 && rank == 0) {
+            double P[256];
+            for (uint32_t v = 0; v < nb; ++v) P[v] = 0.0;
+            const uint32_t nr = CL ? (1u << this->k) : 1u;
+            for (uint32_t rr = 0; rr < nr; ++rr) {
+                const double* hr = CL ? cg::this_cluster().map_shared_rank(hist, rr) : hist;
+                const uint32_t vh = (CL && kl < k) ? ((rr >> (q0 + kl - nl)) & ((1u << (k - kl)) - 1u)) : 0u;
+                for (uint32_t vl = 0; vl < nbl; ++vl) P[vl | (vh << kl)] += hr[vl];
+            }
+            // sequential decisions with the reference's draws and comparisons
+            uint32_t c = 0;
+            for (int j = 0; j < k; ++j) {
+                const double r = pcg_doub(*sh);
+                // candidates: the values agreeing with the outcomes so far
+                double s0 = 0.0, s1 = 0.0;
+                for (uint32_t t = 0; t < (nb >> j); t += 2) {
+                    s0 += P[c | (t << j)];
+                    s1 += P[c | ((t + 1) << j)];
+                }
+                const double p1 = s1 / (s0 + s1);
+                if (r < p1) c |= 1u << j;
+            }
+            const double sc = 1. / sqrt(P[c]);
+            for (uint32_t rr = 0; rr < nr; ++rr) {
+                Shared* ps = CL ? peer_sh(rr) : sh;
+                ps->bcast_i[1] = (int)c;
+                ps->bcast_d[0] = sc;
+            }
+        }
+        csync();
+        const uint32_t c = (uint32_t)sh->bcast_i[1];
+        const T sc = (T)sh->bcast_d[0];
+        const uint32_t chi = c >> kl, clo = c & (nbl - 1u);
+        if (!flip) {
+            const bool mine = chi == vhi;
+            for (uint32_t i = threadIdx.x; i < Nl; i += blockDim.x) {
+                const bool keep = mine && ((i >> q0) & (nbl - 1u)) == clo;
+                re[at(i)] = (keep ? re[at(i)] : (T)0) * sc;
+                im[at(i)] = (keep ? im[at(i)] : (T)0) * sc;
+            }
+            sync();
+            return c;
+        }
+        // reset: the outcome's elements move to register value 0, all else is zero.
+        // Targets are this CTA's elements with local register bits 0 when its
+        // distributed register bits are 0; the source CTA is rank ^ (chi << ...).
+        if (vhi == 0u) {
+            const uint32_t src = CL && kl < k ? (rank ^ (chi << (q0 + kl - nl))) : rank;
+            const T* sre = (src == rank) ? re : peer_re(src);
+            const T* sim = (src == rank) ? im : peer_im(src);
+            for (uint32_t gi = threadIdx.x; gi < per; gi += blockDim.x) {
+                const uint32_t b = (gi & ((1u << q0) - 1u)) | ((gi >> q0) << (q0 + kl));
+                const uint32_t isrc = b | (clo << q0);
+                const T vr = sre[at(isrc)] * sc, vi = sim[at(isrc)] * sc;
+                for (uint32_t vl = 1; vl < nbl; ++vl) {
+                    re[at(b | (vl << q0))] = (T)0;
+                    im[at(b | (vl << q0))] = (T)0;
+                }
+                re[at(b)] = vr;
+                im[at(b)] = vi;
+            }
+        }
+        csync();
+        if (vhi != 0u) {
+            for (uint32_t i = threadIdx.x; i < Nl; i += blockDim.x) {
+                re[at(i)] = (T)0;
+                im[at(i)] = (T)0;
+            }
+        }
+        csync();
+        return c;
+    }
+
     // QMS acceptance rotation W on the acceptance qubit (the MSB), factors per
     // energy reading Enew = (j >> shift) & (L-1), j the element with acc = 0
     __device__ __noinline__ void w_oracle(int qacc, int shift, uint32_t L, const double* f1, const double* f2) {
@@ -674,7 +967,7 @@ struct Qms {
         const int nbits = cx.dist(c) ? cx.nl : cx.nl - 1;
         const int nw = (int)(blockDim.x >> 5);
         int m = 0, G = 1;
-        if (s <= 9) {
+        if (s <= kChunkSpins) {
             // at least 5 (a warp), up to 8 for register-level parallelism while
             // leaving a chunk per warp; when c is local and >= 5 the chunk stays
             // below it, so a chunk's elements are equally spaced
@@ -686,13 +979,17 @@ struct Qms {
             if (m < s) m = s;
             if (m > nbits) m = nbits;
         } else {
-            // longer rings: chunks of 9 spin bits, the rest across a warp group
-            m = 9;
-            G = 1 << (s - 9);
+            // longer rings: chunks of kChunkSpins spin bits, the rest across a warp group
+            m = kChunkSpins;
+            G = 1 << (s - kChunkSpins);
         }
         *m_out = m;
         *G_out = G;
-        return nbits >= 5 && nbits >= s && m >= 5 && G <= 8 && G <= nw && (G == 1 || MODE == 2 || cx.dist(c) || c >= m);
+        // the exchange needs equally spaced chunk elements (modes 0, 1) or a
+        // staging area large enough for every warp's chunk (mode 2)
+        const bool xok = G == 1 || (MODE == 2 ? cx.stage_elems >= 2u * blockDim.x * (uint32_t)kStageR
+                                              : (cx.dist(c) || c >= m));
+        return nbits >= 5 && nbits >= s && m >= 5 && G <= 8 && G <= nw && xok;
     }
 
     // the coefficient tables of this chain (exp(-iHt) = Trotter steps of width
@@ -729,6 +1026,30 @@ struct Qms {
                 sincos(dir == 0 ? -powr * P->t_pe * P->t_shift : powr * P->t_pe * P->t_shift, &su, &cu);
                 tb->u1c[dir][trg] = (T)cu;
                 tb->u1s[dir][trg] = (T)su;
+            }
+        }
+        const int L = 1 << e;
+        for (int idx = threadIdx.x; idx < 3 * L; idx += blockDim.x) {
+            const int v = idx % L, which = idx / L;
+            double ang;
+            if (which == 0) {
+                ang = 2.0 * M_PI * (double)v / (double)L;
+            } else {
+                // all phase-estimation shifts U1(-+2^(e-1-trg) t_pe E_min) on the
+                // energy qubits set in v, as one phase
+                ang = 0.0;
+                for (int trg = 0; trg < e; ++trg)
+                    if ((v >> trg) & 1) ang += (double)(1u << (e - 1 - trg)) * P->t_pe * P->t_shift;
+                if (which == 1) ang = -ang;
+            }
+            double sa, ca;
+            sincos(ang, &sa, &ca);
+            if (which == 0) {
+                tb->rtc[v] = (T)ca;
+                tb->rts[v] = (T)sa;
+            } else {
+                tb->u1v_c[which - 1][v] = (T)ca;
+                tb->u1v_s[which - 1][v] = (T)sa;
             }
         }
         for (int idx = threadIdx.x; idx < 2 * 8; idx += blockDim.x) {
@@ -774,39 +1095,52 @@ struct Qms {
         }
     }
 
-    // QFT over the energy register (phases 2 pi / 2^m, the reference's table)
-    __device__ void qft(bool inverse) {
-        if (!inverse) {
-            for (int o = e - 1; o >= 0; o--) {
-                cx.h(s + o);
-                for (int i = o - 1; i >= 0; i--) cx.cu1(s + i, s + o, tb->qc[0][o - i], tb->qs[0][o - i]);
+    // One fused step of a QFT over the energy register: the controlled phases
+    // onto qubit o (reference: cu1(s+i, s+o, -+2 pi / 2^(1+o-i)) for i < o, whose
+    // product is the phase -+2 pi v_low / 2^(o+1) on elements with bit o set,
+    // v_low the lower register bits) as one diagonal, optionally times the
+    // phase-estimation shifts (dir's U1 table), fused with H on qubit o.
+    __device__ void qft_step(int o, bool inverse, int u1dir) {
+        const int L = 1 << e;
+        for (int v = threadIdx.x; v < L; v += blockDim.x) {
+            T c = (T)1, sn = (T)0;
+            if ((v >> o) & 1) {
+                const int kx = (v & ((1 << o) - 1)) << (e - o - 1);
+                c = tb->rtc[kx];
+                sn = inverse ? -tb->rts[kx] : tb->rts[kx];
             }
-        } else {
-            for (int o = 0; o < e; o++) {
-                for (int i = 0; i < o; i++) cx.cu1(s + i, s + o, tb->qc[1][o - i], tb->qs[1][o - i]);
-                cx.h(s + o);
+            if (u1dir >= 0) {
+                const T uc = tb->u1v_c[u1dir][v], us = tb->u1v_s[u1dir][v];
+                const T t = c;
+                c = t * uc - sn * us;
+                sn = sn * uc + t * us;
             }
+            tb->dc[v] = c;
+            tb->ds[v] = sn;
         }
+        __syncthreads();
+        // inverse QFT: phases then H(o); forward: H(o) then phases
+        cx.diag_h(inverse, s + o, s, e, tb->dc, tb->ds);
     }
 
+    // the reference's apply_phase_estimation: H on the energy register, the
+    // controlled powers of exp(-iHt) with their U1(-2^k t E_min) shifts (the
+    // shifts are diagonal and commute with the evolutions, so they join the
+    // first QFT step), then the inverse QFT
     __device__ void phi() {
         nphi++;
-        for (int kk = 0; kk < e; ++kk) cx.h(s + kk);
-        for (int trg = e - 1; trg > -1; --trg) {
-            evolution(0, trg);
-            cx.u1(s + trg, 1, tb->u1c[0][trg], tb->u1s[0][trg]);
-        }
-        qft(true);
+        cx.h_layer(s, e);
+        for (int trg = e - 1; trg > -1; --trg) evolution(0, trg);
+        for (int o = 0; o < e; o++) qft_step(o, true, o == 0 ? 0 : -1);
     }
 
+    // apply_phase_estimation_inverse: the QFT (its last step also carries the
+    // U1 shifts), the evolutions, H on the energy register
     __device__ void phi_inverse() {
         nphi++;
-        qft(false);
-        for (int trg = 0; trg < e; ++trg) {
-            evolution(1, trg);
-            cx.u1(s + trg, 1, tb->u1c[1][trg], tb->u1s[1][trg]);
-        }
-        for (int kk = 0; kk < e; ++kk) cx.h(s + kk);
+        for (int o = e - 1; o >= 0; o--) qft_step(o, false, o == 0 ? 1 : -1);
+        for (int trg = 0; trg < e; ++trg) evolution(1, trg);
+        cx.h_layer(s, e);
     }
 
     __device__ void w() {
@@ -837,18 +1171,10 @@ struct Qms {
         cx.h(gCi);
     }
 
-    __device__ void reset(int q) {
-        const double r = cx.draw();
-        if (cx.measure(q, r)) cx.x(q);
-    }
-
-    __device__ uint32_t read_energy() {
-        double r[8];
-        for (int kk = 0; kk < e; ++kk) r[kk] = cx.draw();
-        uint32_t v = 0;
-        for (int kk = 0; kk < e; ++kk) v += (uint32_t)cx.measure(s + kk, r[kk]) << kk;
-        return v;
-    }
+    // measure_qbits on the energy register with e fresh draws
+    __device__ uint32_t read_energy() { return cx.measure_register(s, e, false, tb->hist); }
+    // apply_reset on the energy register (and the acceptance qubit above it)
+    __device__ void reset_energy(bool with_acc) { cx.measure_register(s, with_acc ? e + 1 : e, true, tb->hist); }
 
     __device__ double energy_of(uint32_t v) const { return P->t_shift + v / (double)(P->pe_factor * L); }
 
@@ -885,13 +1211,11 @@ struct Qms {
     // one Metropolis step; returns 1/2 accepted (not/sampled), 3/4 restored, -1 failed
     __device__ int metro_step(bool take, double* Eout, double* Aout, bool* sampled) {
         *sampled = false;
-        for (int kk = 0; kk < e; ++kk) reset(s + kk);
-        reset(acc);
+        reset_energy(true);
         phi();
         const uint32_t eo = read_energy();
         E_old = eo;
-        for (int kk = 0; kk < e; ++kk)
-            if ((eo >> kk) & 1u) cx.x(s + kk);
+        cx.xor_register(s, e, eo);
         gCi = draw_C();
         apply_U();
         const int c_acc = cx.measure(acc, cx.draw());
@@ -900,11 +1224,10 @@ struct Qms {
             phi_inverse();
             if (!take) return 1;
             *Eout = energy_of(en);
-            for (int kk = 0; kk < e; ++kk)
-                if ((en >> kk) & 1u) cx.x(s + kk);
+            cx.xor_register(s, e, en);
             *Aout = measure_magnetisation();
             *sampled = true;
-            for (int kk = 0; kk < e; ++kk) reset(s + kk);
+            reset_energy(false);
             phi();
             read_energy();
             phi_inverse();
@@ -920,10 +1243,10 @@ struct Qms {
             if (E_old == en) {
                 if (take) {
                     *Eout = energy_of(E_old);
-                    for (int kk = 0; kk < e; ++kk) reset(s + kk);
+                    reset_energy(false);
                     *Aout = measure_magnetisation();
                     *sampled = true;
-                    for (int kk = 0; kk < e; ++kk) reset(s + kk);
+                    reset_energy(false);
                     phi();
                     read_energy();
                     phi_inverse();
@@ -992,6 +1315,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 256 : 512, 1) k_qms_tfim(cons
         q.cx.gre = sre;
         q.cx.gim = sim;
         q.cx.stage = reinterpret_cast<T*>(smem_raw);
+        q.cx.stage_elems = a.stage_elems;
         q.tb = &tbl;
         q.fill_tables();
         if (MODE == 2) {

@@ -45,7 +45,8 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-qms", action="store_true")
     ap.add_argument("--qms-chains", type=int, default=1024)
-    ap.add_argument("--qms-steps", type=int, default=3)
+    ap.add_argument("--qms-steps", type=int, default=6)
+    ap.add_argument("--skip-30", action="store_true", help="skip the 30-qubit FP64 repeat")
     return ap.parse_args()
 
 
@@ -142,32 +143,58 @@ def qms_section(n_chains, steps, seed=2024):
     """Batched quantum Metropolis sampling of TFIM rings: a sample of the
     4096-chain workload (spins 4-10, energy register 4-6 qubits, J = 1,
     h ~ U[0.5, 1.5], beta ~ U[0.2, 2.0], dt = 0.1, one PCG32 stream per chain),
-    run as FP32 and FP64 batches, against the host-driven plain GPU chain (the
-    drop-in qms driver on the libsq state API) on a 7-spin, 5-energy-qubit ring."""
+    run as resumable batches (segments of 2 steps replayed from a CUDA graph;
+    FP32 with autotuned CTA sizes) in FP32 and FP64, against the host-driven
+    plain GPU chain (the drop-in qms driver on the libsq state API) on a 7-spin,
+    5-energy-qubit ring."""
     import numpy as np
-    from suqa_gb300.batch import TfimChain, run_tfim_batch
+    from suqa_gb300.batch import Batch, TfimChain, run_tfim_batch
     rng = np.random.default_rng(seed)
     chains = [TfimChain(spins=int(rng.integers(4, 11)), ene_qbits=int(rng.integers(4, 7)), steps=steps,
                         beta=float(rng.uniform(0.2, 2.0)), h=float(rng.uniform(0.5, 1.5)), thermalization=0,
                         seed=1 + i) for i in range(n_chains)]
-    out = {"workload": f"{n_chains} TFIM-ring chains x {steps} Metropolis steps (8-17 qubits)"}
-    runs = {}
+    out = {"workload": f"{n_chains} TFIM-ring chains x {steps} Metropolis steps (8-17 qubits)",
+           "mode": "resumable batch, segments of 2 steps from a CUDA graph, all width classes concurrent"}
+    runs, batches = {}, {}
     for prec in ("f32", "f64"):
         t0 = time.perf_counter()
-        r, ms = run_tfim_batch(chains, prec)
-        runs[prec] = r
+        b = Batch(chains, prec, segment_steps=2, use_graph=True, autotune=(prec == "f32"))
+        t1 = time.perf_counter()
+        ms = b.run(steps)
+        r = b.results()
+        runs[prec], batches[prec] = r, b
+        cyc = sum(x.cycles for x in r)
         out[prec] = {"chain_steps_per_s": n_chains * steps / (ms / 1e3), "device_ms": ms,
-                     "wall_s": time.perf_counter() - t0,
-                     "phase_estimations_per_step": float(np.mean([x.phase_estimations for x in r])) / steps}
-    # FP32 vs FP64 on identical chains and draws: identical measured sequences and energies
-    same = sum(1 for a, b in zip(runs["f32"], runs["f64"])
-               if a.accepted == b.accepted and np.array_equal(a.E, b.E) and np.array_equal(a.A, b.A))
-    e32 = np.concatenate([x.E for x in runs["f32"]])
-    e64 = np.concatenate([x.E for x in runs["f64"]])
-    out["fp32_vs_fp64"] = {"chains_identical": same, "chains": n_chains,
-                           "mean_E_f32": float(e32.mean()) if len(e32) else None,
-                           "mean_E_f64": float(e64.mean()) if len(e64) else None,
-                           "stderr_E_f64": float(e64.std() / max(1, len(e64)) ** 0.5) if len(e64) else None}
+                     "setup_s": t1 - t0, "wall_s": time.perf_counter() - t0,
+                     "phase_estimations_per_step": float(np.mean([x.phase_estimations for x in r])) / steps,
+                     "evolution_share_of_sm_time": sum(x.evolution_cycles for x in r) / max(cyc, 1),
+                     "plan": b.plan()}
+    # FP32 vs FP64 on identical chains and draws: measured sequences, energies, and
+    # the final amplitudes of chains whose sequences agree (the FP64 batch chain is
+    # the plain reference procedure, outcome for outcome)
+    same = [i for i, (a, b) in enumerate(zip(runs["f32"], runs["f64"]))
+            if a.accepted == b.accepted and np.array_equal(a.E, b.E) and np.array_equal(a.A, b.A)]
+    amp_err = []
+    for i in same[:32]:
+        s32, s64 = batches["f32"].state(i), batches["f64"].state(i)
+        amp_err.append(float(np.max(np.abs(s32 - s64)) / np.max(np.abs(s64))))
+    groups = {}
+    for c, a, b in zip(chains, runs["f32"], runs["f64"]):
+        g = groups.setdefault(c.spins, {"f32": [], "f64": []})
+        g["f32"].append(a.E)
+        g["f64"].append(b.E)
+    per_group = {}
+    for sp, g in sorted(groups.items()):
+        e32, e64 = np.concatenate(g["f32"]), np.concatenate(g["f64"])
+        if len(e64) < 2:
+            continue
+        per_group[str(sp)] = {"mean_E_f32": float(e32.mean()), "mean_E_f64": float(e64.mean()),
+                              "stderr_E_f64": float(e64.std() / len(e64) ** 0.5), "samples": int(len(e64))}
+    out["fp32_vs_fp64"] = {"chains_identical": len(same), "chains": n_chains,
+                           "max_rel_amplitude_error_f32": max(amp_err) if amp_err else None,
+                           "amplitude_error_chains": len(amp_err), "energy_by_ring_length": per_group}
+    for b in batches.values():
+        b.close()
     # plain GPU chain: one chain, one launch per fused gate group, host sync per measurement
     exe = os.path.join(ROOT, "suqa_gb300", "_build", "qms_tfim_s7")
     plain_steps = 4
@@ -183,9 +210,9 @@ def qms_section(n_chains, steps, seed=2024):
     # the same chain run by the batch engine has identical outcomes, hence the same
     # number of phase estimations: the per-estimation rate removes the seed-dependent
     # length of the restoration loops from the comparison
-    same, _ = run_tfim_batch([TfimChain(spins=7, ene_qbits=5, steps=plain_steps, beta=1.0, h=1.0, ene_min=-14.0,
-                                        ene_max=14.0, thermalization=0, seed=5)], "f64")
-    plain_pe = same[0].phase_estimations / dt if cp.returncode == 0 else None
+    same1, _ = run_tfim_batch([TfimChain(spins=7, ene_qbits=5, steps=plain_steps, beta=1.0, h=1.0, ene_min=-14.0,
+                                         ene_max=14.0, thermalization=0, seed=5)], "f64")
+    plain_pe = same1[0].phase_estimations / dt if cp.returncode == 0 else None
     f32_pe = out["f32"]["phase_estimations_per_step"] * out["f32"]["chain_steps_per_s"]
     out["plain_gpu_chain"] = {"steps_per_s": plain, "phase_estimations_per_s": plain_pe,
                               "config": "7 spins, 5 energy qubits (13 qubits), FP64, host-driven (libsq state API)"}
@@ -374,6 +401,51 @@ def main():
         del h32r, h32i
         st = None
 
+    # secondary: the same gate mix on a 30-qubit FP64 state (16 GiB), device-resident
+    # (the state is drawn on the device: re, im ~ N(0, 1) from torch's seeded
+    # generator, normalised in FP64), one warm-up and one timed pass of 1000 gates
+    n30_line = None
+    if args.precision == "f64" and rank == 0 and not args.skip_30 and n < 30:
+        n30 = 30
+        g30 = random_circuit(n30, args.gates, seed=7)
+        st30 = State(n30, "f64")
+        st30.set_stream(stream.cuda_stream)
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(7)
+        pre, pim = st30.device_ptrs()
+        N30 = 1 << n30
+        nrm2 = 0.0
+        for ptr in (pre, pim):
+            t = torch.randn(N30, dtype=torch.float64, device="cuda", generator=gen)
+            nrm2 += float((t * t).sum())
+            torch.as_tensor(_DeviceArray(ptr, N30), device="cuda").copy_(t)
+            del t
+        nrm = nrm2 ** 0.5
+        for ptr in (pre, pim):
+            torch.as_tensor(_DeviceArray(ptr, N30), device="cuda").div_(nrm)
+        torch.cuda.synchronize()
+        apply_circuit(st30, g30)
+        st30.flush()
+        torch.cuda.synchronize()
+        st30.set_timing(True)
+        st30.kernel_time()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        apply_circuit(st30, g30)
+        st30.flush()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ms30 = f0.elapsed_time(f1)
+        k30, l30, b30 = st30.kernel_time()
+        alg30 = algorithmic_bytes(g30, n30, 16)
+        n30_line = {"value": alg30 / (ms30 / 1e3) / 1e9, "unit": "GB/s", "ms_per_step": ms30,
+                    "n_qubits": n30, "state_gib": 16, "steps": 1, "warmup": 1,
+                    "gates_per_s": len([g for g in g30 if g[0] != "measure"]) / (ms30 / 1e3),
+                    "pass_kernel_gbs": b30 / (k30 / 1e3) / 1e9 if k30 > 0 else None,
+                    "pass_kernel_frac_of_hbm": (b30 / (k30 / 1e3) / 1e9 / peak) if (k30 > 0 and peak) else None,
+                    "state": "device-drawn N(0,1), torch generator seed 7, normalised"}
+        st30.close()
+
     qms = None
     if rank == 0 and not args.skip_qms:
         qms = qms_section(args.qms_chains, args.qms_steps)
@@ -401,12 +473,20 @@ def main():
                 "roofline": roofline,
                 "cpu_baseline": cpu,
                 "fp32_same_circuit": fp32_line,
+                "fp64_30_qubits": n30_line,
                 "qms_batched": qms}
         print(json.dumps(line), flush=True)
     if st is not None:
         st.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+class _DeviceArray:
+    """A device buffer of doubles owned by libsq, exposed to torch without a copy."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 3}
 
 
 def traffic_per_launch():

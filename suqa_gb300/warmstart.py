@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import time
 
 import numpy as np
 
@@ -141,14 +142,16 @@ def training_set(chains, runs, burn_in):
 
 def burn_in_experiment(spins=(4, 5, 6), ene_qbits=4, train_chains=512, train_steps=12, train_burn=6,
                        eval_groups=((6, 1.0, 0.3), (6, 1.0, 1.0), (6, 0.7, 1.8)), eval_chains=96, eval_steps=8,
-                       precision="f32", iters=1500, seed=7):
+                       precision="f32", iters=1500, seed=7, eval_ene_qbits=None):
     """Trains the network on plain cold-start chains and compares warm- and
     cold-started chains of held-out parameter sets.  Returns a dict with, per
     group, the equilibrium energy (cold chains after burn-in), the mean energy
     error of the first samples for cold and warm starts, and the number of steps
     each start needs before its step-averaged energy stays within two standard
-    errors of equilibrium."""
+    errors of equilibrium.  The training chains use ene_qbits energy qubits, the
+    evaluation chains eval_ene_qbits (default: the same)."""
     from .batch import TfimChain, run_tfim_batch
+    ee = ene_qbits if eval_ene_qbits is None else eval_ene_qbits
     rng = np.random.default_rng(seed)
     chains = [TfimChain(spins=int(rng.choice(spins)), ene_qbits=ene_qbits, steps=train_steps,
                         beta=float(rng.uniform(0.2, 2.0)), h=float(rng.uniform(0.5, 1.5)), thermalization=0,
@@ -156,17 +159,32 @@ def burn_in_experiment(spins=(4, 5, 6), ene_qbits=4, train_chains=512, train_ste
     runs, ms_data = run_tfim_batch(chains, precision)
     x, t, m = training_set(chains, runs, train_burn)
     net = WarmStartNet(seed=seed)
+    t0 = time.perf_counter()
     losses = net.fit(x, t, m, iters=iters, batch=256, lr=2e-3, seed=seed)
-    out = {"train_samples": int(sum(len(r.E) for r in runs)), "train_rows": int(x.shape[0]),
-           "data_device_ms": ms_data, "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-20:])),
-           "groups": []}
+    fit_s = time.perf_counter() - t0
+    out = {"train_chains": train_chains, "train_qubits": sorted({c.nqubits for c in chains}),
+           "train_samples": int(sum(int(np.sum(r.step >= train_burn)) for r in runs)),
+           "train_rows": int(x.shape[0]), "data_device_ms": ms_data,
+           "data_chain_steps_per_s": train_chains * train_steps / (ms_data / 1e3),
+           "fit_iters": iters, "fit_s": fit_s,
+           "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-20:])),
+           "eval_chains_per_group": eval_chains, "eval_qubits": None, "groups": []}
+    # every group's cold and warm chains run as one batch (better load balance)
+    allc, angs = [], []
     for gi, (s, h, beta) in enumerate(eval_groups):
-        base = dict(spins=s, ene_qbits=ene_qbits, steps=eval_steps, beta=beta, h=h, thermalization=0)
-        cold = [TfimChain(seed=50_000 + 1000 * gi + k, **base) for k in range(eval_chains)]
+        base = dict(spins=s, ene_qbits=ee, steps=eval_steps, beta=beta, h=h, thermalization=0)
         ang = net.angles(s, 1.0, h, beta)
-        warm = [TfimChain(seed=50_000 + 1000 * gi + k, warm_angles=ang, **base) for k in range(eval_chains)]
-        rc, _ = run_tfim_batch(cold, precision)
-        rw, _ = run_tfim_batch(warm, precision)
+        angs.append(ang)
+        allc += [TfimChain(seed=50_000 + 1000 * gi + k, **base) for k in range(eval_chains)]
+        allc += [TfimChain(seed=50_000 + 1000 * gi + k, warm_angles=ang, **base) for k in range(eval_chains)]
+    out["eval_qubits"] = allc[0].nqubits
+    rall, ms_eval = run_tfim_batch(allc, precision)
+    out["eval_device_ms"] = ms_eval
+    out["eval_chain_steps_per_s"] = len(allc) * eval_steps / (ms_eval / 1e3)
+    for gi, (s, h, beta) in enumerate(eval_groups):
+        o = 2 * eval_chains * gi
+        rc, rw = rall[o:o + eval_chains], rall[o + eval_chains:o + 2 * eval_chains]
+        ang = angs[gi]
 
         def per_step(rr):
             mat = np.full((len(rr), eval_steps), np.nan)
@@ -184,18 +202,58 @@ def burn_in_experiment(spins=(4, 5, 6), ene_qbits=4, train_chains=512, train_ste
         mc, sc = per_step(rc)
         mw, _ = per_step(rw)
         eq = float(np.nanmean(mc[eval_steps // 2:]))
-        err = float(np.nanmean(sc[eval_steps // 2:]))
+        err = float(np.nanmean(sc[eval_steps // 2:]))  # standard error of one step's mean
+        err_eq = err / np.sqrt(max(1, eval_steps - eval_steps // 2))  # ... of the equilibrium estimate
         first = slice(1, 4)  # step 0 is never sampled (the driver samples from step 1 on)
 
         def burn(mean):
-            for k in range(1, eval_steps):
-                if np.all(np.abs(mean[k:] - eq) <= 2 * err + 1e-12):
+            # first step from which every 3-step average of the step means stays
+            # within two standard errors of the equilibrium estimate
+            tol = 2.0 * (err / np.sqrt(3.0) + err_eq) + 1e-12
+            for k in range(1, eval_steps - 2):
+                if all(abs(np.nanmean(mean[j:j + 3]) - eq) <= tol for j in range(k, eval_steps - 2)):
                     return k
             return eval_steps
 
-        out["groups"].append({"spins": s, "h": h, "beta": beta, "E_eq": eq, "E_eq_err": err,
+        late = slice(eval_steps // 2, eval_steps)
+        q4 = slice(3 * eval_steps // 4, eval_steps)
+        head = slice(1, min(11, eval_steps))
+        out["groups"].append({"spins": s, "h": h, "beta": beta, "E_eq": eq, "E_eq_err": float(err_eq),
+                              "step_mean_err": err,
+                              "cold_excess_first10": float(np.nansum(np.abs(mc[head] - eq))),
+                              "warm_excess_first10": float(np.nansum(np.abs(mw[head] - eq))),
+                              "cold_curve": [round(float(v), 3) for v in mc[:min(12, eval_steps)]],
+                              "warm_curve": [round(float(v), 3) for v in mw[:min(12, eval_steps)]],
                               "warm_angle": ang[0], "cold_first_err": float(np.nanmean(np.abs(mc[first] - eq))),
                               "warm_first_err": float(np.nanmean(np.abs(mw[first] - eq))),
-                              "cold_burn_in_steps": burn(mc), "warm_burn_in_steps": burn(mw)})
+                              "cold_burn_in_steps": burn(mc), "warm_burn_in_steps": burn(mw),
+                              "warm_late_E": float(np.nanmean(mw[late])),
+                              "cold_last_quarter_E": float(np.nanmean(mc[q4])),
+                              "warm_last_quarter_E": float(np.nanmean(mw[q4])),
+                              "cold_curve_by_10": [round(float(np.nanmean(mc[k:k + 10])), 3)
+                                                   for k in range(0, eval_steps, 10)],
+                              "warm_curve_by_10": [round(float(np.nanmean(mw[k:k + 10])), 3)
+                                                   for k in range(0, eval_steps, 10)],
+                              "warm_late_minus_cold_late": float(np.nanmean(mw[late]) - eq)})
     net.close()
     return out
+
+
+# The learned warm-start study at its full size: 12-spin TFIM rings, training
+# data from 1024 plain cold-start chains (4 energy qubits, 17 qubits) with 50
+# samples each after 10 burn-in steps (~48k samples), evaluation on 2 groups of
+# 48 chains of 12 spins + 6 energy qubits (19 qubits), 100 steps, FP32; the
+# equilibrium energy of a group is the cold chains' mean over steps 50-99.
+FULL_STUDY = dict(spins=(12,), ene_qbits=4, train_chains=1024, train_steps=60, train_burn=10,
+                  eval_groups=((12, 1.0, 1.0), (12, 0.8, 1.9)),
+                  eval_chains=48, eval_steps=100, eval_ene_qbits=6, iters=2000)
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="learned warm-start burn-in study")
+    ap.add_argument("--full", action="store_true", help="the full-size study (several GPU minutes)")
+    a = ap.parse_args()
+    res = burn_in_experiment(**FULL_STUDY) if a.full else burn_in_experiment()
+    print(json.dumps(res))

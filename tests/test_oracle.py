@@ -71,3 +71,16 @@ def test_pcg32_matches_reference_draws():
         tok = line.split()
         g = oracle.Pcg32(int(tok[0]))
         assert [g.doub() for _ in tok[1:]] == [float.fromhex(v) for v in tok[1:]]
+
+
+def test_tfim_exact_energies():
+    """Exact TFIM ring spectra: h = 0 is the classical ring (ground energy -J s),
+    J = 0 the free field (+-h per spin), and the 2-spin ring's ground energy is
+    -sqrt(4J^2 + 4h^2) (two bonds between the same pair)."""
+    import math
+    from tfim_exact import spectrum, thermal_energy
+    assert abs(spectrum(6, 1.0, 0.0)[0] + 6.0) < 1e-12
+    w = spectrum(4, 0.0, 0.7)
+    assert abs(w[0] + 2.8) < 1e-12 and abs(w[-1] - 2.8) < 1e-12
+    assert abs(spectrum(2, 1.0, 0.5)[0] + math.sqrt(4.0 + 1.0)) < 1e-12
+    assert abs(thermal_energy(4, 1.0, 1.0, 0.0)) < 1e-12  # traceless

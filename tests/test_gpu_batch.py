@@ -206,3 +206,28 @@ def test_wide_fp32_chains_in_global_memory_match_fp64():
         assert abs(np.vdot(st, st).real - 1.0) < 1e-4
         b.close()
     _same(res["f32"], res["f64"])
+
+
+def test_sharded_batches_sum_to_the_whole():
+    """Each rank's share run as its own batch (here one after the other on one
+    GPU) gives per-group sums that add up to the unsharded batch's, to the bit."""
+    from suqa_gb300 import shard
+    from suqa_gb300.batch import Batch
+    chains = _mixed(30, 5, seed=12)
+    key = lambda c: c.spins
+    b = Batch(chains, "f32")
+    b.run(5)
+    keys, whole = shard.group_sums(chains, b.results(), key)
+    b.close()
+    acc = np.zeros_like(whole)
+    pos = {k: i for i, k in enumerate(keys)}
+    for part in shard.partition(chains, 3):
+        sub = [chains[i] for i in part]
+        bs = Batch(sub, "f32")
+        bs.run(5)
+        k2, a2 = shard.group_sums(sub, bs.results(), key)
+        bs.close()
+        for k, row in zip(k2, a2):
+            acc[pos[k]] += row
+    assert np.allclose(acc, whole, rtol=1e-15, atol=0)
+    assert shard.run_sharded(chains, "f32", key=key, rank=0, world=1) == shard.averages(keys, whole)

@@ -90,6 +90,18 @@ __device__ __forceinline__ uint32_t insert_zero(uint32_t p, uint32_t b) {
     return ((p >> b) << (b + 1u)) | lo;
 }
 
+// p with a zero bit inserted at every set bit of m (ascending): enumerates the
+// indices whose bits in m are zero, so a loop runs only over the elements a
+// controlled or diagonal gate touches (every lane busy)
+__device__ __forceinline__ uint32_t deposit_zeros(uint32_t p, uint32_t m) {
+    while (m) {
+        const uint32_t b = (uint32_t)(__ffs(m) - 1);
+        p = insert_zero(p, b);
+        m &= m - 1u;
+    }
+    return p;
+}
+
 __device__ __forceinline__ int parity64(uint64_t x) { return __popcll(x) & 1; }
 
 // out = c*a + s*(i^k * b), the reference's rotate2 form (a*c -/+ x*s).  The
@@ -228,19 +240,22 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
             const uint32_t lcm = op.lcm, lcv = op.lcv;
             if (kind <= OP_PAULI && !(kind == OP_PAULI && op.lflip == 0u) || kind == OP_W) {
                 const uint32_t lp = op.lpair, lf = op.lflip;
+                // pairs (t0, t0 ^ lf) with bit lp of t0 clear and its control bits
+                // equal to lcv, enumerated directly (none if lp is a control bit
+                // required to be set)
+                const uint32_t sel = lcm | (1u << lp);
+                const uint32_t npair = ((lcm & lcv) >> lp) & 1u ? 0u : TS >> __popc(sel);
                 if (kind == OP_SWAPP) {
                     // include/suqa_cpu.hpp:223-253 (MCX), :268-319 (SWAP)
-                    for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
-                        const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
-                        if ((t0 & lcm) != lcv) continue;
+                    for (uint32_t u = threadIdx.x; u < npair; u += blockDim.x) {
+                        const uint32_t t0 = deposit_zeros(u, sel) | lcv, t1 = t0 ^ lf;
                         const T a0r = sre[t0], a0i = sim[t0];
                         sre[t0] = sre[t1]; sim[t0] = sim[t1]; sre[t1] = a0r; sim[t1] = a0i;
                     }
                 } else if (kind == OP_YP) {
                     // include/suqa_cpu.hpp:96-122: a1' = i a0, a0' = -i a1
-                    for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
-                        const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
-                        if ((t0 & lcm) != lcv) continue;
+                    for (uint32_t u = threadIdx.x; u < npair; u += blockDim.x) {
+                        const uint32_t t0 = deposit_zeros(u, sel) | lcv, t1 = t0 ^ lf;
                         const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
                         sre[t1] = -a0i; sim[t1] = a0r; sre[t0] = a1i; sim[t0] = -a1r;
                     }
@@ -256,9 +271,8 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                         sigma *= 0.7071067811865475;
                     } else {
                         const T h = (T)0.7071067811865475;
-                        for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
-                            const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
-                            if ((t0 & lcm) != lcv) continue;
+                        for (uint32_t u = threadIdx.x; u < npair; u += blockDim.x) {
+                            const uint32_t t0 = deposit_zeros(u, sel) | lcv, t1 = t0 ^ lf;
                             const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
                             sre[t0] = h * (a0r + a1r); sim[t0] = h * (a0i + a1i);
                             sre[t1] = h * (a0r - a1r); sim[t1] = h * (a0i - a1i);
@@ -287,9 +301,8 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                         }
                         sigma *= cbig ? op.c : op.s;
                     } else {
-                        for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
-                            const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
-                            if ((t0 & lcm) != lcv) continue;
+                        for (uint32_t u = threadIdx.x; u < npair; u += blockDim.x) {
+                            const uint32_t t0 = deposit_zeros(u, sel) | lcv, t1 = t0 ^ lf;
                             const int pz0 = tpar ^ (__popc(t0 & lzy) & 1);
                             const int k1 = (1 + ny + 2 * pz0) & 3;
                             const int k0 = (1 + ny + 2 * (pz0 ^ fz)) & 3;
@@ -312,9 +325,11 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                     }
                 }
             } else if (kind == OP_PHASE) {
-                // include/suqa_kernels.cuh:175-190, :209-221
-                for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
-                    if ((t & lcm) != lcv) continue;
+                // include/suqa_kernels.cuh:175-190, :209-221: only the elements
+                // whose bits in lcm equal lcv
+                const uint32_t nsel = TS >> __popc(lcm);
+                for (uint32_t u = threadIdx.x; u < nsel; u += blockDim.x) {
+                    const uint32_t t = deposit_zeros(u, lcm) | lcv;
                     const T ar = sre[t], ai = sim[t];
                     sre[t] = ar * c - ai * s;
                     sim[t] = ai * c + ar * s;
@@ -334,8 +349,9 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                     }
                     sigma *= cbig ? op.c : op.s;
                 } else {
-                    for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
-                        if ((t & lcm) != lcv) continue;
+                    const uint32_t nsel = TS >> __popc(lcm);
+                    for (uint32_t u = threadIdx.x; u < nsel; u += blockDim.x) {
+                        const uint32_t t = deposit_zeros(u, lcm) | lcv;
                         const T ar = sre[t], ai = sim[t];
                         T r, i;
                         rot_k<T>(ar, ai, ar, ai, (1 + 2 * (tpar ^ (__popc(t & lzy) & 1))) & 3, c, s, sneg, r, i);

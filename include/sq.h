@@ -228,6 +228,23 @@ int sq_batch_restore(sq_batch* b, const void* host, uint64_t bytes);
 /* the launch plan: one entry per chain-width class (widest first) */
 int sq_batch_plan(const sq_batch* b, sq_batch_class* info, uint32_t max, uint32_t* nclasses);
 
+/* --- batched time evolution with probability read-out ---
+ * The reference's evo driver (src/evo.cu:51-98) for many transverse-field
+ * Ising rings at once: job j evolves its ring (H = -J sum Z_i Z_{i+1} - h sum X_i)
+ * from |0...0> (or RY(ry_i) per spin) by `steps` first-order Trotter steps of
+ * width dt (ZZ bond phases, then the X rotations) and records, after 0, 1, ...,
+ * steps steps, the 2^spins basis probabilities in FP64 (prob_filter of every
+ * pattern).  probs receives, job after job, (steps + 1) rows of 2^spins values.
+ * spins 2..12. */
+typedef struct sq_tfim_evolution {
+    uint32_t spins, steps;
+    double J, h, dt;
+    uint32_t warm_start, pad;
+    double ry[20];
+} sq_tfim_evolution;
+int sq_tfim_evolve_batch(const sq_tfim_evolution* jobs, uint32_t njobs, int precision, double* probs,
+                         float* kernel_ms);
+
 /* --- learned warm start: a small MLP with BF16 weights/activations, FP32 sums ---
  * No reference counterpart.  in -> `layers` hidden layers of `hidden` GELU units
  * -> out.  Parameters are one flat FP32 array (W_l row-major, then b_l, layer by

@@ -41,6 +41,11 @@ class SqChainResult(C.Structure):
                 ("phase_estimations", C.c_uint32), ("cycles", C.c_uint64), ("evolution_cycles", C.c_uint64)]
 
 
+class SqTfimEvolution(C.Structure):
+    _fields_ = [("spins", C.c_uint32), ("steps", C.c_uint32), ("J", C.c_double), ("h", C.c_double),
+                ("dt", C.c_double), ("warm_start", C.c_uint32), ("pad", C.c_uint32), ("ry", C.c_double * 20)]
+
+
 class SqBatchOpts(C.Structure):
     _fields_ = [("segment_steps", C.c_uint32), ("use_graph", C.c_uint32), ("autotune", C.c_uint32),
                 ("threads", C.c_uint32), ("l2_budget_bytes", C.c_uint64), ("cta_qubits", C.c_uint32),
@@ -102,6 +107,8 @@ _SIGS = {
     "sq_batch_checkpoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "sq_batch_restore": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "sq_batch_plan": (C.c_int, [C.c_void_p, C.POINTER(SqBatchClass), C.c_uint32, C.POINTER(C.c_uint32)]),
+    "sq_tfim_evolve_batch": (C.c_int, [C.POINTER(SqTfimEvolution), C.c_uint32, C.c_int, C.c_void_p,
+                                       C.POINTER(C.c_float)]),
     "sq_mlp_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64]),
     "sq_mlp_destroy": (C.c_int, [C.c_void_p]),
     "sq_mlp_num_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),

@@ -10,7 +10,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import SQ_F32, SQ_F64, SqBatchClass, SqBatchOpts, SqChainResult, SqTfimChain, check
+from ._lib import SQ_F32, SQ_F64, SqBatchClass, SqBatchOpts, SqChainResult, SqTfimChain, SqTfimEvolution, check
 
 
 @dataclass
@@ -191,3 +191,38 @@ class Batch:
         return [{"n": c.n, "chains": c.count, "mode": MODES.get(c.mode, c.mode), "cluster": c.cluster,
                  "threads": c.threads, "grid": c.grid, "smem_bytes": c.smem_bytes,
                  "probe_ms": round(float(c.probe_ms), 3)} for c in info[:cnt.value]]
+
+
+@dataclass
+class TfimEvolution:
+    """A ring evolved by `steps` Trotter steps of width dt (see sq_tfim_evolve_batch)."""
+    spins: int
+    steps: int
+    dt: float
+    h: float
+    J: float = 1.0
+    warm_angles: list | None = None
+
+
+def run_tfim_evolution(jobs: list[TfimEvolution], precision: str = "f64"):
+    """Returns ([array (steps+1, 2^spins) of probabilities per job], device ms)."""
+    L = _lib.load()
+    n = len(jobs)
+    arr = (SqTfimEvolution * n)()
+    total = 0
+    for i, j in enumerate(jobs):
+        arr[i] = SqTfimEvolution(j.spins, j.steps, j.J, j.h, j.dt)
+        if j.warm_angles is not None:
+            arr[i].warm_start = 1
+            for k, a in enumerate(j.warm_angles[:20]):
+                arr[i].ry[k] = float(a)
+        total += (j.steps + 1) << j.spins
+    out = np.zeros(total, dtype=np.float64)
+    ms = C.c_float()
+    check(L.sq_tfim_evolve_batch(arr, n, _precision(precision), out.ctypes.data_as(C.c_void_p), C.byref(ms)))
+    res, off = [], 0
+    for j in jobs:
+        k = (j.steps + 1) << j.spins
+        res.append(out[off:off + k].reshape(j.steps + 1, 1 << j.spins).copy())
+        off += k
+    return res, ms.value

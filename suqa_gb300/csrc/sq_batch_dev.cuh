@@ -345,8 +345,9 @@ struct Ctx {
     __device__ void trotter_group(int s, int g0, int c, bool with_zz, const T* tc, const T* ts, T xc, T xs) {
         constexpr int G = 1 << M;
         const uint32_t smask = (1u << s) - 1u;
-        const bool local_c = !dist(c);
-        if (!local_c && !rbit(c)) { sync(); return; }
+        // c < 0: uncontrolled (the whole slice)
+        const bool local_c = c >= 0 && !dist(c);
+        if (c >= 0 && !local_c && !rbit(c)) { sync(); return; }
         const uint32_t ngroups = local_c ? (Nl >> (M + 1)) : (Nl >> M);
         for (uint32_t gi = threadIdx.x; gi < ngroups; gi += blockDim.x) {
             uint32_t base = ((gi >> g0) << (g0 + M)) | (gi & ((1u << g0) - 1u));
@@ -420,8 +421,9 @@ struct Ctx {
     // two FMAs per amplitude.
     template <int R, bool XG>
     __device__ __noinline__ void evolve_regs(int s, int c, int steps, int G, const T* tz, const T* sz, T tn) {
-        const bool local_c = !dist(c);
-        if (!local_c && !rbit(c)) { sync(); return; }
+        // c < 0: uncontrolled (the whole slice)
+        const bool local_c = c >= 0 && !dist(c);
+        if (c >= 0 && !local_c && !rbit(c)) { sync(); return; }
         constexpr int LR = R == 1 ? 0 : R == 2 ? 1 : R == 4 ? 2 : R == 8 ? 3 : R == 16 ? 4 : 5;
         constexpr int m = 5 + LR;
         const int lg = s > m ? s - m : 0;  // log2 G

@@ -15,6 +15,15 @@
 #include "system.cuh"
 #include "qms.cuh"
 
+#ifdef GATECOUNT
+// gate-cost counters, registered as src/qms.cu:33-39, 97-106 does
+GateCounter gctr_global("global");
+GateCounter gctr_metrostep("metro step");
+GateCounter gctr_sample("sample");
+GateCounter gctr_measure("measure");
+GateCounter gctr_reverse("reverse");
+#endif
+
 static void save_measures(const std::string& path) {
     FILE* f = fopen(path.c_str(), "a");
     for (uint i = 0; i < qms::E_measures.size(); ++i)
@@ -69,6 +78,12 @@ int main(int argc, char** argv) {
 
     suqa::setup(qms::nqubits);
     qms::setup(beta);
+#ifdef GATECOUNT
+    for (GateCounter* c : {&gctr_global, &gctr_metrostep, &gctr_sample, &gctr_measure, &gctr_reverse})
+        suqa::gatecounters.add_counter(c);
+    gctr_global.new_record();
+    gctr_sample.new_record();
+#endif
     init_state();
 
     const uint save_every = (qms::metro_steps + 19) / 20;

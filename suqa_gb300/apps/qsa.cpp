@@ -14,6 +14,15 @@
 #include "system.cuh"
 #include "qsa.cuh"
 
+#ifdef GATECOUNT
+// gate-cost counters, placed as src/qsa.cu:33-39, 130-137, 160-264 places them
+GateCounter gctr_global("global");
+GateCounter gctr_annstep("ann. step");
+GateCounter gctr_annealing("annealing");
+GateCounter gctr_sample("sample");
+GateCounter gctr_measure("measure");
+#endif
+
 static void save_measures(const std::string& path, int rej) {
     FILE* f = fopen(path.c_str(), "a");
     for (uint i = 0; i < qsa::E_measures.size(); ++i)
@@ -71,11 +80,20 @@ int main(int argc, char** argv) {
         fprintf(f, "# E A\n");
         fclose(f);
     }
+#ifdef GATECOUNT
+    for (GateCounter* c : {&gctr_global, &gctr_annstep, &gctr_annealing, &gctr_sample, &gctr_measure})
+        suqa::gatecounters.add_counter(c);
+    gctr_global.new_record();
+#endif
 
     int rejection = 0, rejection1 = 0, itctr = 0;
     double mean = 0.0, sq = 0.0;
     const double beta_i = qsa::beta / ((double)annealing_sequences);
     for (uint sample = 0; sample < sampling;) {
+#ifdef GATECOUNT
+        gctr_sample.new_record();
+        gctr_annealing.new_record();
+#endif
         std::vector<uint> c_test(qsa::szegedy_qbits, 0), c_E(qsa::szegedy_qbits, 0);
         uint c_ac = 0U;
         bool done = false;
@@ -85,9 +103,15 @@ int main(int argc, char** argv) {
             qsa::reset_non_syst_qbits();
             qsa_init_state();
             for (uint s = 0U; s < annealing_sequences; s++) {
+#ifdef GATECOUNT
+                gctr_annstep.new_record();
+#endif
                 move = qsa::draw_C();
                 qsa::apply_PE_szegedy(qsa::bm_states, qsa::bm_szegedy, (double)(s + 1) * beta_i, move);
                 suqa::measure_qbits(qsa::bm_szegedy, c_test, qsa::extract_rands(qsa::szegedy_qbits));
+#ifdef GATECOUNT
+                gctr_annstep.deactivate();
+#endif
                 if (qsa::creg_to_uint(c_test) != 0U) {  // left the stationary subspace: restart
                     restart = true;
                     rejection1++;
@@ -97,7 +121,13 @@ int main(int argc, char** argv) {
             }
             if (!restart) done = true;
         }
+#ifdef GATECOUNT
+        gctr_annealing.deactivate();
+#endif
         if (c_ac == 0U) {
+#ifdef GATECOUNT
+            gctr_measure.new_record();
+#endif
             qsa::apply_phase_estimation_measure(qsa::bm_states, qsa::bm_szegedy, qsa::t_phase_estimation_szegedy,
                                                 qsa::n_phase_estimation);
             suqa::measure_qbits(qsa::bm_szegedy, c_E, qsa::extract_rands(qsa::szegedy_qbits));
@@ -115,6 +145,9 @@ int main(int argc, char** argv) {
             qsa::X_measures.push_back(measure_X(qsa::rangen));
             std::cout << "iteration: " << sample + 1 << "/" << sampling << std::endl;
             save_measures(out, rejection1);
+#ifdef GATECOUNT
+            gctr_measure.deactivate();
+#endif
             ++sample;
         } else {
             rejection++;

@@ -73,6 +73,7 @@ def build_libsq(force=False):
 
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-w", "-I" + SHIM_INCLUDE, "-I" + INCLUDE]
 DRIVERS = ["qms", "qsa", "evo"]
+GC_DRIVERS = ["qms", "qsa"]
 
 
 def cxx():
@@ -87,17 +88,20 @@ def build_dropin(force=False):
              "triangle": os.path.join(PKG, "systems", "triangle.cpp")}
     for d in DRIVERS:
         units["app_" + d] = os.path.join(PKG, "apps", d + ".cpp")
+    for d in GC_DRIVERS:  # the same drivers with the reference's gate-cost counters
+        units["app_" + d + "_gc"] = os.path.join(PKG, "apps", d + ".cpp")
     jobs, objs = [], {}
     for name, src in units.items():
         o = os.path.join(BUILD, name + ".o")
         objs[name] = o
         if force or not _newer(o, [src] + headers):
-            jobs.append([cxx()] + CXX_FLAGS + ["-c", src, "-o", o])
+            extra = ["-DGATECOUNT"] if name.endswith("_gc") else []
+            jobs.append([cxx()] + CXX_FLAGS + extra + ["-c", src, "-o", o])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
         list(ex.map(_run, jobs))
     lib = os.path.join(BUILD, "libsq.so")
     outs = []
-    for d in DRIVERS:
+    for d in DRIVERS + [g + "_gc" for g in GC_DRIVERS]:
         exe = os.path.join(BUILD, d)
         deps = [objs["app_" + d], objs["suqa_shim"], objs["triangle"], lib]
         if force or jobs or not _newer(exe, deps):

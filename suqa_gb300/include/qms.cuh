@@ -31,6 +31,16 @@ void apply_C(const uint& Ci);
 void apply_C_inverse(const uint& Ci);
 std::vector<double> get_C_weigthsums();
 
+#ifdef GATECOUNT
+// gate-cost records of a metro step, a sample, a measurement, a restoration
+// (defined by the driver, as src/qms.cu:33-39)
+extern GateCounter gctr_global;
+extern GateCounter gctr_metrostep;
+extern GateCounter gctr_sample;
+extern GateCounter gctr_measure;
+extern GateCounter gctr_reverse;
+#endif
+
 namespace qms {
 
 uint syst_qbits;
@@ -153,6 +163,10 @@ inline uint draw_C() {
 inline void apply_W() {
     const int rc = sq_apply_qms_w(suqa::engine(), bm_acc, W_mask_Enew, bm_enes_new[0], curr_E_old, c_factor);
     if (rc != SQ_OK) throw std::runtime_error(std::string("qms::apply_W: ") + sq_last_error());
+    // cost: one (2 e)-controlled Toffoli per pair of energy levels (include/qms.cuh:324-328)
+    const GateRecord gr = GateCounter::n_ctrl_toffoli_gates(2 * ene_qbits);
+    const uint npairs = (ene_levels * (ene_levels - 1)) / 2;
+    suqa::gatecounters.increment_g1g2(npairs * gr.ng1, npairs * gr.ng2);
 }
 
 inline void apply_W_inverse() { apply_W(); }
@@ -184,6 +198,9 @@ inline void sample_observable_and_reproject(std::vector<uint>& c_E) {
 // return values: 1 accepted, 2 accepted and sampled, 3 rejected and restored,
 // 4 rejected, restored and sampled, -1 restoration failed
 inline int metro_step(bool take_measure) {
+#ifdef GATECOUNT
+    gctr_metrostep.new_record();
+#endif
     reset_non_syst_qbits();
     apply_Phi();
     std::vector<uint> c_E_news(ene_qbits, 0), c_E_olds(ene_qbits, 0);
@@ -201,16 +218,26 @@ inline int metro_step(bool take_measure) {
         suqa::measure_qbits(bm_enes_new, c_E_news, extract_rands(ene_qbits));
         apply_Phi_inverse();
         if (!take_measure) return 1;
+#ifdef GATECOUNT
+        gctr_measure.new_record();
+#endif
         E_measures.push_back(energy_of(creg_to_uint(c_E_news)));
         for (uint ei = 0U; ei < ene_qbits; ++ei)
             if (c_E_news[ei]) suqa::apply_x(bm_enes_new[ei]);
         sample_observable_and_reproject(c_E_news);
+#ifdef GATECOUNT
+        gctr_measure.deactivate();
+        gctr_sample.new_record();
+#endif
         return 2;
     }
 
     apply_U_inverse();
     int ret = 0;
     uint iters = 0;
+#ifdef GATECOUNT
+    gctr_reverse.new_record();
+#endif
     while (iters < max_reverse_attempts) {
         apply_Phi();
         suqa::measure_qbits(bm_enes_new, c_E_news, extract_rands(ene_qbits));
@@ -233,6 +260,9 @@ inline int metro_step(bool take_measure) {
         apply_U_inverse();
         iters++;
     }
+#ifdef GATECOUNT
+    gctr_reverse.deactivate();
+#endif
     if (record_reverse) reverse_counters.push_back(iters);
     if (iters == max_reverse_attempts) return -1;
     return ret;

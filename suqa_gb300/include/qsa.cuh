@@ -70,19 +70,26 @@ inline void fill_rphase(const uint& n) { fill_phase_table(rphase_m, n); }
 inline void fill_rphase_szegedy(const uint& n) { fill_phase_table(rphase_m_szegedy, n); }
 
 // The Szegedy control is the base of the global mask; inner controls add to it.
+// (each change also refreshes the gate counters' control count, include/qsa.cuh:70-96)
 inline void activate_gc_mask_szegedy(const bmReg& q_controls) {
     gc_mask_szegedy = 0U;
     for (const auto& q : q_controls) gc_mask_szegedy |= 1U << q;
     suqa::gc_mask = gc_mask_szegedy;
+    suqa::gatecounters.update_cmask_setbits(suqa::gc_mask);
 }
 inline void deactivate_gc_mask_szegedy() {
     gc_mask_szegedy = 0U;
     suqa::gc_mask = 0U;
+    suqa::gatecounters.update_cmask_setbits(suqa::gc_mask);
 }
 inline void activate_gc_mask_into_szegedy(const bmReg& q_controls) {
     for (const auto& q : q_controls) suqa::gc_mask |= 1U << q;
+    suqa::gatecounters.update_cmask_setbits(suqa::gc_mask);
 }
-inline void deactivate_gc_mask_into_szegedy() { suqa::gc_mask = gc_mask_szegedy; }
+inline void deactivate_gc_mask_into_szegedy() {
+    suqa::gc_mask = gc_mask_szegedy;
+    suqa::gatecounters.update_cmask_setbits(suqa::gc_mask);
+}
 
 std::vector<uint> bm_states;
 std::vector<uint> bm_enes;

@@ -37,6 +37,9 @@ typedef std::vector<uint> bmReg;
 namespace suqa {
 
 extern ComplexVec state;
+// gate-cost counters (reference include/gatecounters.hpp); drivers built with
+// -DGATECOUNT register their counters here
+extern GateCounterList gatecounters;
 
 #ifdef GPU
 #define NUM_THREADS 128

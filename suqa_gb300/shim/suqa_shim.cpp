@@ -46,12 +46,43 @@ void suqa::print_banner() {
     printf("\n   SUQA gate API on libsq (GB300, sm_103a)\n\n Simulator for Universal Quantum Algorithms\n\n");
 }
 
+GateCounterList suqa::gatecounters;
+
+namespace {
+// gate costs as the reference's GATECOUNT hooks (src/suqa.cu): a gate with
+// `extra` controls of its own under the global mask costs mult x an
+// (n + extra)-controlled Toffoli, n the mask's set bits when it last changed
+void count_gate(uint extra, uint mult = 1U) {
+    const GateRecord gr = GateCounter::n_ctrl_toffoli_gates(suqa::gatecounters.gc_mask_set_qbits + extra);
+    suqa::gatecounters.increment_g1g2(mult * gr.ng1, mult * gr.ng2);
+}
+// a k-qubit Pauli rotation (src/suqa.cu, end of apply_pauli_TP_rotation): one n-
+// and 2(k-1) (n+1)-controlled Toffolis, and with x > 0 non-Z factors two more
+// n-controlled Toffolis and 2(x-1) CNOTs for the basis changes
+void count_pauli(const std::vector<uint>& paulis) {
+    const uint n = suqa::gatecounters.gc_mask_set_qbits;
+    const uint k = (uint)paulis.size();
+    const GateRecord g0 = GateCounter::n_ctrl_toffoli_gates(n), g1 = GateCounter::n_ctrl_toffoli_gates(n + 1);
+    suqa::gatecounters.increment_g1g2(g0.ng1, g0.ng2);
+    suqa::gatecounters.increment_g1g2(2 * (k - 1) * g1.ng1, 2 * (k - 1) * g1.ng2);
+    uint x = 0;
+    for (uint p : paulis)
+        if (p != PAULI_Z) ++x;
+    if (x > 0) {
+        suqa::gatecounters.increment_g1g2(2 * g0.ng1, 2 * g0.ng2);
+        suqa::gatecounters.increment_g1g2(0, 2 * (x - 1));
+    }
+}
+}  // namespace
+
 void suqa::activate_gc_mask(const bmReg& q_controls) {
     for (const auto& q : q_controls) suqa::gc_mask |= 1U << q;
+    suqa::gatecounters.update_cmask_setbits(suqa::gc_mask);
 }
 
 void suqa::deactivate_gc_mask(const bmReg& q_controls) {
     for (const auto& q : q_controls) suqa::gc_mask &= ~(1U << q);
+    suqa::gatecounters.update_cmask_setbits(suqa::gc_mask);
 }
 
 double suqa::vnorm() {
@@ -84,13 +115,22 @@ void suqa::allocate_state(uint Dim) {
 }
 
 // ---- single-qubit gates
-void suqa::apply_x(uint q) { check(sq_apply_x(st(), q, suqa::gc_mask)); }
+void suqa::apply_x(uint q) {
+    check(sq_apply_x(st(), q, suqa::gc_mask));
+    count_gate(0);
+}
 void suqa::apply_x(const bmReg& qs) { for (const auto& q : qs) suqa::apply_x(q); }
-void suqa::apply_y(uint q) { check(sq_apply_y(st(), q, suqa::gc_mask)); }
+void suqa::apply_y(uint q) {
+    check(sq_apply_y(st(), q, suqa::gc_mask));
+    count_gate(0);
+}
 void suqa::apply_y(const bmReg& qs) { for (const auto& q : qs) suqa::apply_y(q); }
 void suqa::apply_z(uint q) { suqa::apply_u1(q, M_PI); }
 void suqa::apply_z(const bmReg& qs) { for (const auto& q : qs) suqa::apply_u1(q, M_PI); }
-void suqa::apply_h(uint q) { check(sq_apply_h(st(), q, suqa::gc_mask)); }
+void suqa::apply_h(uint q) {
+    check(sq_apply_h(st(), q, suqa::gc_mask));
+    count_gate(0);
+}
 void suqa::apply_h(const bmReg& qs) { for (const auto& q : qs) suqa::apply_h(q); }
 void suqa::apply_t(uint q) { suqa::apply_u1(q, M_PI / 4.0); }
 void suqa::apply_t(const bmReg& qs) { for (const auto& q : qs) suqa::apply_u1(q, M_PI / 4.0); }
@@ -102,6 +142,7 @@ void suqa::apply_s(const bmReg& qs) { for (const auto& q : qs) suqa::apply_u1(q,
 void suqa::apply_u1(uint q, double phase) { suqa::apply_u1(q, 1U, phase); }
 void suqa::apply_u1(uint q, uint q_mask, double phase) {
     check(sq_apply_u1(st(), q, q_mask, phase, suqa::gc_mask));
+    count_gate(0);
 }
 
 // ---- multi-qubit gates: control masks as src/suqa.cu:289-393 builds them
@@ -110,12 +151,14 @@ void suqa::apply_cx(const uint& q_control, const uint& q_target, const uint& q_m
     const uint64_t mask = mask_qs | (1ull << q_control);
     if (q_mask) mask_qs |= 1ull << q_control;
     check(sq_apply_mcx(st(), mask, mask_qs, q_target));
+    count_gate(1);
 }
 
 void suqa::apply_mcx(const bmReg& q_controls, const uint& q_target) {
     uint64_t mask = suqa::gc_mask;
     for (const auto& q : q_controls) mask |= 1ull << q;
     check(sq_apply_mcx(st(), mask, mask, q_target));
+    count_gate((uint)q_controls.size());
 }
 
 void suqa::apply_mcx(const bmReg& q_controls, const bmReg& q_mask, const uint& q_target) {
@@ -124,6 +167,7 @@ void suqa::apply_mcx(const bmReg& q_controls, const bmReg& q_mask, const uint& q
     for (size_t k = 0; k < q_controls.size(); ++k)
         if (q_mask[k]) mask_qs |= 1ull << q_controls[k];
     check(sq_apply_mcx(st(), mask, mask_qs, q_target));
+    count_gate((uint)q_controls.size());
 }
 
 void suqa::apply_cu1(uint q_control, uint q_target, double phase, uint q_mask) {
@@ -131,6 +175,7 @@ void suqa::apply_cu1(uint q_control, uint q_target, double phase, uint q_mask) {
     const uint64_t mask = mask_qs | (1ull << q_control);
     if (q_mask) mask_qs |= 1ull << q_control;
     check(sq_apply_mcu1(st(), mask, mask_qs, phase));
+    count_gate(1);
 }
 
 void suqa::apply_mcu1(const bmReg& q_controls, const bmReg& q_mask, const uint& q_target, double phase) {
@@ -140,18 +185,29 @@ void suqa::apply_mcu1(const bmReg& q_controls, const bmReg& q_mask, const uint& 
     for (size_t k = 0; k < q_controls.size(); ++k)
         if (q_mask[k]) mask_qs |= 1ull << q_controls[k];
     check(sq_apply_mcu1(st(), mask, mask_qs, phase));
+    count_gate((uint)q_controls.size());
 }
 
 void suqa::apply_mcu1(const bmReg& q_controls, const uint& q_target, double phase) {
     suqa::apply_mcu1(q_controls, std::vector<uint>(q_controls.size(), 1U), q_target, phase);
 }
 
-void suqa::apply_swap(const uint& q1, const uint& q2) { check(sq_apply_swap(st(), q1, q2, suqa::gc_mask)); }
+// a swap is three CNOTs (src/suqa.cu:409-415)
+void suqa::apply_swap(const uint& q1, const uint& q2) {
+    check(sq_apply_swap(st(), q1, q2, suqa::gc_mask));
+    count_gate(1, 3U);
+}
 
 void suqa::apply_phase_list(uint q0, uint q_size, const std::vector<double>& phases) {
     if (!(q_size > 0U && (uint)phases.size() == (1U << q_size)))
         throw std::runtime_error("ERROR: in suqa::apply_phase_list(): invalid q_size or phases.size()");
     check(sq_apply_phase_list(st(), q0, q_size, phases.data(), suqa::gc_mask));
+    // src/suqa.cu:442-453: 2^(q_size-2) (the reference's `1U<<(q_size+1)-3`, the
+    // shift count taken modulo 32) times an n- plus an (n+1)-controlled Toffoli
+    const uint fact = 1U << ((q_size + 1U - 3U) & 31U);
+    const uint n = suqa::gatecounters.gc_mask_set_qbits;
+    const GateRecord a = GateCounter::n_ctrl_toffoli_gates(n), b = GateCounter::n_ctrl_toffoli_gates(n + 1);
+    suqa::gatecounters.increment_g1g2(fact * (a.ng1 + b.ng1), fact * (a.ng2 + b.ng2));
 }
 
 void suqa::apply_pauli_TP_rotation(const bmReg& q_apply, const std::vector<uint>& pauli_TPtype, double phase) {
@@ -163,6 +219,7 @@ void suqa::apply_pauli_TP_rotation(const bmReg& q_apply, const std::vector<uint>
     if (rc == SQ_ERR_UNSUPPORTED)
         throw std::runtime_error("ERROR: unimplemented pauli TP rotation in the selected configuration");
     check(rc);
+    count_pauli(pauli_TPtype);
 }
 
 void suqa::apply_pauli_rotation(const bmReg& q_apply, const std::vector<uint>& paulis, double phase) {
@@ -170,6 +227,7 @@ void suqa::apply_pauli_rotation(const bmReg& q_apply, const std::vector<uint>& p
         throw std::runtime_error("ERROR: in suqa::apply_pauli_rotation(): qubit and Pauli lists differ in length");
     check(sq_apply_pauli_rotation(st(), (uint32_t)q_apply.size(), q_apply.data(), paulis.data(), phase,
                                   suqa::gc_mask, SQ_PAULI_EXACT));
+    count_pauli(paulis);
 }
 
 // ---- QFT (src/suqa.cu:611-661): H and controlled phases 2*pi/2^m
@@ -249,7 +307,10 @@ void suqa::setup(uint num_qubits) {
     suqa::allocate_state(1U << suqa::nq);
 }
 
-void suqa::clear() { deallocate_state(); }
+void suqa::clear() {
+    deallocate_state();
+    suqa::gatecounters.print_counts();  // prints only when a driver registered counters
+}
 
 void suqa::debug_print_state() {
     if (!g_state) return;

@@ -62,7 +62,7 @@ RUNS = [
 
 
 def build_reference():
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "tfim", "port", "-j8"], check=True)
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "tfim", "port", "gatecount", "-j8"], check=True)
 
 
 def gate_fixtures():
@@ -130,6 +130,35 @@ def run_fixtures():
         json.dump(manifest, f, indent=1)
 
 
+# runs repeated with the reference built with -DGATECOUNT: the printed gate-cost tables
+GATECOUNT_RUNS = ["qms_c1", "qms_rev", "qsa_c1"]
+
+
+def gate_count_table(stdout: str) -> str:
+    """The 'Gate counts' block the drivers print at suqa::clear()."""
+    lines = stdout.splitlines()
+    i = lines.index("Gate counts")
+    out = []
+    for ln in lines[i:]:
+        if out and ln == "" and len(out) > 3:
+            break
+        out.append(ln)
+    return "\n".join(out).strip() + "\n"
+
+
+def gatecount_fixtures():
+    rdir = os.path.join(HERE, "runs")
+    spec = {name: (exe, args) for name, exe, args, env in RUNS}
+    for name in GATECOUNT_RUNS:
+        exe, args = spec[name]
+        with tempfile.TemporaryDirectory() as td:
+            out = os.path.join(td, "out.txt")
+            argv = [os.path.join(REF, exe + "_gc")] + [a.replace("{out}", out) for a in args]
+            cp = subprocess.run(argv, capture_output=True, text=True, check=True)
+        with open(os.path.join(rdir, f"{name}_gatecounts.txt"), "w") as f:
+            f.write(gate_count_table(cp.stdout))
+
+
 def pcg_fixture():
     cp = subprocess.run([os.path.join(REF, "pcg_dump")], capture_output=True, text=True, check=True)
     with open(os.path.join(HERE, "pcg32_draws.txt"), "w") as f:
@@ -140,5 +169,6 @@ if __name__ == "__main__":
     build_reference()
     gate_fixtures()
     run_fixtures()
+    gatecount_fixtures()
     pcg_fixture()
     print("fixtures written to", HERE)

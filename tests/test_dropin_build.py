@@ -15,15 +15,17 @@ BUILD = os.path.join(ROOT, "suqa_gb300", "_build")
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")), reason="reference sources not present")
 
 
-def _compile(src, out, tmp):
-    cmd = ["g++", "-std=c++17", "-O1", "-w", "-DNDEBUG", "-x", "c++", "-I" + os.path.join(ROOT, "suqa_gb300", "include"),
-           "-I" + os.path.join(ROOT, "include"), "-c", src, "-o", out]
+def _compile(src, out, tmp, extra=()):
+    cmd = ["g++", "-std=c++17", "-O1", "-w", "-DNDEBUG", *extra, "-x", "c++",
+           "-I" + os.path.join(ROOT, "suqa_gb300", "include"), "-I" + os.path.join(ROOT, "include"), "-c", src, "-o", out]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
 
 
-@pytest.mark.parametrize("driver", ["qms", "qsa", "evo", "test_suqa"])
-def test_reference_driver_compiles_and_links_unchanged(driver, tmp_path):
+@pytest.mark.parametrize("driver,gatecount", [("qms", False), ("qsa", False), ("evo", False), ("test_suqa", False),
+                                             ("qms", True), ("qsa", True), ("test_suqa", True)])
+def test_reference_driver_compiles_and_links_unchanged(driver, gatecount, tmp_path):
+    """Also with -DGATECOUNT, the reference's gate-cost counter build."""
     lib = os.path.join(BUILD, "libsq.so")
     shim = os.path.join(BUILD, "suqa_shim.o")
     if not (os.path.exists(lib) and os.path.exists(shim)):
@@ -31,7 +33,7 @@ def test_reference_driver_compiles_and_links_unchanged(driver, tmp_path):
     objs = []
     for name in (driver, "system"):
         o = str(tmp_path / f"{name}.o")
-        _compile(os.path.join(REF, "src", f"{name}.cu"), o, tmp_path)
+        _compile(os.path.join(REF, "src", f"{name}.cu"), o, tmp_path, ("-DGATECOUNT",) if gatecount else ())
         objs.append(o)
     exe = str(tmp_path / driver)
     r = subprocess.run(["g++"] + objs + [shim, "-L" + BUILD, "-lsq", "-Wl,-rpath," + BUILD, "-o", exe],

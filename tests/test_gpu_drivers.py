@@ -56,3 +56,28 @@ def test_qms_tfim_drivers_match_reference_output(name, tmp_path):
     """The host-driven drop-in path with the TFIM ring plugin."""
     man, out, stdout = run_driver(name, tmp_path)
     assert open(out).read() == golden_io.run_output(name)
+
+
+def _gate_count_table(stdout):
+    lines = stdout.splitlines()
+    i = lines.index("Gate counts")
+    out = []
+    for ln in lines[i:]:
+        if out and ln == "" and len(out) > 3:
+            break
+        out.append(ln)
+    return "\n".join(out).strip() + "\n"
+
+
+@pytest.mark.parametrize("name", ["qms_c1", "qms_rev", "qsa_c1"])
+def test_gate_count_tables_match_reference(name, tmp_path):
+    """Drivers built with -DGATECOUNT print the reference's gate-cost table
+    (one- and two-qubit gate counts per metro step, sample, measurement,
+    restoration / annealing step) identically."""
+    man = golden_io.run_manifest()[name]
+    out = str(tmp_path / f"{name}.txt")
+    argv = [os.path.join(BUILD, man["driver"] + "_gc")] + [a.replace("{out}", out) for a in man["args"]]
+    cp = subprocess.run(argv, capture_output=True, text=True, timeout=900)
+    assert cp.returncode == 0, cp.stdout[-2000:] + cp.stderr[-2000:]
+    assert _gate_count_table(cp.stdout) == golden_io.run_output(f"{name}_gatecounts")
+    assert open(out).read() == golden_io.run_output(name)  # counting changes no result

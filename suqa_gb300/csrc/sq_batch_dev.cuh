@@ -92,8 +92,6 @@ struct Tables {
     T tz[2][8][24], sz[2][8][24];  // ZZ phase by domain-wall count (cos(hd)^s folded in on the register path)
     T tn[2][8], xc[2][8], xs[2][8];  // tan(hd), cos(hd), sin(hd) of the X rotations
     int steps[2][8], regs[2][8];   // Trotter steps of the controlled power; register path usable
-    T u1c[2][8], u1s[2][8];        // phase-estimation shift on energy qubit trg
-    T qc[2][8], qs[2][8];          // QFT controlled phase at distance k (forward / inverse)
     T rtc[128], rts[128];          // e^{i 2 pi k / 2^e}
     T u1v_c[2][128], u1v_s[2][128];  // all phase-estimation shifts as one phase per register value
     T dc[128], ds[128];            // the diagonal of the current fused QFT step
@@ -258,19 +256,6 @@ struct Ctx {
         sync();
     }
 
-    __device__ __noinline__ void x(int q) {
-        if (dist(q)) { cross_pair(q, 0); return; }
-        for (uint32_t p = threadIdx.x; p < Nl / 2; p += blockDim.x) {
-            const uint32_t i0 = ins0(p, (uint32_t)q), i1 = i0 | (1u << q);
-            const T r = re[at(i0)], i = im[at(i0)];
-            re[at(i0)] = re[at(i1)];
-            im[at(i0)] = im[at(i1)];
-            re[at(i1)] = r;
-            im[at(i1)] = i;
-        }
-        sync();
-    }
-
     // RY(theta) on a local qubit: a0' = c a0 - s a1, a1' = s a0 + c a1 (c, s of theta/2)
     __device__ __noinline__ void ry(int q, T cs, T sn) {
         for (uint32_t p = threadIdx.x; p < Nl / 2; p += blockDim.x) {
@@ -280,59 +265,6 @@ struct Ctx {
             im[at(i0)] = cs * a0i - sn * a1i;
             re[at(i1)] = sn * a0r + cs * a1r;
             im[at(i1)] = sn * a0i + cs * a1i;
-        }
-        sync();
-    }
-
-    // phase (cs + i sn) on the elements with bit q == val (U1 with q_mask = val)
-    __device__ __noinline__ void u1(int q, int val, T cs, T sn) {
-        if (dist(q)) {
-            if (rbit(q) == (uint32_t)val) {
-                for (uint32_t i = threadIdx.x; i < Nl; i += blockDim.x) {
-                    const T a = re[at(i)];
-                    re[at(i)] = a * cs - im[at(i)] * sn;
-                    im[at(i)] = im[at(i)] * cs + a * sn;
-                }
-            }
-            sync();
-            return;
-        }
-        for (uint32_t p = threadIdx.x; p < Nl / 2; p += blockDim.x) {
-            const uint32_t i = ins0(p, (uint32_t)q) | ((uint32_t)val << q);
-            const T a = re[at(i)];
-            re[at(i)] = a * cs - im[at(i)] * sn;
-            im[at(i)] = im[at(i)] * cs + a * sn;
-        }
-        sync();
-    }
-
-    // controlled phase: both bits set
-    __device__ __noinline__ void cu1(int qc, int qt, T cs, T sn) {
-        int fixed[2];
-        int nf = 0;
-        bool skip = false;
-        for (int q : {qc, qt}) {
-            if (dist(q)) {
-                if (!rbit(q)) skip = true;
-            } else {
-                fixed[nf++] = q;
-            }
-        }
-        if (!skip) {
-            const uint32_t cnt = Nl >> nf;
-            for (uint32_t p = threadIdx.x; p < cnt; p += blockDim.x) {
-                uint32_t i = p;
-                if (nf == 2) {
-                    const int lo = fixed[0] < fixed[1] ? fixed[0] : fixed[1], hi = fixed[0] < fixed[1] ? fixed[1] : fixed[0];
-                    i = ins0(ins0(i, lo), hi);
-                } else if (nf == 1) {
-                    i = ins0(i, fixed[0]);
-                }
-                for (int f = 0; f < nf; ++f) i |= 1u << fixed[f];
-                const T a = re[at(i)];
-                re[at(i)] = a * cs - im[at(i)] * sn;
-                im[at(i)] = im[at(i)] * cs + a * sn;
-            }
         }
         sync();
     }
@@ -1024,10 +956,6 @@ struct Qms {
                 tb->xs[dir][trg] = (T)shd;
                 tb->steps[dir][trg] = steps;
                 tb->regs[dir][trg] = regs ? 1 : 0;
-                double su, cu;
-                sincos(dir == 0 ? -powr * P->t_pe * P->t_shift : powr * P->t_pe * P->t_shift, &su, &cu);
-                tb->u1c[dir][trg] = (T)cu;
-                tb->u1s[dir][trg] = (T)su;
             }
         }
         const int L = 1 << e;
@@ -1053,14 +981,6 @@ struct Qms {
                 tb->u1v_c[which - 1][v] = (T)ca;
                 tb->u1v_s[which - 1][v] = (T)sa;
             }
-        }
-        for (int idx = threadIdx.x; idx < 2 * 8; idx += blockDim.x) {
-            const int k = idx % 8, dir = idx / 8;
-            const double ph = 2.0 * M_PI / (double)(1u << (1 + k));
-            double sq, cq;
-            sincos(dir == 0 ? ph : -ph, &sq, &cq);
-            tb->qc[dir][k] = (T)cq;
-            tb->qs[dir][k] = (T)sq;
         }
         __syncthreads();
     }

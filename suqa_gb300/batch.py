@@ -226,3 +226,56 @@ def run_tfim_evolution(jobs: list[TfimEvolution], precision: str = "f64"):
         res.append(out[off:off + k].reshape(j.steps + 1, 1 << j.spins).copy())
         off += k
     return res, ms.value
+
+
+def tfim_config3(n_chains: int = 4096, steps: int = 500, seed: int = 2024):
+    """The 4096-chain TFIM workload: spins ~ U{4..10}, energy register ~ U{4..6}
+    qubits, J = 1, h ~ U[0.5, 1.5], beta ~ U[0.2, 2.0], dt = 0.1, window
+    +-s(|J|+|h|), chain k seeded base + k."""
+    rng = np.random.default_rng(seed)
+    return [TfimChain(spins=int(rng.integers(4, 11)), ene_qbits=int(rng.integers(4, 7)), steps=steps,
+                      beta=float(rng.uniform(0.2, 2.0)), h=float(rng.uniform(0.5, 1.5)), thermalization=20,
+                      seed=1 + i) for i in range(n_chains)]
+
+
+def config3_study(n_chains=4096, steps=500, segment=50, f64_chains=128):
+    """Runs the full workload in FP32 as one resumable batch (graph-replayed
+    segments, checkpointed half-way and resumed in a fresh batch), then the
+    first f64_chains chains in FP64, and compares their trajectories; returns
+    the throughput and per-ring-length energies."""
+    import time
+    from . import shard
+    chains = tfim_config3(n_chains, steps)
+    out = {"chains": n_chains, "steps": steps}
+    t0 = time.perf_counter()
+    b = Batch(chains, "f32", segment_steps=segment, use_graph=True, autotune=True)
+    out["f32_setup_s"] = time.perf_counter() - t0
+    ms1 = b.run(steps // 2)
+    blob = b.checkpoint()
+    b.close()
+    b = Batch(chains, "f32", segment_steps=segment, use_graph=True, autotune=True)
+    b.restore(blob)
+    ms2 = b.run(steps - steps // 2)
+    r32 = b.results()
+    b.close()
+    out["f32_device_s"] = (ms1 + ms2) / 1e3
+    out["f32_chain_steps_per_s"] = n_chains * steps / ((ms1 + ms2) / 1e3)
+    out["checkpoint_bytes"] = len(blob)
+    keys, acc = shard.group_sums(chains, r32, lambda c: c.spins)
+    out["f32_energy_by_ring_length"] = shard.averages(keys, acc)
+    sub = chains[:f64_chains]
+    b = Batch(sub, "f64", segment_steps=segment, use_graph=True)
+    ms = b.run(steps)
+    r64 = b.results()
+    b.close()
+    out["f64_chains"] = f64_chains
+    out["f64_chain_steps_per_s"] = f64_chains * steps / (ms / 1e3)
+    out["f64_trajectories_identical_to_f32"] = int(sum(
+        1 for a, c in zip(r32[:f64_chains], r64)
+        if a.accepted == c.accepted and np.array_equal(a.E, c.E) and np.array_equal(a.A, c.A)))
+    return out
+
+
+if __name__ == "__main__":
+    import json
+    print(json.dumps(config3_study()))

@@ -39,3 +39,31 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib, "_lib", None)
     with pytest.raises(RuntimeError):
         _lib.load()
+
+
+def test_batch_entry_points_reject_bad_arguments_before_any_device_call():
+    """Argument checks of the batched entry points run on the host first (no
+    GPU needed): out-of-range rings, a bad precision, empty lists."""
+    from suqa_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("libsq not built")
+    L = _lib.load()
+    ev = (_lib.SqTfimEvolution * 1)()
+    ev[0] = _lib.SqTfimEvolution(13, 2, 1.0, 1.0, 0.1)  # 13 spins: beyond 12
+    ms = ctypes.c_float()
+    buf = (ctypes.c_double * 8)()
+    assert L.sq_tfim_evolve_batch(ev, 1, _lib.SQ_F64, buf, ctypes.byref(ms)) == _lib.SQ_ERR_ARG
+    assert b"ring length" in L.sq_last_error()
+    ev[0] = _lib.SqTfimEvolution(4, 2, 1.0, 1.0, 0.0)  # dt = 0
+    assert L.sq_tfim_evolve_batch(ev, 1, _lib.SQ_F64, buf, ctypes.byref(ms)) == _lib.SQ_ERR_ARG
+    assert L.sq_tfim_evolve_batch(ev, 0, _lib.SQ_F64, buf, ctypes.byref(ms)) == _lib.SQ_ERR_ARG
+    ch = (_lib.SqTfimChain * 1)()
+    ch[0] = _lib.SqTfimChain(4, 4, 10, 0, 1, 100, 1.0, 1.0, 1.0, -8.0, 8.0, 0.1, 1)
+    h = ctypes.c_void_p()
+    opts = _lib.SqBatchOpts(0, 0, 0, 384, 0, 0, 0)  # 384 threads: not a supported CTA size
+    assert L.sq_batch_create(ctypes.byref(h), ch, 1, _lib.SQ_F32, ctypes.byref(opts)) == _lib.SQ_ERR_ARG
+    assert L.sq_batch_create(ctypes.byref(h), ch, 1, 7, None) == _lib.SQ_ERR_ARG  # unknown precision
+    ch[0].spins = 21
+    assert L.sq_batch_create(ctypes.byref(h), ch, 1, _lib.SQ_F32, None) == _lib.SQ_ERR_ARG
+    ch[0].spins, ch[0].ene_qbits = 16, 7  # 24 qubits
+    assert L.sq_batch_create(ctypes.byref(h), ch, 1, _lib.SQ_F32, None) == _lib.SQ_ERR_ARG

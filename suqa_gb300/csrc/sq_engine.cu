@@ -37,6 +37,7 @@ struct HostOp {
     uint32_t shift = 0;
     double c = 0.0, s = 0.0;
     std::vector<double> tab;        // complex pairs (PLIST: cos/sin, W: f1/f2)
+    uint8_t gdefer = 0;             // its scale factor is kept in sq_state::gscale
 };
 
 inline int popc(uint64_t x) { return __builtin_popcountll(x); }
@@ -62,6 +63,12 @@ struct sq_state {
     unsigned int* d_ticket = nullptr;
     double* h_result = nullptr;     // pinned
     int fusion = 1;
+    // global scale: the state is gscale x the stored amplitudes.  Uncontrolled H
+    // and Pauli rotations leave their common factor (1/sqrt 2, cos or sin of the
+    // angle) here instead of multiplying every amplitude, and so do the
+    // renormalisations of measurement and vnormalize; it is applied to memory
+    // (one fused scale) before any read-out and when it drifts far from 1.
+    double gscale = 1.0;
     int nsm = 1;
     int max_grid = 1;
     int kp = 0;                     // default tile size for this state
@@ -205,7 +212,8 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         }
         o.lcm = lcm;
         o.lcv = lcv;
-        if ((h.kind == sqk::OP_HP || h.kind == sqk::OP_PAULI) && lcm == 0u) p.defer++;
+        o.gdefer = h.gdefer;
+        if ((h.kind == sqk::OP_HP || h.kind == sqk::OP_PAULI) && lcm == 0u && !h.gdefer) p.defer++;
         o.lzy = (h.kind == sqk::OP_PAULI) ? lzy : 0u;
         o.cmask = h.cmask;
         o.cval = h.cval;
@@ -324,6 +332,28 @@ int enqueue(sq_state* s, HostOp&& h) {
     return SQ_OK;
 }
 
+// Applies the global scale to memory (as one scale op, fused into the next pass).
+int materialize(sq_state* s) {
+    if (s->gscale == 1.0) return SQ_OK;
+    HostOp h;
+    h.kind = sqk::OP_SCALE;
+    h.s = s->gscale;
+    s->gscale = 1.0;
+    s->pending.push_back(std::move(h));
+    if (s->pending.size() >= 4096) return flush(s);
+    return SQ_OK;
+}
+
+// Multiplies the global scale by f; keeps the stored amplitudes in range (FP32
+// has an 8-bit exponent) by materialising it when it leaves [2^-lim, 2^lim].
+int scale_by(sq_state* s, double f) {
+    s->gscale *= f;
+    const double lim = s->prec == SQ_F64 ? 300.0 : 40.0;
+    const double e = std::fabs(std::log2(std::fabs(s->gscale)));
+    if (e > lim) return materialize(s);
+    return SQ_OK;
+}
+
 int check_q(const sq_state* s, uint32_t q) {
     if (!s) return fail(SQ_ERR_ARG, "null state");
     if (q >= s->n) return fail(SQ_ERR_ARG, "qubit index out of range");
@@ -405,7 +435,8 @@ int sq_state_destroy(sq_state* s) {
 
 int sq_state_ptrs(sq_state* s, void** re, void** im) {
     if (!s) return fail(SQ_ERR_ARG, "null state");
-    int rc = flush(s);
+    int rc = materialize(s);
+    if (!rc) rc = flush(s);
     if (rc) return rc;
     if (re) *re = s->data;
     if (im) *im = (char*)s->data + s->N * s->esz;
@@ -457,7 +488,8 @@ int sq_set_fusion(sq_state* s, int enabled) {
 
 int sq_get_state(sq_state* s, double* re, double* im) {
     if (!s || !re || !im) return fail(SQ_ERR_ARG, "null argument");
-    int rc = flush(s);
+    int rc = materialize(s);
+    if (!rc) rc = flush(s);
     if (rc) return rc;
     if (s->prec == SQ_F64) {
         SQ_CUDA(cudaMemcpyAsync(re, s->data, s->N * 8, cudaMemcpyDeviceToHost, s->stream));
@@ -478,6 +510,7 @@ int sq_get_state(sq_state* s, double* re, double* im) {
 int sq_set_state(sq_state* s, const double* re, const double* im) {
     if (!s || !re || !im) return fail(SQ_ERR_ARG, "null argument");
     s->pending.clear();
+    s->gscale = 1.0;
     if (s->prec == SQ_F64) {
         SQ_CUDA(cudaMemcpyAsync(s->data, re, s->N * 8, cudaMemcpyHostToDevice, s->stream));
         SQ_CUDA(cudaMemcpyAsync((char*)s->data + s->N * 8, im, s->N * 8, cudaMemcpyHostToDevice, s->stream));
@@ -497,6 +530,7 @@ int sq_set_state(sq_state* s, const double* re, const double* im) {
 int sq_upload(sq_state* s, const void* re, const void* im) {
     if (!s || !re || !im) return fail(SQ_ERR_ARG, "null argument");
     s->pending.clear();
+    s->gscale = 1.0;
     const size_t b = s->N * s->esz;
     SQ_CUDA(cudaMemcpyAsync(s->data, re, b, cudaMemcpyHostToDevice, s->stream));
     SQ_CUDA(cudaMemcpyAsync((char*)s->data + b, im, b, cudaMemcpyHostToDevice, s->stream));
@@ -505,7 +539,8 @@ int sq_upload(sq_state* s, const void* re, const void* im) {
 
 int sq_download(sq_state* s, void* re, void* im) {
     if (!s || !re || !im) return fail(SQ_ERR_ARG, "null argument");
-    int rc = flush(s);
+    int rc = materialize(s);
+    if (!rc) rc = flush(s);
     if (rc) return rc;
     const size_t b = s->N * s->esz;
     SQ_CUDA(cudaMemcpyAsync(re, s->data, b, cudaMemcpyDeviceToHost, s->stream));
@@ -517,6 +552,7 @@ int sq_download(sq_state* s, void* re, void* im) {
 int sq_init_state(sq_state* s) {
     if (!s) return fail(SQ_ERR_ARG, "null state");
     s->pending.clear();
+    s->gscale = 1.0;
     SQ_CUDA(cudaMemsetAsync(s->data, 0, 2 * s->N * s->esz, s->stream));
     if (s->prec == SQ_F64) {
         const double one = 1.0;
@@ -533,7 +569,7 @@ int sq_vnorm(sq_state* s, double* norm) {
     if (!s || !norm) return fail(SQ_ERR_ARG, "null argument");
     int rc = flush(s, 2, 0, 0);
     if (rc) return rc;
-    *norm = std::sqrt(s->h_result[0]);
+    *norm = std::sqrt(s->h_result[0]) * std::fabs(s->gscale);
     return SQ_OK;
 }
 
@@ -541,10 +577,8 @@ int sq_vnormalize(sq_state* s) {
     double nrm = 0.0;
     int rc = sq_vnorm(s, &nrm);
     if (rc) return rc;
-    HostOp h;
-    h.kind = sqk::OP_SCALE;
-    h.s = 1. / nrm;
-    return enqueue(s, std::move(h));
+    s->stats.gates++;
+    return scale_by(s, 1. / nrm);  // src/suqa.cu:105: multiply by 1./norm
 }
 
 // A global control mask may contain the gate's own qubits (the reference's QSA
@@ -572,7 +606,11 @@ static int pair_op(sq_state* s, uint8_t kind, uint32_t q, uint64_t gc) {
     h.cval = g;
     h.skm = g;
     h.skv = g;
-    return enqueue(s, std::move(h));
+    const bool defer = kind == sqk::OP_HP && g == 0;  // uncontrolled H: 1/sqrt(2) into the global scale
+    h.gdefer = defer ? 1 : 0;
+    rc = enqueue(s, std::move(h));
+    if (rc || !defer) return rc;
+    return scale_by(s, 0.7071067811865475);
 }
 
 int sq_apply_x(sq_state* s, uint32_t q, uint64_t gc) { return pair_op(s, sqk::OP_SWAPP, q, gc); }
@@ -780,7 +818,14 @@ int sq_apply_pauli_rotation(sq_state* s, uint32_t k, const uint32_t* qubits, con
     h.skm = gc;
     h.skv = gc;
     sincos(phase, &h.s, &h.c);
-    return enqueue(s, std::move(h));
+    // uncontrolled: the larger of cos and sin into the global scale, the kernel
+    // stores a + (s/c) iP a (or (c/s) a + iP a); the same choice as the kernel's
+    const bool defer = gc == 0;
+    const double f = std::fabs(h.c) >= std::fabs(h.s) ? h.c : h.s;
+    h.gdefer = defer ? 1 : 0;
+    rc = enqueue(s, std::move(h));
+    if (rc || !defer) return rc;
+    return scale_by(s, f);
 }
 
 int sq_apply_qms_w(sq_state* s, uint32_t q_acc, uint64_t mask_enew, uint32_t shift, uint32_t E_old,
@@ -821,17 +866,21 @@ int sq_measure_qbit(sq_state* s, uint32_t q, double r, uint32_t* c) {
     const uint64_t b = 1ull << q;
     rc = flush(s, 1, b, 0);
     if (rc) return rc;
-    const double p0 = s->h_result[0], p1 = s->h_result[1];
-    // src/suqa.cu:690-695: c = r < prob1; keep branch c; multiply by 1./norm
+    const double g2 = s->gscale * s->gscale;
+    const double p0 = s->h_result[0] * g2, p1 = s->h_result[1] * g2;
+    // src/suqa.cu:690-695: c = r < prob1; keep branch c; multiply by 1./norm (kept
+    // in the global scale; the pass only zeroes the other branch)
     const uint32_t cc = (uint32_t)(r < p1);
     const double keep = cc ? p1 : p0;
     HostOp h;
     h.kind = sqk::OP_COLLAPSE;
     h.cmask = b;
     h.cval = cc ? b : 0ull;
-    h.s = 1. / std::sqrt(keep);
+    h.s = 1.0;
     *c = cc;
-    return enqueue(s, std::move(h));
+    rc = enqueue(s, std::move(h));
+    if (rc) return rc;
+    return scale_by(s, 1. / std::sqrt(keep));
 }
 
 int sq_prob_filter(sq_state* s, uint64_t mask_qs, uint64_t mask, double* prob) {
@@ -840,7 +889,7 @@ int sq_prob_filter(sq_state* s, uint64_t mask_qs, uint64_t mask, double* prob) {
     if (!prob) return fail(SQ_ERR_ARG, "null output");
     rc = flush(s, 2, mask_qs, mask);
     if (rc) return rc;
-    *prob = s->h_result[0];
+    *prob = s->h_result[0] * s->gscale * s->gscale;
     return SQ_OK;
 }
 

@@ -49,7 +49,7 @@ struct Op {
     uint32_t lcm, lcv;     // tile-local control condition
     uint32_t lzy;          // tile-local Y|Z mask (Pauli signs)
     uint32_t shift, tab;   // PLIST/W: shift and table offset (in complex entries)
-    uint32_t pad;
+    uint32_t gdefer;       // H / rotation whose scale factor the host keeps in the state's global scale
     uint64_t cmask, cval;  // global element condition (diagonal slow paths)
     uint64_t ocm, ocv;     // part of the condition on qubits outside the tile
     uint64_t zy;           // Pauli: global Y|Z mask; PLIST/W: extraction mask
@@ -261,14 +261,14 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                     }
                 } else if (kind == OP_HP) {
                     // include/suqa_cpu.hpp:150-206
-                    if (lcm == 0u && p.defer) {
+                    if (lcm == 0u && (op.gdefer || p.defer)) {
                         for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
                             const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
                             const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
                             sre[t0] = a0r + a1r; sim[t0] = a0i + a1i;
                             sre[t1] = a0r - a1r; sim[t1] = a0i - a1i;
                         }
-                        sigma *= 0.7071067811865475;
+                        if (!op.gdefer) sigma *= 0.7071067811865475;
                     } else {
                         const T h = (T)0.7071067811865475;
                         for (uint32_t u = threadIdx.x; u < npair; u += blockDim.x) {
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                     const int tpar = parity64(base & op.zy);
                     const uint32_t lzy = op.lzy;
                     const int ny = op.ny, fz = op.fz;
-                    if (lcm == 0u && p.defer) {
+                    if (lcm == 0u && (op.gdefer || p.defer)) {
                         const bool cbig = fabs(op.c) >= fabs(op.s);
                         const double ud = cbig ? op.s / op.c : op.c / op.s;
                         const T up = (T)ud, un = (T)(-ud);
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                             rot_deferred<T>(a1r, a1i, a0r, a0i, k1, up, un, cbig, r1, i1);
                             sre[t0] = r0; sim[t0] = i0; sre[t1] = r1; sim[t1] = i1;
                         }
-                        sigma *= cbig ? op.c : op.s;
+                        if (!op.gdefer) sigma *= cbig ? op.c : op.s;
                     } else {
                         for (uint32_t u = threadIdx.x; u < npair; u += blockDim.x) {
                             const uint32_t t0 = deposit_zeros(u, sel) | lcv, t1 = t0 ^ lf;
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
             } else if (kind == OP_PAULI) {  // all-Z string: diagonal c + i s (-1)^parity
                 const int tpar = parity64(base & op.zy);
                 const uint32_t lzy = op.lzy;
-                if (lcm == 0u && p.defer) {
+                if (lcm == 0u && (op.gdefer || p.defer)) {
                     const bool cbig = fabs(op.c) >= fabs(op.s);
                     const double ud = cbig ? op.s / op.c : op.c / op.s;
                     const T up = (T)ud, un = (T)(-ud);
@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                         rot_deferred<T>(ar, ai, ar, ai, (1 + 2 * (tpar ^ (__popc(t & lzy) & 1))) & 3, up, un, cbig, r, i);
                         sre[t] = r; sim[t] = i;
                     }
-                    sigma *= cbig ? op.c : op.s;
+                    if (!op.gdefer) sigma *= cbig ? op.c : op.s;
                 } else {
                     const uint32_t nsel = TS >> __popc(lcm);
                     for (uint32_t u = threadIdx.x; u < nsel; u += blockDim.x) {
@@ -371,10 +371,16 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                         sim[t] = ar * cy + ai * cx;
                     } else if (kind == OP_COLLAPSE) {
                         // src/suqa.cu:664-696: zero the discarded branch, rescale everything
-                        // (a zero state gives 0 * inf = NaN everywhere, like the reference)
+                        // (a zero state gives 0 * inf = NaN everywhere, like the reference);
+                        // a scale of exactly 1 (kept by the host's global scale) is skipped
                         const bool keep = (g & op.cmask) == op.cval;
-                        sre[t] = (keep ? ar : (T)0) * s;
-                        sim[t] = (keep ? ai : (T)0) * s;
+                        if (op.s == 1.0) {
+                            sre[t] = keep ? ar : (T)0;
+                            sim[t] = keep ? ai : (T)0;
+                        } else {
+                            sre[t] = (keep ? ar : (T)0) * s;
+                            sim[t] = (keep ? ai : (T)0) * s;
+                        }
                     } else {  // OP_SCALE
                         sre[t] = ar * s;
                         sim[t] = ai * s;

@@ -276,6 +276,27 @@ def config3_study(n_chains=4096, steps=500, segment=50, f64_chains=128):
     return out
 
 
+def evolution_study(n_rings=2048, steps=50, seed=3):
+    """Throughput of the batched evolution: rings of 8-12 spins (h ~ U[0.5, 1.5],
+    dt = 0.1) evolved `steps` Trotter steps with every step's probabilities
+    recorded, in FP32 and FP64."""
+    rng = np.random.default_rng(seed)
+    jobs = [TfimEvolution(spins=int(rng.integers(8, 13)), steps=steps, dt=0.1, h=float(rng.uniform(0.5, 1.5)))
+            for _ in range(n_rings)]
+    out = {"rings": n_rings, "steps": steps, "spins": "8-12"}
+    for prec in ("f32", "f64"):
+        rows, ms = run_tfim_evolution(jobs, prec)
+        amps = sum((1 << j.spins) * j.steps for j in jobs)
+        out[prec] = {"device_ms": ms, "ring_steps_per_s": n_rings * steps / (ms / 1e3),
+                     "amplitude_steps_per_s": amps / (ms / 1e3),
+                     "probability_bytes": int(sum(r.nbytes for r in rows))}
+    return out
+
+
 if __name__ == "__main__":
+    import argparse
     import json
-    print(json.dumps(config3_study()))
+    ap = argparse.ArgumentParser(description="batched-chain studies")
+    ap.add_argument("--evolution", action="store_true", help="time the batched evolution instead")
+    a = ap.parse_args()
+    print(json.dumps(evolution_study() if a.evolution else config3_study()))

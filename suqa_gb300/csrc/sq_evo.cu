@@ -52,7 +52,7 @@ __host__ __device__ inline void evo_geometry(int s, int* m, int* G) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_evo(const EvoJob* __restrict__ jobs, const int* __restrict__ ids,
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 1 : 3) k_evo(const EvoJob* __restrict__ jobs, const int* __restrict__ ids,
                                              double* __restrict__ probs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ Shared sh;

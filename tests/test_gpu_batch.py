@@ -231,3 +231,26 @@ def test_sharded_batches_sum_to_the_whole():
             acc[pos[k]] += row
     assert np.allclose(acc, whole, rtol=1e-15, atol=0)
     assert shard.run_sharded(chains, "f32", key=key, rank=0, world=1) == shard.averages(keys, whole)
+
+
+def test_uneven_lengths_and_fp64_autotune():
+    """Chains of different lengths (including zero steps) in one resumable FP64
+    batch with autotuned CTA sizes: every chain stops at its own length and the
+    results equal the one-shot run."""
+    from suqa_gb300.batch import Batch, TfimChain, run_tfim_batch
+    chains = _mixed(20, 6, seed=21)
+    for i, c in enumerate(chains):
+        c.steps = (0, 3, 7)[i % 3]
+    ref, _ = run_tfim_batch(chains, "f64")
+    b = Batch(chains, "f64", autotune=True, segment_steps=2, use_graph=True)
+    assert all(p["threads"] in (128, 256) for p in b.plan())
+    b.run(3)
+    assert list(b.progress()) == [min(c.steps, 3) for c in chains]
+    b.run(10)
+    assert list(b.progress()) == [c.steps for c in chains]
+    _same(ref, b.results())
+    for i, c in enumerate(chains):
+        if c.steps == 0:
+            with pytest.raises(Exception):
+                b.state(i)  # a chain that never ran has no state yet
+    b.close()

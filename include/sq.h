@@ -245,6 +245,42 @@ typedef struct sq_tfim_evolution {
 int sq_tfim_evolve_batch(const sq_tfim_evolution* jobs, uint32_t njobs, int precision, double* probs,
                          float* kernel_ms);
 
+/* --- batched Szegedy-walk annealing (QSA) on Ising rings ---
+ * Generalises the reference's triangle-only QSA (include/qsa.cuh:616-756 walk,
+ * src/qsa.cu:159-268 annealing loop) to a ring of s spins with integer couplings
+ * and no field, H(x) = -sum_i J_i s_i s_{i+1 mod s}, with the rotation and
+ * reflection of the reference's commented general form (qsa.cuh:372-418).
+ * Each walk anneals beta_k = (k+1) beta / stages, k < stages, with
+ * steps_per_stage walk steps at each; a step draws the move (qsa::draw_C with
+ * weights 1/s), runs the walk-phase estimation with a phase_qbits register and
+ * reads it (phase_qbits draws); a nonzero value restarts the anneal
+ * (qsa.cu:199-205).  A completed anneal reads the s spins (s draws).  The
+ * energy-difference register is exact for integer couplings and is applied in
+ * closed form.  p0_trace (optional) receives, walk after walk, one slot per
+ * allowed step (max_steps, or 8 x stages x steps_per_stage when 0): the
+ * probability of the zero walk phase at each step run. */
+typedef struct sq_qsa_walk {
+    uint32_t spins;           /* ring length, 2..12 */
+    uint32_t phase_qbits;     /* walk-phase register, 1..6 qubits */
+    uint32_t stages;          /* annealing stages */
+    uint32_t steps_per_stage; /* walk steps at each temperature */
+    uint32_t max_steps;       /* cap on steps over all attempts (0: 8 x stages x steps_per_stage) */
+    int32_t J[12];            /* bond couplings, bond i joins spins i and i+1 mod s; -8..8 */
+    uint32_t pad;
+    double beta;              /* final inverse temperature */
+    uint64_t seed;            /* PCG32 seed (pcg32::seed(seed, 1)) */
+} sq_qsa_walk;
+typedef struct sq_qsa_walk_result {
+    uint32_t done;     /* 1: the anneal completed and the spins were read; 0: capped */
+    uint32_t restarts; /* attempts abandoned on a nonzero walk phase */
+    uint32_t steps;    /* walk steps run over all attempts */
+    uint32_t readout;  /* spin configuration read (bit i = spin i) */
+    double E, absM;    /* energy and |magnetisation| of the readout */
+    double last_p0;    /* probability of the zero walk phase at the last step */
+} sq_qsa_walk_result;
+int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int precision, sq_qsa_walk_result* results,
+                      double* p0_trace, float* kernel_ms);
+
 /* --- learned warm start: a small MLP with BF16 weights/activations, FP32 sums ---
  * No reference counterpart.  in -> `layers` hidden layers of `hidden` GELU units
  * -> out.  Parameters are one flat FP32 array (W_l row-major, then b_l, layer by

@@ -46,6 +46,17 @@ class SqTfimEvolution(C.Structure):
                 ("dt", C.c_double), ("warm_start", C.c_uint32), ("pad", C.c_uint32), ("ry", C.c_double * 20)]
 
 
+class SqQsaWalk(C.Structure):
+    _fields_ = [("spins", C.c_uint32), ("phase_qbits", C.c_uint32), ("stages", C.c_uint32),
+                ("steps_per_stage", C.c_uint32), ("max_steps", C.c_uint32), ("J", C.c_int32 * 12),
+                ("pad", C.c_uint32), ("beta", C.c_double), ("seed", C.c_uint64)]
+
+
+class SqQsaWalkResult(C.Structure):
+    _fields_ = [("done", C.c_uint32), ("restarts", C.c_uint32), ("steps", C.c_uint32), ("readout", C.c_uint32),
+                ("E", C.c_double), ("absM", C.c_double), ("last_p0", C.c_double)]
+
+
 class SqBatchOpts(C.Structure):
     _fields_ = [("segment_steps", C.c_uint32), ("use_graph", C.c_uint32), ("autotune", C.c_uint32),
                 ("threads", C.c_uint32), ("l2_budget_bytes", C.c_uint64), ("cta_qubits", C.c_uint32),
@@ -109,6 +120,8 @@ _SIGS = {
     "sq_batch_plan": (C.c_int, [C.c_void_p, C.POINTER(SqBatchClass), C.c_uint32, C.POINTER(C.c_uint32)]),
     "sq_tfim_evolve_batch": (C.c_int, [C.POINTER(SqTfimEvolution), C.c_uint32, C.c_int, C.c_void_p,
                                        C.POINTER(C.c_float)]),
+    "sq_qsa_walk_batch": (C.c_int, [C.POINTER(SqQsaWalk), C.c_uint32, C.c_int, C.POINTER(SqQsaWalkResult),
+                                    C.c_void_p, C.POINTER(C.c_float)]),
     "sq_mlp_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64]),
     "sq_mlp_destroy": (C.c_int, [C.c_void_p]),
     "sq_mlp_num_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),

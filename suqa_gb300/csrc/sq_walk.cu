@@ -1,0 +1,636 @@
+// Batched Szegedy-walk annealing (QSA) on Ising rings with integer couplings
+// and no field: the reference's walk (include/qsa.cuh:616-756, driver loop
+// src/qsa.cu:159-268) in the general form of its own commented-out rotation and
+// reflection (qsa.cuh:372-418), for many walks at once.
+//
+// Registers per walk: system x and copy x~ (s qubits each), the acceptance
+// qubit, the q-qubit walk-phase register and an energy-difference register.  The
+// ring's Hamiltonian is diagonal with integer spectrum, so phase estimation of
+// the energy difference is exact and every "estimate, act on the level,
+// un-estimate" block equals its action applied directly as a function of
+// dE = H(x~) - H(x): the energy register is never stored.  The walk-phase
+// register's branches are independent: branch k carries W^k psi, so a walk step
+// needs v_k = W^k psi for k < L = 2^q, the overlaps g_k = <psi, v_k> (which give
+// the register's readout distribution after the inverse QFT) and sum_k v_k
+// (the state after reading zero).
+//
+// State: real amplitudes psi[acc][d][x], d = x XOR x~, 2^(2s+1) per walk.  For
+// the step's move C the operator W (L1 H_C R S0 R^T H_C L1 H_C R S0 R^T H_C)
+// only ever mixes the 16 amplitudes
+//     x in {x0, x0^d', x0^e_C, x0^d'^e_C},  d in {d', d'^e_C},  acc in {0, 1}
+// (d' = d without bit C), so one thread keeps such an orbit in registers and
+// applies W L-1 times without touching memory.  Orbits with d' = 0 have 8
+// amplitudes; they run duplicated in the 16 registers and count half.
+//
+// Per step (one launch of k_walk_step and one of k_walk_measure):
+//   k_walk_step     every orbit: load psi (scaled by the last normalisation, or
+//                   the initial state), L-1 applications of W, per-k warp sums
+//                   of <psi, v_k> accumulated in FP64, store sum_k v_k;
+//   k_walk_measure  per walk: g_k, P(m), the register readout with q draws,
+//                   restart on a nonzero value, the next move and temperature.
+// k_walk_readout reads the spins of every completed walk.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "sq.h"
+
+namespace sqi {
+void set_error(const char* msg);
+}
+
+namespace sqw {
+
+constexpr int kThreads = 256;
+constexpr int kOrbitsPerThread = 4;
+constexpr int kOrbitsPerCta = kThreads * kOrbitsPerThread;
+constexpr int kMaxL = 64;
+constexpr int kMaxJ = 8;
+constexpr int kMaxD = 2 * 12 * kMaxJ;  // largest |dE|
+
+struct WalkDev {
+    int s, q, stages, per;
+    uint32_t nominal, cap;
+    double beta;
+    uint64_t seed;
+    uint64_t state_off;  // first element of psi[acc][d][x]
+    uint64_t trace_off;  // first p0 trace slot
+    uint32_t e_off;      // first entry of the energy table (2^s int32)
+    uint32_t cta0, ncta; // CTAs of the walk in the step grid
+    int dmax;            // largest |dE| of the ring
+};
+
+struct WalkRec {
+    uint64_t rng_state, rng_inc;
+    double beta_k;   // inverse temperature of the next step
+    double scale;    // factor of the stored state
+    double last_p0;  // P(zero walk phase) at the last step
+    uint32_t C;      // move of the next step
+    uint32_t fresh;  // the next step starts from the initial state
+    uint32_t att;    // completed steps of the current attempt
+    uint32_t total, restarts;
+    uint32_t status; // 0 running, 1 capped, 2 completed, 3 read out
+    uint32_t readout, pad;
+};
+
+__host__ __device__ inline uint32_t ins0(uint32_t p, int b) {
+    return ((p >> b) << (b + 1)) | (p & ((1u << b) - 1u));
+}
+
+__host__ __device__ inline uint32_t norbits(int s) {
+    return (1u << (s - 1)) + ((1u << (s - 1)) - 1u) * (1u << (s - 2));
+}
+
+__device__ __forceinline__ uint32_t pcg_next(uint64_t& st, uint64_t inc) {
+    const uint64_t old = st;
+    st = old * 6364136223846793005ULL + inc;
+    const uint32_t x = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    const uint32_t rot = (uint32_t)(old >> 59u);
+    return (x >> rot) | (x << ((0u - rot) & 31u));
+}
+
+__device__ __forceinline__ double pcg_doub(uint64_t& st, uint64_t inc) {
+    const uint64_t bits = ((uint64_t)pcg_next(st, inc) << 20) | 0x3ff0000000000000ULL;
+    return __longlong_as_double((long long)bits) - 1.0;
+}
+
+// qsa::draw_C (qsa.cuh:334-343) with weight sums (i+1)/s
+__device__ __forceinline__ uint32_t draw_move(uint64_t& st, uint64_t inc, int s) {
+    const double u = pcg_doub(st, inc);
+    for (int i = 0; i < s; ++i)
+        if (u < (double)(i + 1) / (double)s) return (uint32_t)i;
+    return (uint32_t)s;
+}
+
+// register slot of orbit coordinates (a: x ^= d', b: x ^= e_C, c: d ^= e_C, acc)
+#define SLOT(a, b, c, acc) (((a) << 3) | ((b) << 2) | ((c) << 1) | (acc))
+
+template <typename T>
+struct Orbit {
+    T v[16];
+    T e[8], r[8], he[8], hr[8];  // rotation per position (a, b, c); he/hr carry the 1/2 of two Hadamards
+    uint32_t zmask;              // positions with dE = 0
+
+    __device__ __forceinline__ void lam() {
+#pragma unroll
+        for (int p = 0; p < 8; ++p)
+            if ((zmask >> p) & 1u) v[2 * p] = -v[2 * p];
+    }
+    // Hadamard on copy bit C, unnormalised: the copy bit is b ^ c
+    __device__ __forceinline__ void hc() {
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+                for (int acc = 0; acc < 2; ++acc) {
+                    const T A = v[SLOT(a, b, 0, acc)], B = v[SLOT(a, b, 1, acc)];
+                    if (b == 0) {
+                        v[SLOT(a, b, 0, acc)] = A + B;
+                        v[SLOT(a, b, 1, acc)] = A - B;
+                    } else {
+                        v[SLOT(a, b, 1, acc)] = A + B;
+                        v[SLOT(a, b, 0, acc)] = B - A;
+                    }
+                }
+    }
+    // ptp(Y, -acos e) on acc = [[e, -r], [r, e]], times 1/2
+    __device__ __forceinline__ void rot_half() {
+#pragma unroll
+        for (int p = 0; p < 8; ++p) {
+            const T p0 = v[2 * p], p1 = v[2 * p + 1];
+            v[2 * p] = he[p] * p0 - hr[p] * p1;
+            v[2 * p + 1] = hr[p] * p0 + he[p] * p1;
+        }
+    }
+    __device__ __forceinline__ void rot_inv() {
+#pragma unroll
+        for (int p = 0; p < 8; ++p) {
+            const T p0 = v[2 * p], p1 = v[2 * p + 1];
+            v[2 * p] = e[p] * p0 + r[p] * p1;
+            v[2 * p + 1] = e[p] * p1 - r[p] * p0;
+        }
+    }
+    // swap x <-> x~ on acc = 0: (a, b, c) <-> (a ^ 1, b ^ c, c)
+    __device__ __forceinline__ void sw0() {
+        T t;
+        t = v[SLOT(0, 0, 0, 0)]; v[SLOT(0, 0, 0, 0)] = v[SLOT(1, 0, 0, 0)]; v[SLOT(1, 0, 0, 0)] = t;
+        t = v[SLOT(0, 1, 0, 0)]; v[SLOT(0, 1, 0, 0)] = v[SLOT(1, 1, 0, 0)]; v[SLOT(1, 1, 0, 0)] = t;
+        t = v[SLOT(0, 0, 1, 0)]; v[SLOT(0, 0, 1, 0)] = v[SLOT(1, 1, 1, 0)]; v[SLOT(1, 1, 1, 0)] = t;
+        t = v[SLOT(0, 1, 1, 0)]; v[SLOT(0, 1, 1, 0)] = v[SLOT(1, 0, 1, 0)]; v[SLOT(1, 0, 1, 0)] = t;
+    }
+    __device__ __forceinline__ void walk() {
+        lam(); hc(); rot_half(); sw0(); rot_inv(); hc();
+        lam(); hc(); rot_half(); sw0(); rot_inv(); hc();
+    }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 8 ? 1 : 2)
+k_walk_step(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk, const WalkRec* __restrict__ recs,
+            const int* __restrict__ energies, T* __restrict__ states, double* __restrict__ partial) {
+    const int w = cta_walk[blockIdx.x];
+    const WalkDev& W = walks[w];
+    const WalkRec& R = recs[w];
+    if (R.status != 0) return;  // uniform over the CTA
+    __shared__ double red[kThreads / 32][kMaxL];
+    __shared__ T tab_e[kMaxD + 1], tab_r[kMaxD + 1];
+    const int s = W.s, C = (int)R.C, L = 1 << W.q;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < (kThreads / 32) * kMaxL; i += blockDim.x) (&red[0][0])[i] = 0.0;
+    for (int k = threadIdx.x; k <= W.dmax; k += blockDim.x) {
+        double e = 1.0, r = 0.0;
+        if (k > 0) {
+            e = exp(-0.5 * R.beta_k * (double)k);
+            r = sqrt(1.0 - e * e);
+        }
+        tab_e[k] = (T)e;
+        tab_r[k] = (T)r;
+    }
+    __syncthreads();
+    const uint32_t N = 1u << s;
+    const uint64_t NN = (uint64_t)N * N;
+    const uint32_t norb = norbits(s);
+    const uint32_t eC = 1u << C;
+    const int* E = energies + W.e_off;
+    T* st = states + W.state_off;
+    const bool fresh = R.fresh != 0;
+    const T scale = (T)R.scale;
+    const T init = (T)(1.0 / sqrt((double)N));
+    const uint32_t first = (blockIdx.x - W.cta0) * (uint32_t)kOrbitsPerCta;
+    for (int it = 0; it < kOrbitsPerThread; ++it) {
+        const uint32_t o = first + (uint32_t)(it * kThreads) + threadIdx.x;
+        const bool active = o < norb;
+        if (!__any_sync(0xffffffffu, active)) continue;  // warp-uniform
+        Orbit<T> ob;
+        uint32_t dp = 0, x0 = 0;
+        bool single = true;
+        if (active) {
+            const uint32_t nb = 1u << (s - 1);
+            if (o < nb) {
+                x0 = ins0(o, C);
+            } else {
+                single = false;
+                const uint32_t o2 = o - nb;
+                const uint32_t di = 1u + (o2 >> (s - 2)), ri = o2 & ((1u << (s - 2)) - 1u);
+                dp = ins0(di, C);
+                const int p = __ffs((int)dp) - 1;
+                x0 = ins0(ins0(ri, min(p, C)), max(p, C));
+            }
+        }
+        ob.zmask = 0;
+#pragma unroll
+        for (int pos = 0; pos < 8; ++pos) {
+            const int a = pos >> 2, b = (pos >> 1) & 1, c = pos & 1;
+            const uint32_t x = x0 ^ (a ? dp : 0u) ^ (b ? eC : 0u);
+            const uint32_t d = dp ^ (c ? eC : 0u);
+            int dE = 0;
+            if (active) dE = E[x ^ d] - E[x];
+            const int k = dE > 0 ? dE : 0;
+            ob.e[pos] = tab_e[k];
+            ob.r[pos] = tab_r[k];
+            ob.he[pos] = (T)0.5 * ob.e[pos];
+            ob.hr[pos] = (T)0.5 * ob.r[pos];
+            if (dE == 0) ob.zmask |= 1u << pos;
+#pragma unroll
+            for (int acc = 0; acc < 2; ++acc) {
+                T val = (T)0;
+                if (active) {
+                    if (fresh) {
+                        val = (single && c == 0 && acc == 0) ? init : (T)0;
+                    } else if (!(single && a == 1)) {
+                        val = st[(uint64_t)acc * NN + (uint64_t)d * N + x] * scale;
+                    }
+                }
+                ob.v[SLOT(a, b, c, acc)] = val;
+            }
+        }
+        if (single) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) ob.v[8 + j] = ob.v[j];
+        }
+        T psi[16], S[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            psi[j] = ob.v[j];
+            S[j] = (T)0;
+        }
+        const T wgt = single ? (T)0.5 : (T)1;
+        for (int k = 0; k < L; ++k) {
+            T dot = (T)0;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                dot += psi[j] * ob.v[j];
+                S[j] += ob.v[j];
+            }
+            dot *= wgt;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, off);
+            if (lane == 0) red[warp][k] += (double)dot;
+            if (k < L - 1) ob.walk();
+        }
+        if (active) {
+#pragma unroll
+            for (int pos = 0; pos < 8; ++pos) {
+                const int a = pos >> 2, b = (pos >> 1) & 1, c = pos & 1;
+                if (single && a == 1) continue;
+                const uint32_t x = x0 ^ (a ? dp : 0u) ^ (b ? eC : 0u);
+                const uint32_t d = dp ^ (c ? eC : 0u);
+#pragma unroll
+                for (int acc = 0; acc < 2; ++acc) st[(uint64_t)acc * NN + (uint64_t)d * N + x] = S[SLOT(a, b, c, acc)];
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < L) {
+        double sum = 0.0;
+        for (int wp = 0; wp < kThreads / 32; ++wp) sum += red[wp][threadIdx.x];
+        partial[(uint64_t)blockIdx.x * kMaxL + threadIdx.x] = sum;
+    }
+}
+
+// One CTA of kMaxL threads per walk.
+__global__ void k_walk_measure(const WalkDev* __restrict__ walks, WalkRec* __restrict__ recs,
+                               const double* __restrict__ partial, const double* __restrict__ cos64,
+                               double* __restrict__ trace, unsigned int* __restrict__ running) {
+    const int w = blockIdx.x;
+    const WalkDev& W = walks[w];
+    WalkRec& R = recs[w];
+    if (R.status != 0) return;
+    __shared__ double g[kMaxL], P[kMaxL];
+    __shared__ double n2;
+    const int L = 1 << W.q;
+    const int t = threadIdx.x;
+    if (t < L) {
+        double sum = 0.0;
+        for (uint32_t c = 0; c < W.ncta; ++c) sum += partial[(uint64_t)(W.cta0 + c) * kMaxL + t];
+        g[t] = sum;
+    }
+    __syncthreads();
+    if (t < L) {
+        double acc = 0.0;
+        const int stride = kMaxL / L;
+        for (int j = 1; j < L; ++j) acc += (double)(L - j) * g[j] * cos64[((t * j) % L) * stride];
+        P[t] = ((double)L * g[0] + 2.0 * acc) / ((double)L * L);
+        if (t == 0) {
+            double a2 = 0.0;
+            for (int j = 1; j < L; ++j) a2 += (double)(L - j) * g[j];
+            n2 = (double)L * g[0] + 2.0 * a2;
+        }
+    }
+    __syncthreads();
+    if (t != 0) return;
+    uint64_t rs = R.rng_state;
+    const uint64_t ri = R.rng_inc;
+    // walk-phase readout, qubit by qubit (c = r < p1)
+    uint32_t m = 0;
+    for (int j = 0; j < W.q; ++j) {
+        const double r = pcg_doub(rs, ri);
+        double num = 0.0, den = 0.0;
+        const uint32_t lowmask = (1u << j) - 1u;
+        for (int v = 0; v < L; ++v) {
+            if (((uint32_t)v & lowmask) != m) continue;
+            den += P[v];
+            if ((v >> j) & 1) num += P[v];
+        }
+        const double p1 = den > 0.0 ? num / den : 0.0;
+        if (r < p1) m |= 1u << j;
+    }
+    double ptot = 0.0;
+    for (int v = 0; v < L; ++v) ptot += P[v];
+    const double p0 = ptot > 0.0 ? P[0] / ptot : 0.0;
+    if (trace) trace[W.trace_off + R.total] = p0;
+    R.last_p0 = p0;
+    R.total += 1;
+    if (m == 0) {
+        R.scale = 1.0 / sqrt(n2);
+        R.fresh = 0;
+        R.att += 1;
+        if (R.att == W.nominal) R.status = 2;
+    } else {
+        R.restarts += 1;
+        R.fresh = 1;
+        R.att = 0;
+        R.scale = 1.0;
+    }
+    if (R.status == 0 && R.total >= W.cap) R.status = 1;
+    if (R.status == 0) {
+        R.C = draw_move(rs, ri, W.s);
+        R.beta_k = (double)(R.att / (uint32_t)W.per + 1) * W.beta / (double)W.stages;
+    } else {
+        atomicSub(running, 1u);
+    }
+    R.rng_state = rs;
+}
+
+__global__ void k_walk_init(const WalkDev* __restrict__ walks, WalkRec* __restrict__ recs, int n) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= n) return;
+    const WalkDev& W = walks[w];
+    WalkRec R;
+    // pcg32::seed(initstate, initseq = 1)
+    R.rng_state = 0;
+    R.rng_inc = (1ull << 1u) | 1u;
+    pcg_next(R.rng_state, R.rng_inc);
+    R.rng_state += W.seed;
+    pcg_next(R.rng_state, R.rng_inc);
+    R.C = draw_move(R.rng_state, R.rng_inc, W.s);
+    R.beta_k = W.beta / (double)W.stages;
+    R.scale = 1.0;
+    R.last_p0 = 0.0;
+    R.fresh = 1;
+    R.att = 0;
+    R.total = 0;
+    R.restarts = 0;
+    R.status = 0;
+    R.readout = 0;
+    R.pad = 0;
+    recs[w] = R;
+}
+
+// Spin readout of completed walks: P(x) = sum over (acc, d) of psi^2, then the
+// s spins measured one by one.  One CTA per walk.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_walk_readout(const WalkDev* __restrict__ walks, WalkRec* __restrict__ recs,
+                                                       const T* __restrict__ states) {
+    const int w = blockIdx.x;
+    const WalkDev& W = walks[w];
+    WalkRec& R = recs[w];
+    if (R.status != 2) return;
+    extern __shared__ double px[];
+    const uint32_t N = 1u << W.s;
+    const T* st = states + W.state_off;
+    for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
+        double acc = 0.0;
+        for (uint32_t row = 0; row < 2 * N; ++row) {
+            const double v = (double)st[(uint64_t)row * N + x];
+            acc += v * v;
+        }
+        px[x] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    uint64_t rs = R.rng_state;
+    const uint64_t ri = R.rng_inc;
+    uint32_t m = 0;
+    for (int j = 0; j < W.s; ++j) {
+        double r = 0.0;
+        if (lane == 0) r = pcg_doub(rs, ri);
+        const uint32_t lowmask = (1u << j) - 1u;
+        double num = 0.0, den = 0.0;
+        for (uint32_t x = lane; x < N; x += 32) {
+            if ((x & lowmask) != m) continue;
+            den += px[x];
+            if ((x >> j) & 1u) num += px[x];
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            num += __shfl_xor_sync(0xffffffffu, num, off);
+            den += __shfl_xor_sync(0xffffffffu, den, off);
+        }
+        int c = 0;
+        if (lane == 0) c = r < (den > 0.0 ? num / den : 0.0) ? 1 : 0;
+        c = __shfl_sync(0xffffffffu, c, 0);
+        m |= (uint32_t)c << j;
+    }
+    if (lane == 0) {
+        R.readout = m;
+        R.status = 3;
+        R.rng_state = rs;
+    }
+}
+
+}  // namespace sqw
+
+namespace {
+int wfail(int code, const std::string& m) {
+    sqi::set_error(m.c_str());
+    return code;
+}
+}  // namespace
+
+extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int precision,
+                                 sq_qsa_walk_result* results, double* p0_trace, float* kernel_ms) {
+    using namespace sqw;
+    if (kernel_ms) *kernel_ms = 0.f;
+    if (!walks || nwalks == 0 || !results) return wfail(SQ_ERR_ARG, "null or empty walk list");
+    if (precision != SQ_F64 && precision != SQ_F32) return wfail(SQ_ERR_ARG, "unknown precision");
+    const size_t esz = precision == SQ_F64 ? 8 : 4;
+    std::vector<WalkDev> wd(nwalks);
+    std::vector<int> energies;
+    std::vector<int> cta_walk;
+    uint64_t state_elems = 0, trace_len = 0;
+    uint32_t max_cap = 0;
+    for (uint32_t i = 0; i < nwalks; ++i) {
+        const sq_qsa_walk& a = walks[i];
+        if (a.spins < 2 || a.spins > 12) return wfail(SQ_ERR_ARG, "ring length out of range (2..12 spins)");
+        if (a.phase_qbits < 1 || a.phase_qbits > 6) return wfail(SQ_ERR_ARG, "walk-phase register out of range (1..6 qubits)");
+        if (a.stages == 0 || a.steps_per_stage == 0) return wfail(SQ_ERR_ARG, "empty annealing schedule");
+        if ((uint64_t)a.stages * a.steps_per_stage > (1u << 24)) return wfail(SQ_ERR_ARG, "annealing schedule too long");
+        if (!(a.beta >= 0.0) || !std::isfinite(a.beta)) return wfail(SQ_ERR_ARG, "beta must be finite and non-negative");
+        int sumJ = 0;
+        for (uint32_t b = 0; b < a.spins; ++b) {
+            if (a.J[b] < -kMaxJ || a.J[b] > kMaxJ) return wfail(SQ_ERR_ARG, "couplings must lie in -8..8");
+            sumJ += std::abs(a.J[b]);
+        }
+        WalkDev& d = wd[i];
+        d.s = (int)a.spins;
+        d.q = (int)a.phase_qbits;
+        d.stages = (int)a.stages;
+        d.per = (int)a.steps_per_stage;
+        d.nominal = a.stages * a.steps_per_stage;
+        const uint64_t cap = a.max_steps ? (uint64_t)a.max_steps : 8ull * d.nominal;
+        d.cap = (uint32_t)std::min<uint64_t>(cap, 0xffffffffu);
+        d.beta = a.beta;
+        d.seed = a.seed;
+        d.state_off = state_elems;
+        d.trace_off = trace_len;
+        d.e_off = (uint32_t)energies.size();
+        d.dmax = 2 * sumJ;
+        const uint32_t N = 1u << a.spins;
+        for (uint32_t x = 0; x < N; ++x) {
+            int E = 0;
+            for (uint32_t b = 0; b < a.spins; ++b) {
+                const int sb = 1 - 2 * (int)((x >> b) & 1u);
+                const uint32_t b2 = (b + 1) % a.spins;
+                const int sb2 = 1 - 2 * (int)((x >> b2) & 1u);
+                E -= a.J[b] * sb * sb2;
+            }
+            energies.push_back(E);
+        }
+        const uint32_t ncta = (norbits(d.s) + kOrbitsPerCta - 1) / kOrbitsPerCta;
+        d.cta0 = (uint32_t)cta_walk.size();
+        d.ncta = ncta;
+        for (uint32_t c = 0; c < ncta; ++c) cta_walk.push_back((int)i);
+        state_elems += 2ull << (2 * a.spins);
+        trace_len += d.cap;
+        max_cap = std::max(max_cap, d.cap);
+    }
+    std::vector<double> cos64(kMaxL);
+    for (int t = 0; t < kMaxL; ++t) cos64[t] = std::cos(2.0 * M_PI * (double)t / (double)kMaxL);
+
+    WalkDev* d_walks = nullptr;
+    WalkRec* d_recs = nullptr;
+    int* d_cta = nullptr;
+    int* d_E = nullptr;
+    void* d_states = nullptr;
+    double* d_partial = nullptr;
+    double* d_cos = nullptr;
+    double* d_trace = nullptr;
+    unsigned int* d_running = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(d_walks);
+        cudaFree(d_recs);
+        cudaFree(d_cta);
+        cudaFree(d_E);
+        cudaFree(d_states);
+        cudaFree(d_partial);
+        cudaFree(d_cos);
+        cudaFree(d_trace);
+        cudaFree(d_running);
+    };
+    const size_t nct = cta_walk.size();
+    bool ok = cudaMalloc(&d_walks, sizeof(WalkDev) * nwalks) == cudaSuccess &&
+              cudaMalloc(&d_recs, sizeof(WalkRec) * nwalks) == cudaSuccess &&
+              cudaMalloc(&d_cta, sizeof(int) * nct) == cudaSuccess &&
+              cudaMalloc(&d_E, sizeof(int) * energies.size()) == cudaSuccess &&
+              cudaMalloc(&d_states, esz * state_elems) == cudaSuccess &&
+              cudaMalloc(&d_partial, sizeof(double) * kMaxL * nct) == cudaSuccess &&
+              cudaMalloc(&d_cos, sizeof(double) * kMaxL) == cudaSuccess &&
+              cudaMalloc(&d_running, sizeof(unsigned int)) == cudaSuccess &&
+              (!p0_trace || cudaMalloc(&d_trace, sizeof(double) * trace_len) == cudaSuccess);
+    if (!ok) {
+        cudaGetLastError();
+        cleanup();
+        return wfail(SQ_ERR_NOMEM, "device allocation for the walk batch failed");
+    }
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t err = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    const unsigned int nrun = nwalks;
+    if (err == cudaSuccess) err = cudaMemcpyAsync(d_walks, wd.data(), sizeof(WalkDev) * nwalks, cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(d_cta, cta_walk.data(), sizeof(int) * nct, cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(d_E, energies.data(), sizeof(int) * energies.size(), cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(d_cos, cos64.data(), sizeof(double) * kMaxL, cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(d_running, &nrun, sizeof(unsigned int), cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess && d_trace) err = cudaMemsetAsync(d_trace, 0, sizeof(double) * trace_len, st);
+    if (err == cudaSuccess) err = cudaEventRecord(e0, st);
+    if (err == cudaSuccess) {
+        k_walk_init<<<(nwalks + 127) / 128, 128, 0, st>>>(d_walks, d_recs, (int)nwalks);
+        err = cudaGetLastError();
+    }
+    // advance every running walk one step per iteration; poll the running count
+    // every `chunk` iterations
+    const uint32_t chunk = 16;
+    uint32_t iter = 0;
+    unsigned int left = nrun;
+    while (err == cudaSuccess && left > 0 && iter < max_cap) {
+        const uint32_t q = std::min(chunk, max_cap - iter);
+        for (uint32_t k = 0; k < q && err == cudaSuccess; ++k) {
+            if (precision == SQ_F64)
+                k_walk_step<double><<<(unsigned)nct, kThreads, 0, st>>>(d_walks, d_cta, d_recs, d_E,
+                                                                        (double*)d_states, d_partial);
+            else
+                k_walk_step<float><<<(unsigned)nct, kThreads, 0, st>>>(d_walks, d_cta, d_recs, d_E,
+                                                                       (float*)d_states, d_partial);
+            err = cudaGetLastError();
+            if (err != cudaSuccess) break;
+            k_walk_measure<<<nwalks, kMaxL, 0, st>>>(d_walks, d_recs, d_partial, d_cos, d_trace, d_running);
+            err = cudaGetLastError();
+        }
+        iter += q;
+        if (err == cudaSuccess) err = cudaMemcpyAsync(&left, d_running, sizeof(unsigned int), cudaMemcpyDeviceToHost, st);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    }
+    if (err == cudaSuccess) {
+        uint32_t smax = 0;
+        for (uint32_t i = 0; i < nwalks; ++i) smax = std::max<uint32_t>(smax, walks[i].spins);
+        const size_t smem = sizeof(double) << smax;
+        if (precision == SQ_F64) {
+            err = cudaFuncSetAttribute(k_walk_readout<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (err == cudaSuccess) k_walk_readout<double><<<nwalks, 1024, smem, st>>>(d_walks, d_recs, (const double*)d_states);
+        } else {
+            err = cudaFuncSetAttribute(k_walk_readout<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (err == cudaSuccess) k_walk_readout<float><<<nwalks, 1024, smem, st>>>(d_walks, d_recs, (const float*)d_states);
+        }
+        if (err == cudaSuccess) err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = cudaEventRecord(e1, st);
+    std::vector<WalkRec> rec(nwalks);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(rec.data(), d_recs, sizeof(WalkRec) * nwalks, cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess && p0_trace)
+        err = cudaMemcpyAsync(p0_trace, d_trace, sizeof(double) * trace_len, cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    float ms = 0.f;
+    if (err == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    if (kernel_ms) *kernel_ms = ms;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st) cudaStreamDestroy(st);
+    cleanup();
+    if (err != cudaSuccess) return wfail(SQ_ERR_CUDA, std::string("walk batch: ") + cudaGetErrorString(err));
+    for (uint32_t i = 0; i < nwalks; ++i) {
+        const WalkRec& R = rec[i];
+        sq_qsa_walk_result& o = results[i];
+        const uint32_t s = walks[i].spins;
+        o.done = R.status == 3 ? 1u : 0u;
+        o.restarts = R.restarts;
+        o.steps = R.total;
+        o.readout = o.done ? R.readout : 0u;
+        o.last_p0 = R.last_p0;
+        o.E = 0.0;
+        o.absM = 0.0;
+        if (o.done) {
+            o.E = (double)energies[wd[i].e_off + R.readout];
+            int M = 0;
+            for (uint32_t b = 0; b < s; ++b) M += 1 - 2 * (int)((R.readout >> b) & 1u);
+            o.absM = (double)std::abs(M);
+        }
+    }
+    return SQ_OK;
+}

@@ -67,3 +67,31 @@ def test_batch_entry_points_reject_bad_arguments_before_any_device_call():
     assert L.sq_batch_create(ctypes.byref(h), ch, 1, _lib.SQ_F32, None) == _lib.SQ_ERR_ARG
     ch[0].spins, ch[0].ene_qbits = 16, 7  # 24 qubits
     assert L.sq_batch_create(ctypes.byref(h), ch, 1, _lib.SQ_F32, None) == _lib.SQ_ERR_ARG
+
+
+def test_walk_batch_rejects_bad_arguments_before_any_device_call():
+    from suqa_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("libsq not built")
+    L = _lib.load()
+    w = (_lib.SqQsaWalk * 1)()
+    res = (_lib.SqQsaWalkResult * 1)()
+    ms = ctypes.c_float()
+
+    def walk(**kw):
+        a = dict(spins=4, phase_qbits=3, stages=2, steps_per_stage=2, max_steps=0, beta=1.0, seed=1)
+        a.update(kw)
+        J = kw.get("J", [1] * 12)
+        return _lib.SqQsaWalk(a["spins"], a["phase_qbits"], a["stages"], a["steps_per_stage"], a["max_steps"],
+                              (ctypes.c_int32 * 12)(*J), 0, a["beta"], a["seed"])
+
+    for bad, msg in ((dict(spins=13), b"ring length"), (dict(spins=1), b"ring length"),
+                     (dict(phase_qbits=7), b"walk-phase"), (dict(phase_qbits=0), b"walk-phase"),
+                     (dict(stages=0), b"schedule"), (dict(beta=-1.0), b"beta"),
+                     (dict(J=[9] + [1] * 11), b"couplings")):
+        w[0] = walk(**bad)
+        assert L.sq_qsa_walk_batch(w, 1, _lib.SQ_F32, res, None, ctypes.byref(ms)) == _lib.SQ_ERR_ARG, bad
+        assert msg in L.sq_last_error(), (bad, L.sq_last_error())
+    w[0] = walk()
+    assert L.sq_qsa_walk_batch(w, 0, _lib.SQ_F32, res, None, ctypes.byref(ms)) == _lib.SQ_ERR_ARG
+    assert L.sq_qsa_walk_batch(w, 1, 7, res, None, ctypes.byref(ms)) == _lib.SQ_ERR_ARG

@@ -1,0 +1,84 @@
+"""Batched Szegedy-walk annealing on the GPU against the oracle walk driver:
+the same PCG32 streams give the same restarts, step counts and spin readouts,
+and the per-step probability of the zero walk phase agrees to rounding."""
+import numpy as np
+import pytest
+
+import oracle
+import qsa_walk as qw
+
+pytestmark = pytest.mark.gpu
+
+
+def _walks(n, seed, spins=(2, 7), q=(1, 7), stages=3, per=4, J=(-2, 3), beta=(0.3, 3.0), max_steps=0):
+    from suqa_gb300.walk import QsaWalk
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        s = int(rng.integers(*spins))
+        out.append(QsaWalk(s, [int(v) for v in rng.integers(J[0], J[1], s)], float(rng.uniform(*beta)), stages, per,
+                           int(rng.integers(*q)), 900 + k, max_steps))
+    return out
+
+
+def _oracle(w):
+    return qw.run_walk(w.spins, w.J, w.beta, w.stages, w.steps_per_stage, w.phase_qbits, w.seed, w.max_steps,
+                       rng=oracle.Pcg32(w.seed))
+
+
+def _check(runs, walks, tol):
+    for r, w in zip(runs, walks):
+        o = _oracle(w)
+        assert (r.done, r.restarts, r.steps, r.readout) == (bool(o.done), o.restarts, o.steps, o.readout), w
+        assert (r.E, r.absM) == (o.E, o.absM)
+        assert np.max(np.abs(r.p0 - np.array(o.p0))) < tol, w
+
+
+def test_fp64_walks_match_the_oracle():
+    from suqa_gb300.walk import run_qsa_walks
+    walks = _walks(24, 1)
+    runs, ms = run_qsa_walks(walks, "f64", trace=True)
+    assert ms > 0
+    _check(runs, walks, 1e-10)
+
+
+def test_fp32_walks_match_the_oracle():
+    from suqa_gb300.walk import run_qsa_walks
+    walks = _walks(24, 2, q=(2, 5))
+    runs, _ = run_qsa_walks(walks, "f32", trace=True)
+    _check(runs, walks, 2e-5)
+
+
+def test_capped_and_restarting_walks():
+    """Cold rings with a wide walk-phase register restart often; a small cap
+    stops them with done = 0 after exactly max_steps steps."""
+    from suqa_gb300.walk import run_qsa_walks
+    walks = _walks(12, 3, spins=(3, 6), q=(5, 7), stages=4, per=5, beta=(4.0, 8.0), max_steps=9)
+    runs, _ = run_qsa_walks(walks, "f64", trace=True)
+    _check(runs, walks, 1e-10)
+    assert any(not r.done for r in runs) and all(r.steps <= 9 for r in runs)
+
+
+def test_eight_spin_rings_match_the_oracle():
+    from suqa_gb300.walk import run_qsa_walks
+    walks = _walks(3, 4, spins=(8, 9), q=(6, 7), stages=1, per=3, J=(-1, 2))
+    for w in walks:
+        w.J = [v if v != 0 else 1 for v in w.J]
+    runs, _ = run_qsa_walks(walks, "f64", trace=True)
+    _check(runs, walks, 1e-10)
+
+
+def test_ten_spin_rings_fp32_follow_fp64():
+    """The configured ring length (10 spins, 2^21 amplitudes per walk): FP32
+    and FP64 give the same walks, p0 to FP32 rounding."""
+    from suqa_gb300.walk import ising_ring_walks, run_qsa_walks
+    walks = ising_ring_walks(16, 10, 1.0, 5, 2, 6, seed=7)
+    r64, _ = run_qsa_walks(walks, "f64", trace=True)
+    r32, _ = run_qsa_walks(walks, "f32", trace=True)
+    same = 0
+    for a, b in zip(r32, r64):
+        assert 0.0 <= b.last_p0 <= 1.0 + 1e-12
+        if (a.done, a.restarts, a.steps, a.readout) == (b.done, b.restarts, b.steps, b.readout):
+            same += 1
+            assert np.max(np.abs(a.p0 - b.p0)) < 1e-4
+    assert same >= 14

@@ -107,12 +107,24 @@ __device__ __forceinline__ uint32_t draw_move(uint64_t& st, uint64_t inc, int s)
 // register slot of orbit coordinates (a: x ^= d', b: x ^= e_C, c: d ^= e_C, acc)
 #define SLOT(a, b, c, acc) (((a) << 3) | ((b) << 2) | ((c) << 1) | (acc))
 
+// The walk W on one orbit, scalar form (FP64).  The Hadamards run unnormalised;
+// the first rotation of each H R S0 R^T H group carries their factor 1/2.
 template <typename T>
 struct Orbit {
     T v[16];
-    T e[8], r[8], he[8], hr[8];  // rotation per position (a, b, c); he/hr carry the 1/2 of two Hadamards
+    T e[8], r[8], he[8], hr[8];  // rotation per position (a, b, c)
     uint32_t zmask;              // positions with dE = 0
 
+    __device__ __forceinline__ void setup(const T (&ce)[8], const T (&cr)[8], uint32_t z) {
+#pragma unroll
+        for (int p = 0; p < 8; ++p) {
+            e[p] = ce[p];
+            r[p] = cr[p];
+            he[p] = (T)0.5 * ce[p];
+            hr[p] = (T)0.5 * cr[p];
+        }
+        zmask = z;
+    }
     __device__ __forceinline__ void lam() {
 #pragma unroll
         for (int p = 0; p < 8; ++p)
@@ -165,6 +177,179 @@ struct Orbit {
         lam(); hc(); rot_half(); sw0(); rot_inv(); hc();
         lam(); hc(); rot_half(); sw0(); rot_inv(); hc();
     }
+    // v = psi on entry; returns with v = sum_{k<L} W^k psi, red[k] += <psi, W^k psi>
+    __device__ __forceinline__ void run(int L, T wgt, int lane, double* red) {
+        T psi[16], S[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            psi[j] = v[j];
+            S[j] = (T)0;
+        }
+        for (int k = 0; k < L; ++k) {
+            T dot = (T)0;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                dot += psi[j] * v[j];
+                S[j] += v[j];
+            }
+            dot *= wgt;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, off);
+            if (lane == 0) red[k] += (double)dot;
+            if (k < L - 1) walk();
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = S[j];
+    }
+};
+
+// FP32 form on Blackwell's packed f32x2 arithmetic: each 64-bit register holds
+// the pair (b = 0, b = 1) of one (a, c, acc).  The Hadamard on the copy bit is
+// then two packed FMAs with sign vectors, the swap renames pairs (c = 0) or
+// swaps their halves (c = 1), and both rotations use (e, r) / sqrt(2), which
+// carries the factor 1/2 of the two unnormalised Hadamards around them.
+typedef unsigned long long f2;
+
+__device__ __forceinline__ f2 pk2(float x, float y) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+    return r;
+}
+__device__ __forceinline__ void up2(f2 v, float& x, float& y) { asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v)); }
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 swap2(f2 v) {
+    float x, y;
+    up2(v, x, y);
+    return pk2(y, x);
+}
+
+struct OrbitF2 {
+    f2 P[2][2][2];      // [a][c][acc], halves b = 0, 1
+    f2 A[2][2], B[2][2], NB[2][2], SG[2][2];  // per (a, c): e/sqrt2, r/sqrt2, -r/sqrt2, L1 sign on acc = 0
+
+    __device__ __forceinline__ void setup(const float (&ce)[8], const float (&cr)[8], uint32_t z) {
+        const float h = 0.70710678118654752f;
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const int p0 = (a << 2) | c, p1 = (a << 2) | 2 | c;  // positions (a, b = 0, c), (a, b = 1, c)
+                A[a][c] = pk2(h * ce[p0], h * ce[p1]);
+                B[a][c] = pk2(h * cr[p0], h * cr[p1]);
+                NB[a][c] = pk2(-h * cr[p0], -h * cr[p1]);
+                SG[a][c] = pk2(((z >> p0) & 1u) ? -1.f : 1.f, ((z >> p1) & 1u) ? -1.f : 1.f);
+            }
+    }
+    __device__ __forceinline__ void load(const float (&v)[16]) {
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+#pragma unroll
+                for (int acc = 0; acc < 2; ++acc) P[a][c][acc] = pk2(v[SLOT(a, 0, c, acc)], v[SLOT(a, 1, c, acc)]);
+    }
+    __device__ __forceinline__ void lam() {
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int c = 0; c < 2; ++c) P[a][c][0] = mul2(P[a][c][0], SG[a][c]);
+    }
+    // copy bit = b ^ c: new c0 = (A + B, B - A), new c1 = (A - B, A + B) over the halves b = 0, 1
+    __device__ __forceinline__ void hc(f2 pm, f2 mp) {
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int acc = 0; acc < 2; ++acc) {
+                const f2 X = P[a][0][acc], Y = P[a][1][acc];
+                P[a][0][acc] = fma2(X, pm, Y);
+                P[a][1][acc] = fma2(Y, mp, X);
+            }
+    }
+    __device__ __forceinline__ void rot() {  // [[e, -r], [r, e]] / sqrt2
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const f2 p0 = P[a][c][0], p1 = P[a][c][1];
+                P[a][c][0] = fma2(NB[a][c], p1, mul2(A[a][c], p0));
+                P[a][c][1] = fma2(B[a][c], p0, mul2(A[a][c], p1));
+            }
+    }
+    __device__ __forceinline__ void rot_t() {  // [[e, r], [-r, e]] / sqrt2
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const f2 p0 = P[a][c][0], p1 = P[a][c][1];
+                P[a][c][0] = fma2(B[a][c], p1, mul2(A[a][c], p0));
+                P[a][c][1] = fma2(NB[a][c], p0, mul2(A[a][c], p1));
+            }
+    }
+    __device__ __forceinline__ void sw0() {
+        f2 t = P[0][0][0];
+        P[0][0][0] = P[1][0][0];
+        P[1][0][0] = t;
+        t = P[0][1][0];
+        P[0][1][0] = swap2(P[1][1][0]);
+        P[1][1][0] = swap2(t);
+    }
+    __device__ __forceinline__ void walk(f2 pm, f2 mp) {
+        lam(); hc(pm, mp); rot(); sw0(); rot_t(); hc(pm, mp);
+        lam(); hc(pm, mp); rot(); sw0(); rot_t(); hc(pm, mp);
+    }
+    __device__ __forceinline__ void run(float (&v)[16], int L, float wgt, int lane, double* red) {
+        load(v);
+        const f2 pm = pk2(1.f, -1.f), mp = pk2(-1.f, 1.f);
+        f2 psi[2][2][2], S[2][2][2];
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+#pragma unroll
+                for (int acc = 0; acc < 2; ++acc) {
+                    psi[a][c][acc] = P[a][c][acc];
+                    S[a][c][acc] = 0ull;
+                }
+        for (int k = 0; k < L; ++k) {
+            f2 d2 = 0ull;
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+                for (int c = 0; c < 2; ++c)
+#pragma unroll
+                    for (int acc = 0; acc < 2; ++acc) {
+                        d2 = fma2(psi[a][c][acc], P[a][c][acc], d2);
+                        S[a][c][acc] = add2(S[a][c][acc], P[a][c][acc]);
+                    }
+            float x, y;
+            up2(d2, x, y);
+            float dot = (x + y) * wgt;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, off);
+            if (lane == 0) red[k] += (double)dot;
+            if (k < L - 1) walk(pm, mp);
+        }
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+#pragma unroll
+                for (int acc = 0; acc < 2; ++acc) up2(S[a][c][acc], v[SLOT(a, 0, c, acc)], v[SLOT(a, 1, c, acc)]);
+    }
 };
 
 template <typename T>
@@ -204,7 +389,6 @@ k_walk_step(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
         const uint32_t o = first + (uint32_t)(it * kThreads) + threadIdx.x;
         const bool active = o < norb;
         if (!__any_sync(0xffffffffu, active)) continue;  // warp-uniform
-        Orbit<T> ob;
         uint32_t dp = 0, x0 = 0;
         bool single = true;
         if (active) {
@@ -220,7 +404,8 @@ k_walk_step(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
                 x0 = ins0(ins0(ri, min(p, C)), max(p, C));
             }
         }
-        ob.zmask = 0;
+        T v[16], ce[8], cr[8];
+        uint32_t zmask = 0;
 #pragma unroll
         for (int pos = 0; pos < 8; ++pos) {
             const int a = pos >> 2, b = (pos >> 1) & 1, c = pos & 1;
@@ -229,11 +414,9 @@ k_walk_step(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
             int dE = 0;
             if (active) dE = E[x ^ d] - E[x];
             const int k = dE > 0 ? dE : 0;
-            ob.e[pos] = tab_e[k];
-            ob.r[pos] = tab_r[k];
-            ob.he[pos] = (T)0.5 * ob.e[pos];
-            ob.hr[pos] = (T)0.5 * ob.r[pos];
-            if (dE == 0) ob.zmask |= 1u << pos;
+            ce[pos] = tab_e[k];
+            cr[pos] = tab_r[k];
+            if (dE == 0) zmask |= 1u << pos;
 #pragma unroll
             for (int acc = 0; acc < 2; ++acc) {
                 T val = (T)0;
@@ -244,32 +427,26 @@ k_walk_step(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
                         val = st[(uint64_t)acc * NN + (uint64_t)d * N + x] * scale;
                     }
                 }
-                ob.v[SLOT(a, b, c, acc)] = val;
+                v[SLOT(a, b, c, acc)] = val;
             }
         }
         if (single) {
 #pragma unroll
-            for (int j = 0; j < 8; ++j) ob.v[8 + j] = ob.v[j];
-        }
-        T psi[16], S[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            psi[j] = ob.v[j];
-            S[j] = (T)0;
+            for (int j = 0; j < 8; ++j) v[8 + j] = v[j];
         }
         const T wgt = single ? (T)0.5 : (T)1;
-        for (int k = 0; k < L; ++k) {
-            T dot = (T)0;
+        if constexpr (sizeof(T) == 4) {
+            OrbitF2 ob;
+            ob.setup(ce, cr, zmask);
+            ob.run(v, L, wgt, lane, red[warp]);
+        } else {
+            Orbit<T> ob;
+            ob.setup(ce, cr, zmask);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                dot += psi[j] * ob.v[j];
-                S[j] += ob.v[j];
-            }
-            dot *= wgt;
+            for (int j = 0; j < 16; ++j) ob.v[j] = v[j];
+            ob.run(L, wgt, lane, red[warp]);
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, off);
-            if (lane == 0) red[warp][k] += (double)dot;
-            if (k < L - 1) ob.walk();
+            for (int j = 0; j < 16; ++j) v[j] = ob.v[j];
         }
         if (active) {
 #pragma unroll
@@ -279,7 +456,7 @@ k_walk_step(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
                 const uint32_t x = x0 ^ (a ? dp : 0u) ^ (b ? eC : 0u);
                 const uint32_t d = dp ^ (c ? eC : 0u);
 #pragma unroll
-                for (int acc = 0; acc < 2; ++acc) st[(uint64_t)acc * NN + (uint64_t)d * N + x] = S[SLOT(a, b, c, acc)];
+                for (int acc = 0; acc < 2; ++acc) st[(uint64_t)acc * NN + (uint64_t)d * N + x] = v[SLOT(a, b, c, acc)];
             }
         }
     }

@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--qms-chains", type=int, default=1024)
     ap.add_argument("--qms-steps", type=int, default=6)
     ap.add_argument("--skip-30", action="store_true", help="skip the 30-qubit FP64 repeat")
+    ap.add_argument("--skip-qsa", action="store_true")
+    ap.add_argument("--qsa-walks", type=int, default=1024)
+    ap.add_argument("--qsa-steps", type=int, default=8)
     return ap.parse_args()
 
 
@@ -218,6 +221,47 @@ def qms_section(n_chains, steps, seed=2024):
                               "config": "7 spins, 5 energy qubits (13 qubits), FP64, host-driven (libsq state API)"}
     out["batched_f32_over_plain_steps"] = (out["f32"]["chain_steps_per_s"] / plain) if plain else None
     out["batched_f32_over_plain_phase_estimations"] = (f32_pe / plain_pe) if plain_pe else None
+    return out
+
+
+def qsa_section(n_walks, walk_steps, f64_walks=16, cpu=True, seed=2025):
+    """Batched Szegedy-walk annealing on 10-spin Ising rings (J = +-1 drawn per
+    walk, h = 0, beta 0 -> 1 over 50 stages x 20 walk steps, 6-qubit walk-phase
+    register, one PCG32 stream per walk): every walk capped at its first
+    `walk_steps` walk steps (restarts included), FP32 for all walks, FP64 for the
+    first `f64_walks`.  FP32 work per walk step: 2^9 + 511 * 2^8 register-resident
+    orbits, each 63 applications of W (272 flops: 4 Hadamards x 16, 4 rotations x 48,
+    2 reflections x 8) plus 64 overlap/sum updates (48 flops)."""
+    import numpy as np
+    from suqa_gb300.walk import ising_ring_walks, run_qsa_walks
+    walks = ising_ring_walks(n_walks, 10, 1.0, 50, 20, 6, seed=seed, max_steps=walk_steps)
+    run_qsa_walks(walks[:4], "f32")  # first launch, module load
+    r32, ms32 = run_qsa_walks(walks, "f32", trace=True)
+    r64, ms64 = run_qsa_walks(walks[:f64_walks], "f64", trace=True)
+    st32 = sum(r.steps for r in r32)
+    st64 = sum(r.steps for r in r64)
+    same = [i for i, (a, b) in enumerate(zip(r32, r64)) if (a.restarts, a.steps) == (b.restarts, b.steps)]
+    p0_err = max((float(np.max(np.abs(r32[i].p0 - r64[i].p0))) for i in same), default=None)
+    norb, L = (1 << 9) + ((1 << 9) - 1) * (1 << 8), 64
+    flops = norb * ((L - 1) * 272 + L * 48)
+    out = {"workload": f"{n_walks} walks on 10-spin Ising rings (2^21 amplitudes each), first {walk_steps} walk "
+                       f"steps of the beta 0->1 anneal (50 stages x 20 steps), 6-qubit walk-phase register",
+           "f32": {"walk_steps_per_s": st32 / (ms32 / 1e3), "walk_steps": st32, "device_ms": ms32,
+                   "restarts": int(sum(r.restarts for r in r32)),
+                   "fp32_tflops": flops * st32 / (ms32 / 1e3) / 1e12},
+           "f64": {"walk_steps_per_s": st64 / (ms64 / 1e3), "walk_steps": st64, "device_ms": ms64,
+                   "fp64_tflops": flops * st64 / (ms64 / 1e3) / 1e12, "walks": f64_walks},
+           "fp32_vs_fp64": {"walks_identical": len(same), "walks": f64_walks, "max_abs_p0_diff": p0_err},
+           "flops_per_walk_step": flops}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import qsa_walk as qw
+        cw = qw.CompressedWalk(10, walks[0].J)
+        t0 = time.perf_counter()
+        qw.walk_step(cw, cw.initial(), 3, 0.02, 6)
+        dt = time.perf_counter() - t0
+        out["cpu_port"] = {"s_per_walk_step": dt, "kind": "port", "cores": 1,
+                           "sample": "one walk step of one walk, numpy FP64 oracle"}
     return out
 
 
@@ -449,6 +493,9 @@ def main():
     qms = None
     if rank == 0 and not args.skip_qms:
         qms = qms_section(args.qms_chains, args.qms_steps)
+    qsa = None
+    if rank == 0 and not args.skip_qsa:
+        qsa = qsa_section(args.qsa_walks, args.qsa_steps, cpu=not args.skip_cpu)
 
     if rank == 0:
         cpu = None
@@ -474,7 +521,8 @@ def main():
                 "cpu_baseline": cpu,
                 "fp32_same_circuit": fp32_line,
                 "fp64_30_qubits": n30_line,
-                "qms_batched": qms}
+                "qms_batched": qms,
+                "qsa_walks": qsa}
         print(json.dumps(line), flush=True)
     if st is not None:
         st.close()

@@ -311,7 +311,9 @@ struct OrbitF2 {
         lam(); hc(pm, mp); rot(); sw0(); rot_t(); hc(pm, mp);
         lam(); hc(pm, mp); rot(); sw0(); rot_t(); hc(pm, mp);
     }
-    __device__ __forceinline__ void run(float (&v)[16], int L, float wgt, int lane, double* red) {
+    // v = psi on entry; returns with v = sum_{k<L} W^k psi; red32[k] = the warp's
+    // FP32 sum of <psi, W^k psi> (summed over warps and orbits in FP64 later)
+    __device__ __forceinline__ void run(float (&v)[16], int L, float wgt, int lane, float* red32) {
         load(v);
         const f2 pm = pk2(1.f, -1.f), mp = pk2(-1.f, 1.f);
         f2 psi[2][2][2], S[2][2][2];
@@ -340,7 +342,7 @@ struct OrbitF2 {
             float dot = (x + y) * wgt;
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, off);
-            if (lane == 0) red[k] += (double)dot;
+            if (lane == 0) red32[k] = dot;
             if (k < L - 1) walk(pm, mp);
         }
 #pragma unroll
@@ -360,11 +362,14 @@ k_walk_step(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
     const WalkDev& W = walks[w];
     const WalkRec& R = recs[w];
     if (R.status != 0) return;  // uniform over the CTA
-    __shared__ double red[kThreads / 32][kMaxL];
+    __shared__ double red[kThreads / 32][kMaxL];                    // FP64 path
+    __shared__ float red32[kThreads / 32][kOrbitsPerThread][kMaxL];  // FP32 path
     __shared__ T tab_e[kMaxD + 1], tab_r[kMaxD + 1];
     const int s = W.s, C = (int)R.C, L = 1 << W.q;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < (kThreads / 32) * kMaxL; i += blockDim.x) (&red[0][0])[i] = 0.0;
+    for (int i = threadIdx.x; i < (kThreads / 32) * kOrbitsPerThread * kMaxL; i += blockDim.x)
+        (&red32[0][0][0])[i] = 0.f;
     for (int k = threadIdx.x; k <= W.dmax; k += blockDim.x) {
         double e = 1.0, r = 0.0;
         if (k > 0) {
@@ -438,7 +443,7 @@ k_walk_step(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
         if constexpr (sizeof(T) == 4) {
             OrbitF2 ob;
             ob.setup(ce, cr, zmask);
-            ob.run(v, L, wgt, lane, red[warp]);
+            ob.run(v, L, wgt, lane, red32[warp][it]);
         } else {
             Orbit<T> ob;
             ob.setup(ce, cr, zmask);
@@ -463,7 +468,10 @@ k_walk_step(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
     __syncthreads();
     if (threadIdx.x < L) {
         double sum = 0.0;
-        for (int wp = 0; wp < kThreads / 32; ++wp) sum += red[wp][threadIdx.x];
+        for (int wp = 0; wp < kThreads / 32; ++wp) {
+            sum += red[wp][threadIdx.x];
+            for (int it = 0; it < kOrbitsPerThread; ++it) sum += (double)red32[wp][it][threadIdx.x];
+        }
         partial[(uint64_t)blockIdx.x * kMaxL + threadIdx.x] = sum;
     }
 }

@@ -82,3 +82,25 @@ def test_ten_spin_rings_fp32_follow_fp64():
             same += 1
             assert np.max(np.abs(a.p0 - b.p0)) < 1e-4
     assert same >= 14
+
+
+def test_walk_results_do_not_depend_on_the_batch_split():
+    """Walks are independent: each rank's share (shard.partition) reproduces the
+    walks of the whole batch, so the sharded sums equal the one-batch sums."""
+    from suqa_gb300 import shard
+    from suqa_gb300.walk import run_qsa_walks
+    walks = _walks(20, 5, spins=(3, 8), q=(3, 7))
+    whole, _ = run_qsa_walks(walks, "f32", trace=True)
+    keys, acc = shard.walk_sums(walks, whole, lambda w: w.spins)
+    tot = np.zeros_like(acc)
+    for part in shard.partition(walks, 3, shard.walk_cost):
+        sub = [walks[i] for i in part]
+        runs, _ = run_qsa_walks(sub, "f32", trace=True)
+        for i, r in zip(part, runs):
+            a = whole[i]
+            assert (r.restarts, r.steps, r.readout) == (a.restarts, a.steps, a.readout)
+            assert np.array_equal(r.p0, a.p0)
+        k2, a2 = shard.walk_sums(sub, runs, lambda w: w.spins)
+        for k, row in zip(k2, a2):
+            tot[keys.index(k)] += row
+    assert np.allclose(tot, acc, rtol=0, atol=1e-9)

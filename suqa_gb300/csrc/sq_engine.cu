@@ -183,6 +183,15 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     p.defer = 0;
     p.rmask = rmask;
     p.rval = rval;
+    p.lrm = p.lrv = 0u;
+    for (int b = 0; b < n; ++b) {
+        const int lb = ((rmask >> b) & 1ull) ? local_of(b) : -1;
+        if (lb < 0) continue;
+        p.lrm |= 1u << lb;
+        if ((rval >> b) & 1ull) p.lrv |= 1u << lb;
+    }
+    p.orm = rmask & outer;
+    p.orv = rval & p.orm;
     uint32_t tabpos = 0;
     for (size_t i = i0; i < i1; ++i) {
         const HostOp& h = ops[i];
@@ -224,6 +233,16 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         o.shift = h.shift;
         o.c = h.c;
         o.s = h.s;
+        o.sn = -h.s;
+        // deferred rotations store a + (s/c) iP a (|c| >= |s|) or (c/s) a + iP a
+        o.cbig = std::fabs(h.c) >= std::fabs(h.s) ? 1 : 0;
+        if (h.kind == sqk::OP_PAULI) o.u = o.cbig ? h.s / h.c : h.c / h.s;
+        o.un = -o.u;
+        o.fc = (float)o.c;
+        o.fs = (float)o.s;
+        o.fsn = (float)o.sn;
+        o.fu = (float)o.u;
+        o.fun = (float)o.un;
         if (!h.tab.empty()) {
             o.tab = tabpos;
             std::memcpy(&p.tab[2 * tabpos], h.tab.data(), h.tab.size() * sizeof(double));

@@ -122,8 +122,14 @@ extern "C" int sq_qubit_probs_noalloc(const void* re, const void* im, uint32_t n
     static thread_local sqk::Prog p;
     p.nops = 0;
     p.red = 1;
+    p.defer = 0;
     p.rmask = 1ull << q;
     p.rval = 0;
+    // tiles are the low K qubits: the split qubit is tile-local or outer
+    p.lrm = q < (uint32_t)K ? (1u << q) : 0u;
+    p.lrv = 0u;
+    p.orm = q < (uint32_t)K ? 0ull : (1ull << q);
+    p.orv = 0ull;
     const int block = (K == (int)n) ? (K >= 10 ? 1024 : (K >= 8 ? 256 : 128)) : 256;
     const size_t esz = precision == SQ_F64 ? 8 : 4;
     const size_t smem = 2 * ((size_t)1 << K) * esz + 8;

@@ -36,7 +36,7 @@ enum OpKind : uint8_t {
     OP_SCALE = 8      // a *= s everywhere
 };
 
-// One gate in tile-local form (88 bytes).  For pair operations the pairs are
+// One gate in tile-local form (144 bytes).  For pair operations the pairs are
 // (t0, t0 ^ lflip) with t0 the tile index whose bit lpair is clear.  Control
 // conditions are split into the tile-local part (lcm, lcv: bits of the tile
 // index, tested per element) and the outer part (ocm, ocv: tested once per tile).
@@ -45,6 +45,8 @@ struct Op {
     uint8_t lpair;   // tile-local bit that orders the pair
     uint8_t ny;      // Pauli: number of Y factors
     uint8_t fz;      // Pauli: parity of (flip & zy)
+    uint8_t cbig;    // deferred rotation: |c| >= |s| (the factor c is deferred, else s)
+    uint8_t pad8[3];
     uint32_t lflip;  // tile-local flip mask
     uint32_t lcm, lcv;     // tile-local control condition
     uint32_t lzy;          // tile-local Y|Z mask (Pauli signs)
@@ -53,7 +55,9 @@ struct Op {
     uint64_t cmask, cval;  // global element condition (diagonal slow paths)
     uint64_t ocm, ocv;     // part of the condition on qubits outside the tile
     uint64_t zy;           // Pauli: global Y|Z mask; PLIST/W: extraction mask
-    double c, s;
+    double c, s, sn;       // sn = -s
+    double u, un;          // deferred rotation: u = s/c (cbig) or c/s, un = -u
+    float fc, fs, fsn, fu, fun, fpad;  // the same in FP32 for the FP32 kernel
 };
 
 struct Prog {
@@ -62,6 +66,8 @@ struct Prog {
     int defer;           // 1: uniform H / rotations defer their scale factor
     int pad;
     uint64_t rmask, rval;
+    uint32_t lrm, lrv;   // tile-local part of rmask / rval
+    uint64_t orm, orv;   // part outside the tile
     Op ops[kMaxOps];
     double tab[2 * kMaxTab];
 };
@@ -117,9 +123,17 @@ __device__ __forceinline__ void rot_k(T ar, T ai, T br, T bi, int k, T c, T sp, 
     outi = ai * c + xi * fi;
 }
 
+// x with its sign flipped when f (an integer operation, off the floating-point pipes)
+__device__ __forceinline__ double neg_if(double x, bool f) {
+    return __longlong_as_double(__double_as_longlong(x) ^ ((long long)f << 63));
+}
+__device__ __forceinline__ float neg_if(float x, bool f) {
+    return __uint_as_float(__float_as_uint(x) ^ ((unsigned)f << 31));
+}
+
 // Deferred-scale rotation: with cbig, out = a + u*(i^k b) (u = s/c, the factor c
 // deferred); otherwise out = u*a + i^k b (u = c/s, the factor s deferred).
-// up = +u, un = -u.
+// up = +u, un = -u.  One fused multiply-add per component either way.
 template <typename T>
 __device__ __forceinline__ void rot_deferred(T ar, T ai, T br, T bi, int k, T up, T un, bool cbig, T& outr,
                                              T& outi) {
@@ -127,21 +141,20 @@ __device__ __forceinline__ void rot_deferred(T ar, T ai, T br, T bi, int k, T up
     const T xi = (k & 1) ? br : bi;
     const bool nr = (k == 1 || k == 2), ni = (k >= 2);
     if (cbig) {
-        outr = ar + xr * (nr ? un : up);
-        outi = ai + xi * (ni ? un : up);
+        outr = fma(xr, nr ? un : up, ar);
+        outi = fma(xi, ni ? un : up, ai);
     } else {
-        outr = nr ? (ar * up - xr) : (ar * up + xr);
-        outi = ni ? (ai * up - xi) : (ai * up + xi);
+        outr = fma(ar, up, neg_if(xr, nr));
+        outi = fma(ai, up, neg_if(xi, ni));
     }
 }
 
+// part + |a|^2 (FP64 accumulation; FP32 amplitudes square in FP32)
+__device__ __forceinline__ double add_sq(double part, double r, double i) { return fma(r, r, fma(i, i, part)); }
+__device__ __forceinline__ double add_sq(double part, float r, float i) { return part + (double)fmaf(r, r, i * i); }
+
 __device__ __forceinline__ void scale_vec(double2& v, double s) { v.x *= s; v.y *= s; }
 __device__ __forceinline__ void scale_vec(float4& v, float s) { v.x *= s; v.y *= s; v.z *= s; v.w *= s; }
-
-template <typename T>
-__device__ __forceinline__ double sqnorm(T r, T i) {
-    return (double)(r * r + i * i);
-}
 
 template <typename T>
 __device__ __forceinline__ void block_reduce2(double& a, double& b, double (*sh)[33]) {
@@ -235,7 +248,12 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
         for (int k = 0; k < p.nops; ++k) {
             const Op& op = p.ops[k];
             if ((base & op.ocm) != op.ocv) continue;
-            const T c = (T)op.c, s = (T)op.s, sneg = (T)(-op.s);
+            T c, s, sneg, up, un;
+            if constexpr (sizeof(T) == 8) {
+                c = op.c; s = op.s; sneg = op.sn; up = op.u; un = op.un;
+            } else {
+                c = op.fc; s = op.fs; sneg = op.fsn; up = op.fu; un = op.fun;
+            }
             const int kind = op.kind;
             const uint32_t lcm = op.lcm, lcv = op.lcv;
             if (kind <= OP_PAULI && !(kind == OP_PAULI && op.lflip == 0u) || kind == OP_W) {
@@ -285,9 +303,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                     const uint32_t lzy = op.lzy;
                     const int ny = op.ny, fz = op.fz;
                     if (lcm == 0u && (op.gdefer || p.defer)) {
-                        const bool cbig = fabs(op.c) >= fabs(op.s);
-                        const double ud = cbig ? op.s / op.c : op.c / op.s;
-                        const T up = (T)ud, un = (T)(-ud);
+                        const bool cbig = op.cbig != 0;
                         for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
                             const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
                             const int pz0 = tpar ^ (__popc(t0 & lzy) & 1);
@@ -338,9 +354,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                 const int tpar = parity64(base & op.zy);
                 const uint32_t lzy = op.lzy;
                 if (lcm == 0u && (op.gdefer || p.defer)) {
-                    const bool cbig = fabs(op.c) >= fabs(op.s);
-                    const double ud = cbig ? op.s / op.c : op.c / op.s;
-                    const T up = (T)ud, un = (T)(-ud);
+                    const bool cbig = op.cbig != 0;
                     for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
                         const T ar = sre[t], ai = sim[t];
                         T r, i;
@@ -359,6 +373,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                     }
                 }
             } else {
+                const bool unit = op.s == 1.0;
                 for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
                     const uint64_t g = base | offs[t >> L] | (t & lowmask);
                     T ar = sre[t], ai = sim[t];
@@ -374,7 +389,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                         // (a zero state gives 0 * inf = NaN everywhere, like the reference);
                         // a scale of exactly 1 (kept by the host's global scale) is skipped
                         const bool keep = (g & op.cmask) == op.cval;
-                        if (op.s == 1.0) {
+                        if (unit) {
                             sre[t] = keep ? ar : (T)0;
                             sim[t] = keep ? ai : (T)0;
                         } else {
@@ -392,26 +407,47 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
         const T sg = (T)sigma;
         const double sg2 = sigma * sigma;
 
-        // ---- reduction contribution and store
+        // ---- reduction contribution and store.  Each thread sums the squared
+        // magnitudes of its elements of this tile into an FP64 partial (an FP32
+        // amplitude's |a|^2 is formed in FP32, the same operations in every
+        // entry point, then added in FP64), then adds the partial, times the tile
+        // scale sigma^2, to its accumulators; the split (red = 1) or filter
+        // (red = 2) bit is enumerated directly when it lies in the tile, and
+        // decided once per tile otherwise.
         if (p.red) {
-            for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
-                const uint64_t g = base | offs[t >> L] | (t & lowmask);
-                const double w = sqnorm<T>(sre[t], sim[t]) * sg2;
-                if (p.red == 1) {
-                    if (g & p.rmask) acc1 += w; else acc0 += w;
-                } else if ((g & p.rmask) == p.rval) {
-                    acc0 += w;
+            double part0 = 0.0, part1 = 0.0;
+            if (p.red == 1 && p.lrm) {
+                const uint32_t lb = (uint32_t)(__ffs(p.lrm) - 1);
+                for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
+                    const uint32_t t0 = insert_zero(pp, lb), t1 = t0 | (1u << lb);
+                    part0 = add_sq(part0, sre[t0], sim[t0]);
+                    part1 = add_sq(part1, sre[t1], sim[t1]);
+                }
+            } else if (p.red == 1) {
+                for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) part0 = add_sq(part0, sre[t], sim[t]);
+                if (base & p.rmask) {
+                    part1 = part0;
+                    part0 = 0.0;
+                }
+            } else if ((base & p.orm) == p.orv) {
+                const uint32_t nsel = TS >> __popc(p.lrm);
+                for (uint32_t u = threadIdx.x; u < nsel; u += blockDim.x) {
+                    const uint32_t t = deposit_zeros(u, p.lrm) | p.lrv;
+                    part0 = add_sq(part0, sre[t], sim[t]);
                 }
             }
+            acc0 += part0 * sg2;
+            acc1 += part1 * sg2;
         }
         if (a.store) {
+            const bool scaled = sigma != 1.0;
             if ((1u << L) >= (uint32_t)W) {
                 for (uint32_t v = threadIdx.x; v < TS / W; v += blockDim.x) {
                     const uint32_t t = v * W;
                     const uint64_t g = base | offs[t >> L] | (t & lowmask);
                     V vr = *reinterpret_cast<const V*>(sre + t);
                     V vi = *reinterpret_cast<const V*>(sim + t);
-                    if (sigma != 1.0) {
+                    if (scaled) {
                         scale_vec(vr, sg);
                         scale_vec(vi, sg);
                     }

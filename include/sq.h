@@ -75,6 +75,10 @@ int sq_upload(sq_state* s, const void* host_re, const void* host_im);
 int sq_download(sq_state* s, void* host_re, void* host_im);
 /* Gate fusion on/off (default on); off applies every gate as its own pass. */
 int sq_set_fusion(sq_state* s, int enabled);
+/* Tile size of the fused passes in qubits (0: the default for the state's size
+ * and precision; else 6 .. 13 in FP64, 6 .. 14 in FP32).  A tuning knob: results
+ * do not depend on it beyond floating-point summation order. */
+int sq_set_tile_qubits(sq_state* s, int k);
 
 /* --- state utilities: src/suqa.cu:70-111 --- */
 int sq_init_state(sq_state* s);                   /* suqa::init_state */

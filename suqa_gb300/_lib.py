@@ -83,6 +83,7 @@ _SIGS = {
     "sq_get_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "sq_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "sq_set_fusion": (C.c_int, [C.c_void_p, C.c_int]),
+    "sq_set_tile_qubits": (C.c_int, [C.c_void_p, C.c_int]),
     "sq_upload": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "sq_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "sq_init_state": (C.c_int, [C.c_void_p]),

@@ -505,6 +505,15 @@ int sq_set_fusion(sq_state* s, int enabled) {
     return rc;
 }
 
+int sq_set_tile_qubits(sq_state* s, int k) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    if (k != 0 && (k < 6 || k > tile_cap(s))) return fail(SQ_ERR_ARG, "tile qubits out of range (0, or 6..tile cap)");
+    int rc = flush(s);
+    s->kp = k ? std::min(k, (int)s->n) : default_tile(s);
+    if ((int)s->n <= small_max(s)) s->kp = (int)s->n;  // small states run as one tile
+    return rc;
+}
+
 int sq_get_state(sq_state* s, double* re, double* im) {
     if (!s || !re || !im) return fail(SQ_ERR_ARG, "null argument");
     int rc = materialize(s);

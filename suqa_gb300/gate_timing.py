@@ -3,8 +3,12 @@ over an n-qubit state, timed with the engine's per-launch CUDA events, plus the
 fused random circuit of the benchmark.
 
     python -m suqa_gb300.gate_timing [n] [precision]
+    python -m suqa_gb300.gate_timing --kind h|u1|ptp|x|cx|mcx [n] [precision]
 
 Prints one JSON object: per case (ms per pass, launches, bytes per launch, GB/s).
+The --kind form applies H to every qubit, then 60 gates of one type drawn by the
+benchmark's generator (fusion on): the workload for counting the floating-point
+instructions of one gate type under a profiler.
 """
 from __future__ import annotations
 
@@ -53,7 +57,27 @@ def run(n: int = 28, precision: str = "f64"):
     return out
 
 
+def single_kind(kind: str, n: int = 22, precision: str = "f64", count: int = 60):
+    gates = [g for g in random_circuit(n, 10 * count, seed=3, measure_every=0) if g[0] == kind][:count]
+    st = State(n, precision)
+    st.apply_h(list(range(n)))
+    st.flush()
+    apply_circuit(st, gates)
+    st.flush()
+    st.synchronize()
+    out = {"kind": kind, "gates": len(gates), "stats": st.stats()}
+    st.close()
+    return out
+
+
 if __name__ == "__main__":
-    n = int(sys.argv[1]) if len(sys.argv) > 1 else 28
-    prec = sys.argv[2] if len(sys.argv) > 2 else "f64"
-    print(json.dumps({"n": n, "precision": prec, "passes": run(n, prec)}))
+    args = sys.argv[1:]
+    if args and args[0] == "--kind":
+        kind = args[1]
+        n = int(args[2]) if len(args) > 2 else 22
+        prec = args[3] if len(args) > 3 else "f64"
+        print(json.dumps({"n": n, "precision": prec, **single_kind(kind, n, prec)}))
+    else:
+        n = int(args[0]) if args else 28
+        prec = args[1] if len(args) > 1 else "f64"
+        print(json.dumps({"n": n, "precision": prec, "passes": run(n, prec)}))

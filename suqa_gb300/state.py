@@ -92,6 +92,10 @@ class State:
     def set_fusion(self, enabled: bool):
         check(self.L.sq_set_fusion(self.h, 1 if enabled else 0))
 
+    def set_tile_qubits(self, k: int):
+        """Tile size of the fused passes (0: default)."""
+        check(self.L.sq_set_tile_qubits(self.h, k))
+
     def get_state(self) -> np.ndarray:
         N = self.size()
         re = np.empty(N, dtype=np.float64)

@@ -146,3 +146,27 @@ def test_overlapping_global_control_vs_oracle(seed):
     n = 4 + seed % 9
     lines = circuits.random_script(2000 + seed, n, 80, overlap="engine", dump_every=8)
     golden_io.compare_results(gpu_script.run_script(lines), oracle.run_script(lines), rtol=RTOL64)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_tile_size_does_not_change_results(precision):
+    """The fused-pass tile size is a tuning knob: the same circuit at several
+    tile sizes gives the same measured bits and amplitudes to rounding."""
+    from suqa_gb300 import State
+    from suqa_gb300.workloads import apply_circuit, random_circuit
+    n = 16
+    gates = random_circuit(n, 200, seed=11, measure_every=50)
+    results = []
+    for k in (0, 8, 10, 12):
+        with State(n, precision) as st:
+            st.set_tile_qubits(k)
+            st.apply_h(list(range(n)))
+            bits = apply_circuit(st, gates)
+            results.append((bits, st.get_state()))
+    tol = 1e-12 if precision == "f64" else 2e-5
+    for bits, amp in results[1:]:
+        assert bits == results[0][0]
+        assert np.max(np.abs(amp - results[0][1])) < tol
+    with State(n, precision) as st:
+        with pytest.raises(Exception):
+            st.set_tile_qubits(3)

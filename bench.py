@@ -303,7 +303,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from suqa_gb300 import State
-    from suqa_gb300.workloads import algorithmic_bytes, apply_circuit, random_circuit, random_state
+    from suqa_gb300.workloads import algorithmic_bytes, apply_circuit, fp64_instructions, random_circuit, random_state
 
     n = args.n
     bpa = 16 if args.precision == "f64" else 8
@@ -394,6 +394,19 @@ def main():
     except Exception:
         pass
 
+    # FP64 fused multiply-add rate of the CUDA cores (the pass kernel's own pipe;
+    # DGEMM above runs on the FP64 tensor path)
+    fma_gops = None
+    try:
+        import ctypes
+        from suqa_gb300 import _lib
+        g = ctypes.c_double()
+        if _lib.load().sq_fp64_fma_rate(ctypes.byref(g), None) == 0:
+            fma_gops = g.value
+    except Exception:
+        pass
+    fp64_ins = fp64_instructions(gates, n) * args.steps if args.precision == "f64" else None
+
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -411,7 +424,14 @@ def main():
                 "fp64_tflops_achieved": stats["flops"] / (kms / 1e3) / 1e12 if kms > 0 else None,
                 "fp64_tflops_peak": fp64_peak,
                 "fp64_frac": (stats["flops"] / (kms / 1e3) / 1e12 / fp64_peak) if (kms > 0 and fp64_peak) else None,
-                "fp64_peak_source": "cuBLAS DGEMM 8192^3 measured in this run"}
+                "fp64_peak_source": "cuBLAS DGEMM 8192^3 measured in this run",
+                "fp64_pipe": {"instructions_per_step": fp64_ins / args.steps if fp64_ins else None,
+                              "achieved_gops": (fp64_ins / (kms / 1e3) / 1e9) if (fp64_ins and kms > 0) else None,
+                              "peak_gops": fma_gops,
+                              "frac": (fp64_ins / (kms / 1e3) / 1e9 / fma_gops) if (fp64_ins and kms > 0 and fma_gops)
+                              else None,
+                              "peak_source": "sq_fp64_fma_rate: independent DFMA chains on every SM, measured in "
+                                             "this run (of measured)"}}
 
     # secondary: the same circuit with FP32 amplitudes (FP64 reductions)
     fp32_line = None

@@ -134,6 +134,9 @@ typedef struct sq_stats {
                               Pauli rotation on the amplitudes it touches, 0 for X/CX/MCX/SWAP) */
 } sq_stats;
 int sq_get_stats(const sq_state* s, sq_stats* out);
+/* FP64 fused multiply-add rate of the current device's CUDA cores (independent
+ * chains on every SM), in G operations/s: the ceiling of the FP64 tile pass. */
+int sq_fp64_fma_rate(double* gops, float* kernel_ms);
 int sq_reset_stats(sq_state* s);
 /* Kernel timing: when enabled, every pass launch is bracketed by CUDA events on
  * the state's stream; sq_kernel_time() synchronizes and returns the summed

@@ -95,3 +95,13 @@ def algorithmic_bytes(gates, n: int, bytes_per_amp: int) -> int:
             f = 1.0
         tot += 2.0 * bytes_per_amp * N * f
     return int(tot)
+
+
+def fp64_instructions(gates, n: int) -> int:
+    """FP64 instructions the tile pass needs for an uncontrolled circuit of the
+    benchmark's gate set, per amplitude: H 2 (sum and difference, 1/sqrt2 in the
+    global scale), U1 4 on the half it phases, a Pauli rotation 2 (one fused
+    multiply-add per component, c or s in the global scale), X/CX/MCX 0, a
+    measurement 2 (the squared-magnitude reduction; the collapse is a select)."""
+    cost = {"h": 2, "u1": 2, "ptp": 2, "measure": 2}
+    return sum(cost.get(g[0], 0) for g in gates) * (1 << n)

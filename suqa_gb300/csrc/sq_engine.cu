@@ -4,6 +4,7 @@
 #include "sq_pass.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -106,8 +107,8 @@ size_t tile_smem(const sq_state* s, int K, int L) {
 
 template <typename T>
 int launch_pass_t(sq_state* s, const sqk::PassArgs& a, const sqk::Prog& p, int grid, int block, size_t smem) {
-    static int configured_smem = -1;
-    if ((int)smem > 48 * 1024 && configured_smem < (int)smem) {
+    static std::atomic<int> configured_smem{-1};  // states may run in several host threads
+    if ((int)smem > 48 * 1024 && configured_smem.load() < (int)smem) {
         int optin = 0;
         cudaFuncAttributes fa;
         SQ_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));

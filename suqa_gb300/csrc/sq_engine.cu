@@ -72,6 +72,7 @@ struct sq_state {
     double gscale = 1.0;
     int nsm = 1;
     int max_grid = 1;
+    std::vector<std::pair<uint64_t, int>> occ_cache;  // (block << 32 | smem) -> resident CTAs per SM
     int kp = 0;                     // default tile size for this state
     sq_stats stats{};
     int device = 0;
@@ -105,8 +106,9 @@ size_t tile_smem(const sq_state* s, int K, int L) {
     return (size_t)2 * ((size_t)1 << K) * s->esz + (size_t)8 * ((size_t)1 << (K - L));
 }
 
+// Opts the pass kernel into the shared memory a tile needs (above the default 48 KiB).
 template <typename T>
-int launch_pass_t(sq_state* s, const sqk::PassArgs& a, const sqk::Prog& p, int grid, int block, size_t smem) {
+int configure_smem(sq_state* s, size_t smem) {
     static std::atomic<int> configured_smem{-1};  // states may run in several host threads
     if ((int)smem > 48 * 1024 && configured_smem.load() < (int)smem) {
         int optin = 0;
@@ -118,6 +120,33 @@ int launch_pass_t(sq_state* s, const sqk::PassArgs& a, const sqk::Prog& p, int g
         SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
         configured_smem = dyn;
     }
+    return SQ_OK;
+}
+
+// CTAs of the pass kernel resident per SM at this block and tile size (cached per
+// state): a pass launches one full wave, every CTA looping over an equal share of
+// the tiles, so no partial last wave leaves SMs idle.
+template <typename T>
+int resident_ctas(sq_state* s, int block, size_t smem, int* out) {
+    const uint64_t key = ((uint64_t)block << 32) | (uint64_t)smem;
+    for (const auto& kv : s->occ_cache)
+        if (kv.first == key) {
+            *out = kv.second;
+            return SQ_OK;
+        }
+    int rc = configure_smem<T>(s, smem);
+    if (rc) return rc;
+    int occ = 0;
+    SQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sqk::k_pass<T>, block, smem));
+    s->occ_cache.emplace_back(key, occ);
+    *out = occ;
+    return SQ_OK;
+}
+
+template <typename T>
+int launch_pass_t(sq_state* s, const sqk::PassArgs& a, const sqk::Prog& p, int grid, int block, size_t smem) {
+    int rc = configure_smem<T>(s, smem);
+    if (rc) return rc;
     sqk::k_pass<T><<<grid, block, smem, s->stream>>>(a, p);
     SQ_CUDA(cudaGetLastError());
     return SQ_OK;
@@ -254,9 +283,16 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     p.defer = p.defer >= 2 ? 1 : 0;  // deferring one factor costs as much as it saves
     const bool single = (K == n);
     const int block = single ? (K >= 10 ? 1024 : (K >= 8 ? 256 : 128)) : 256;
-    int grid = (int)std::min<uint64_t>(a.ntiles, (uint64_t)s->max_grid);
-    if (grid < 1) grid = 1;
     const size_t smem = tile_smem(s, K, L);
+    int occ = 0;
+    {
+        const int orc = s->prec == SQ_F64 ? resident_ctas<double>(s, block, smem, &occ)
+                                          : resident_ctas<float>(s, block, smem, &occ);
+        if (orc) return orc;
+    }
+    const uint64_t wave = occ > 0 ? (uint64_t)s->nsm * (uint64_t)occ : (uint64_t)s->max_grid;
+    int grid = (int)std::min<uint64_t>(a.ntiles, std::min<uint64_t>(wave, (uint64_t)s->max_grid));
+    if (grid < 1) grid = 1;
     const uint64_t moved = a.ntiles * ((uint64_t)1 << K) * 2ull * s->esz * (a.store ? 2ull : 1ull);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (s->timing) {

@@ -208,7 +208,7 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     a.ntiles = 1ull << popc(a.ofree);
 
     static thread_local sqk::Prog p;
-    p.nops = (int)(i1 - i0);
+    p.nops = 0;
     p.red = red;
     p.defer = 0;
     p.rmask = rmask;
@@ -222,10 +222,28 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     }
     p.orm = rmask & outer;
     p.orv = rval & p.orm;
+    // Index frame: an uncontrolled X on one tile qubit moves no data.  The pass
+    // records it in xm (physical element t holds logical t ^ xm), later ops are
+    // rewritten for the frame (control values, H / Y pair roles, Pauli sign
+    // parity, collapse and reduction conditions) and the store writes every
+    // element back to its logical position.  Passes with table ops (W, phase
+    // lists: index-valued lookups) keep xm = 0.
+    bool frame_ok = true;
+    for (size_t i = i0; i < i1; ++i)
+        if (ops[i].kind == sqk::OP_W || ops[i].kind == sqk::OP_PLIST) frame_ok = false;
+    uint32_t xm = 0;       // tile-local frame
+    uint64_t xg = 0;       // the same in global qubit positions
     uint32_t tabpos = 0;
     for (size_t i = i0; i < i1; ++i) {
         const HostOp& h = ops[i];
-        sqk::Op& o = p.ops[i - i0];
+        if (frame_ok && h.kind == sqk::OP_SWAPP && h.cmask == 0ull && popc(h.flip) == 1) {
+            const int lb = local_of(__builtin_ctzll(h.flip));
+            if (lb < 0) return fail(SQ_ERR_UNSUPPORTED, "internal: gate qubit outside the pass tile");
+            xm ^= 1u << lb;
+            xg ^= h.flip;
+            continue;
+        }
+        sqk::Op& o = p.ops[p.nops++];
         std::memset(&o, 0, sizeof(o));
         o.kind = h.kind;
         o.ny = h.ny;
@@ -250,12 +268,15 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
             if ((h.zy >> b) & 1ull) lzy |= 1u << lb;
         }
         o.lcm = lcm;
-        o.lcv = lcv;
+        // the pair's first physical element is the logical second one when the
+        // frame flips the pair bit; a control bit inside the flip (SWAP) then flips too
+        o.orient = (uint8_t)(lf ? ((xm >> o.lpair) & 1u) : 0u);
+        o.lcv = lcv ^ (xm & lcm) ^ (o.orient ? (lf & lcm) : 0u);
         o.gdefer = h.gdefer;
         if ((h.kind == sqk::OP_HP || h.kind == sqk::OP_PAULI) && lcm == 0u && !h.gdefer) p.defer++;
         o.lzy = (h.kind == sqk::OP_PAULI) ? lzy : 0u;
         o.cmask = h.cmask;
-        o.cval = h.cval;
+        o.cval = h.cval ^ (xg & h.cmask);
         o.ocm = h.skm & outer;
         o.ocv = h.skv & o.ocm;
         // Pauli: the kernel takes the outer part of the sign parity per tile
@@ -273,6 +294,7 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         o.fsn = (float)o.sn;
         o.fu = (float)o.u;
         o.fun = (float)o.un;
+        o.xpar = (uint8_t)(h.kind == sqk::OP_PAULI ? (popc(xm & o.lzy) & 1) : 0);
         if (!h.tab.empty()) {
             o.tab = tabpos;
             std::memcpy(&p.tab[2 * tabpos], h.tab.data(), h.tab.size() * sizeof(double));
@@ -280,6 +302,9 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         }
     }
 
+    p.xm = xm;
+    p.rswap = (red == 1 && (xm & p.lrm)) ? 1 : 0;
+    if (red == 2) p.lrv ^= xm & p.lrm;
     p.defer = p.defer >= 2 ? 1 : 0;  // deferring one factor costs as much as it saves
     const bool single = (K == n);
     const int block = single ? (K >= 10 ? 1024 : (K >= 8 ? 256 : 128)) : 256;

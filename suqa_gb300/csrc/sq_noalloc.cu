@@ -130,6 +130,8 @@ extern "C" int sq_qubit_probs_noalloc(const void* re, const void* im, uint32_t n
     p.lrv = 0u;
     p.orm = q < (uint32_t)K ? 0ull : (1ull << q);
     p.orv = 0ull;
+    p.xm = 0u;
+    p.rswap = 0;
     const int block = (K == (int)n) ? (K >= 10 ? 1024 : (K >= 8 ? 256 : 128)) : 256;
     const size_t esz = precision == SQ_F64 ? 8 : 4;
     const size_t smem = 2 * ((size_t)1 << K) * esz + 8;

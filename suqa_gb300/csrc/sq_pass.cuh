@@ -46,7 +46,9 @@ struct Op {
     uint8_t ny;      // Pauli: number of Y factors
     uint8_t fz;      // Pauli: parity of (flip & zy)
     uint8_t cbig;    // deferred rotation: |c| >= |s| (the factor c is deferred, else s)
-    uint8_t pad8[3];
+    uint8_t orient;  // H / Y: the pass's index frame swaps the pair's logical roles
+    uint8_t xpar;    // Pauli: parity the index frame adds to every element's sign
+    uint8_t pad8;
     uint32_t lflip;  // tile-local flip mask
     uint32_t lcm, lcv;     // tile-local control condition
     uint32_t lzy;          // tile-local Y|Z mask (Pauli signs)
@@ -68,6 +70,9 @@ struct Prog {
     uint64_t rmask, rval;
     uint32_t lrm, lrv;   // tile-local part of rmask / rval
     uint64_t orm, orv;   // part outside the tile
+    uint32_t xm;         // index frame at the end of the pass: uncontrolled X gates on tile
+                         // qubits move no data; physical element t holds logical t ^ xm
+    int rswap;           // the frame flips the measured qubit: swap the two sums
     Op ops[kMaxOps];
     double tab[2 * kMaxTab];
 };
@@ -154,6 +159,25 @@ __device__ __forceinline__ double add_sq(double part, double r, double i) { retu
 __device__ __forceinline__ double add_sq(double part, float r, float i) { return part + (double)fmaf(r, r, i * i); }
 
 __device__ __forceinline__ void scale_vec(double2& v, double s) { v.x *= s; v.y *= s; }
+
+// element e of the vector becomes element e ^ x (x < vector width)
+__device__ __forceinline__ void permute_vec(double2& v, uint32_t x) {
+    if (x & 1u) {
+        const double t = v.x;
+        v.x = v.y;
+        v.y = t;
+    }
+}
+__device__ __forceinline__ void permute_vec(float4& v, uint32_t x) {
+    if (x & 1u) {
+        float t = v.x; v.x = v.y; v.y = t;
+        t = v.z; v.z = v.w; v.w = t;
+    }
+    if (x & 2u) {
+        float t = v.x; v.x = v.z; v.z = t;
+        t = v.y; v.y = v.w; v.w = t;
+    }
+}
 __device__ __forceinline__ void scale_vec(float4& v, float s) { v.x *= s; v.y *= s; v.z *= s; v.w *= s; }
 
 template <typename T>
@@ -216,7 +240,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                 f ^= b;
             }
         }
-        bool any = p.red != 0;
+        bool any = p.red != 0 || p.xm != 0u;  // a frame permutes every tile
         for (int k = 0; k < p.nops && !any; ++k)
             any = (base & p.ops[k].ocm) == p.ops[k].ocv;
         if (!any) continue;  // uniform over the CTA
@@ -272,34 +296,43 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                     }
                 } else if (kind == OP_YP) {
                     // include/suqa_cpu.hpp:96-122: a1' = i a0, a0' = -i a1
+                    const bool ori = op.orient != 0;  // logical roles swapped: Y negated
                     for (uint32_t u = threadIdx.x; u < npair; u += blockDim.x) {
                         const uint32_t t0 = deposit_zeros(u, sel) | lcv, t1 = t0 ^ lf;
                         const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
-                        sre[t1] = -a0i; sim[t1] = a0r; sre[t0] = a1i; sim[t0] = -a1r;
+                        sre[t1] = neg_if(-a0i, ori); sim[t1] = neg_if(a0r, ori);
+                        sre[t0] = neg_if(a1i, ori); sim[t0] = neg_if(-a1r, ori);
                     }
                 } else if (kind == OP_HP) {
                     // include/suqa_cpu.hpp:150-206
                     if (lcm == 0u && (op.gdefer || p.defer)) {
+                        const bool ori = op.orient != 0;
                         for (uint32_t pp = threadIdx.x; pp < TS / 2; pp += blockDim.x) {
                             const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
                             const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
-                            sre[t0] = a0r + a1r; sim[t0] = a0i + a1i;
-                            sre[t1] = a0r - a1r; sim[t1] = a0i - a1i;
+                            // logical (first, second) = (t0, t1), or (t1, t0) when oriented
+                            const T sr = a0r + a1r, si = a0i + a1i;
+                            const T dr = neg_if(a0r - a1r, ori), di = neg_if(a0i - a1i, ori);
+                            sre[ori ? t1 : t0] = sr; sim[ori ? t1 : t0] = si;
+                            sre[ori ? t0 : t1] = dr; sim[ori ? t0 : t1] = di;
                         }
                         if (!op.gdefer) sigma *= 0.7071067811865475;
                     } else {
                         const T h = (T)0.7071067811865475;
+                        const bool ori = op.orient != 0;
                         for (uint32_t u = threadIdx.x; u < npair; u += blockDim.x) {
                             const uint32_t t0 = deposit_zeros(u, sel) | lcv, t1 = t0 ^ lf;
                             const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
-                            sre[t0] = h * (a0r + a1r); sim[t0] = h * (a0i + a1i);
-                            sre[t1] = h * (a0r - a1r); sim[t1] = h * (a0i - a1i);
+                            const T sr = h * (a0r + a1r), si = h * (a0i + a1i);
+                            const T dr = neg_if(h * (a0r - a1r), ori), di = neg_if(h * (a0i - a1i), ori);
+                            sre[ori ? t1 : t0] = sr; sim[ori ? t1 : t0] = si;
+                            sre[ori ? t0 : t1] = dr; sim[ori ? t0 : t1] = di;
                         }
                     }
                 } else if (kind == OP_PAULI) {
                     // exp(i th P): a0' = c a0 + i s w(g1) a1, a1' = c a1 + i s w(g0) a0,
                     // w(g) = i^ny (-1)^parity(g & zy); the outer part of the parity is per tile
-                    const int tpar = parity64(base & op.zy);
+                    const int tpar = parity64(base & op.zy) ^ op.xpar;
                     const uint32_t lzy = op.lzy;
                     const int ny = op.ny, fz = op.fz;
                     if (lcm == 0u && (op.gdefer || p.defer)) {
@@ -351,7 +384,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                     sim[t] = ai * c + ar * s;
                 }
             } else if (kind == OP_PAULI) {  // all-Z string: diagonal c + i s (-1)^parity
-                const int tpar = parity64(base & op.zy);
+                const int tpar = parity64(base & op.zy) ^ op.xpar;
                 const uint32_t lzy = op.lzy;
                 if (lcm == 0u && (op.gdefer || p.defer)) {
                     const bool cbig = op.cbig != 0;
@@ -441,12 +474,19 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
         }
         if (a.store) {
             const bool scaled = sigma != 1.0;
+            const uint32_t xm = p.xm;
             if ((1u << L) >= (uint32_t)W) {
+                const uint32_t xv = xm & ~(uint32_t)(W - 1), xe = xm & (uint32_t)(W - 1);
                 for (uint32_t v = threadIdx.x; v < TS / W; v += blockDim.x) {
                     const uint32_t t = v * W;
                     const uint64_t g = base | offs[t >> L] | (t & lowmask);
-                    V vr = *reinterpret_cast<const V*>(sre + t);
-                    V vi = *reinterpret_cast<const V*>(sim + t);
+                    // logical element t is the physical element t ^ xm
+                    V vr = *reinterpret_cast<const V*>(sre + (t ^ xv));
+                    V vi = *reinterpret_cast<const V*>(sim + (t ^ xv));
+                    if (xe) {
+                        permute_vec(vr, xe);
+                        permute_vec(vi, xe);
+                    }
                     if (scaled) {
                         scale_vec(vr, sg);
                         scale_vec(vi, sg);
@@ -457,8 +497,8 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
             } else {
                 for (uint32_t t = threadIdx.x; t < TS; t += blockDim.x) {
                     const uint64_t g = base | offs[t >> L] | (t & lowmask);
-                    gre[g] = sre[t] * sg;
-                    gim[g] = sim[t] * sg;
+                    gre[g] = sre[t ^ xm] * sg;
+                    gim[g] = sim[t ^ xm] * sg;
                 }
             }
         }
@@ -466,6 +506,11 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
     }
 
     if (!p.red) return;
+    if (p.rswap) {
+        const double t = acc0;
+        acc0 = acc1;
+        acc1 = t;
+    }
     // ---- deterministic two-level reduction: per-CTA partials, last CTA sums them
     block_reduce2<T>(acc0, acc1, red_sh);
     if (threadIdx.x == 0) {

@@ -310,7 +310,11 @@ def main():
     dt_np = np.float64 if args.precision == "f64" else np.float32
     gates = random_circuit(n, args.gates, seed=7)
     alg = algorithmic_bytes(gates, n, bpa)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the states run on it and the CUDA events are recorded on
+    # it (the legacy default stream's handle is 0, which libsq reads as "the
+    # state's own stream")
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     st = State(n, args.precision)
     st.set_stream(stream.cuda_stream)
     st.set_fusion(not args.no_fusion)

@@ -141,7 +141,9 @@ class State:
         return ms.value, n.value, b.value
 
     def set_stream(self, cuda_stream: int | None):
-        """Run on a caller's CUDA stream (e.g. torch.cuda.current_stream().cuda_stream)."""
+        """Run on a caller's CUDA stream, e.g. torch.cuda.Stream().cuda_stream.  A handle
+        of 0 or None (also what the legacy default stream reports) selects the state's
+        own non-blocking stream, which does not order with the default stream."""
         check(self.L.sq_set_stream(self.h, C.c_void_p(cuda_stream) if cuda_stream else None))
 
     # -- single-qubit gates (src/suqa.cu:115-285) ------------------------------------

@@ -96,12 +96,13 @@ __device__ __forceinline__ double pcg_doub(uint64_t& st, uint64_t inc) {
     return __longlong_as_double((long long)bits) - 1.0;
 }
 
-// qsa::draw_C (qsa.cuh:334-343) with weight sums (i+1)/s
+// qsa::draw_C (qsa.cuh:334-343) with weight sums (i+1)/s.  The last sum is exactly
+// 1 and u < 1, so the loop always returns; the fallback keeps C a valid spin.
 __device__ __forceinline__ uint32_t draw_move(uint64_t& st, uint64_t inc, int s) {
     const double u = pcg_doub(st, inc);
     for (int i = 0; i < s; ++i)
         if (u < (double)(i + 1) / (double)s) return (uint32_t)i;
-    return (uint32_t)s;
+    return (uint32_t)(s - 1);
 }
 
 // register slot of orbit coordinates (a: x ^= d', b: x ^= e_C, c: d ^= e_C, acc)

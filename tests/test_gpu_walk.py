@@ -104,3 +104,16 @@ def test_walk_results_do_not_depend_on_the_batch_split():
         for k, row in zip(k2, a2):
             tot[keys.index(k)] += row
     assert np.allclose(tot, acc, rtol=0, atol=1e-9)
+
+
+def test_twelve_spin_rings_at_the_size_limit():
+    """The largest rings the entry point takes (12 spins, 2^25 amplitudes per
+    walk): FP32 and FP64 take the same steps and readouts."""
+    from suqa_gb300.walk import ising_ring_walks, run_qsa_walks
+    walks = ising_ring_walks(3, 12, 1.0, 2, 2, 4, seed=12)
+    r64, _ = run_qsa_walks(walks, "f64", trace=True)
+    r32, _ = run_qsa_walks(walks, "f32", trace=True)
+    for a, b in zip(r32, r64):
+        assert (a.done, a.restarts, a.steps, a.readout) == (b.done, b.restarts, b.steps, b.readout)
+        assert np.max(np.abs(a.p0 - b.p0)) < 1e-4
+        assert b.done and abs(b.E) <= 12 and 0 <= b.absM <= 12

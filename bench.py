@@ -468,6 +468,8 @@ def main():
                 "fp64_tflops_peak": fp64_peak,
                 "fp64_frac": (stats["flops"] / (kms / 1e3) / 1e12 / fp64_peak) if (kms > 0 and fp64_peak) else None,
                 "fp64_peak_source": "cuBLAS DGEMM 8192^3 measured in this run",
+                "limiter": ("the FP64 CUDA-core pipe (fp64_pipe below; HBM traffic is a small fraction)"
+                            if args.precision == "f64" else "shared-memory sweeps (issue-bound)"),
                 "fp64_pipe": {"instructions_per_step": fp64_ins / args.steps if fp64_ins else None,
                               "achieved_gops": (fp64_ins / (kms / 1e3) / 1e9) if (fp64_ins and kms > 0) else None,
                               "peak_gops": fma_gops,

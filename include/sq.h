@@ -273,7 +273,9 @@ typedef struct sq_qsa_walk {
     uint32_t steps_per_stage; /* walk steps at each temperature */
     uint32_t max_steps;       /* cap on steps over all attempts (0: 8 x stages x steps_per_stage) */
     int32_t J[12];            /* bond couplings, bond i joins spins i and i+1 mod s; -8..8 */
-    uint32_t pad;
+    uint32_t algo;            /* 0: iterate W per orbit; 1: per orbit class (W, eigenvectors of
+                                 (W + W^T)/2, sum of powers), at most 96 classes per move;
+                                 one value for the whole batch */
     double beta;              /* final inverse temperature */
     uint64_t seed;            /* PCG32 seed (pcg32::seed(seed, 1)) */
 } sq_qsa_walk;

@@ -49,7 +49,7 @@ class SqTfimEvolution(C.Structure):
 class SqQsaWalk(C.Structure):
     _fields_ = [("spins", C.c_uint32), ("phase_qbits", C.c_uint32), ("stages", C.c_uint32),
                 ("steps_per_stage", C.c_uint32), ("max_steps", C.c_uint32), ("J", C.c_int32 * 12),
-                ("pad", C.c_uint32), ("beta", C.c_double), ("seed", C.c_uint64)]
+                ("algo", C.c_uint32), ("beta", C.c_double), ("seed", C.c_uint64)]
 
 
 class SqQsaWalkResult(C.Structure):

@@ -33,6 +33,7 @@
 #include <cmath>
 #include <cstdint>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "sq.h"
@@ -477,19 +478,424 @@ k_walk_step(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Orbit classes (algo 1).  W on an orbit depends only on the energy differences
+// at its four a = 0 positions (the a = 1 ones are their negatives), and a step
+// has few distinct such signatures (62-69 among 131,328 orbits of a 10-spin
+// ring).  Per class: W (16 x 16), A = (W + W^T)/2 = V diag(lambda) V^T,
+// Q = sum_{k<L} W^k and d_{k,i} = v_i^T W^k v_i.  W is real orthogonal, so
+// <psi, W^k psi> = psi^T T_k(A) psi (T_k: Chebyshev) and T_k(lambda_i) = d_{k,i}:
+// an orbit adds the 16 values (V^T psi)_i^2 to its class, g_k = sum_{c,i} N_{c,i}
+// d_{c,k,i}, and the state after reading zero is Q psi per orbit.  The d table
+// comes from the powers of W themselves (errors grow with k, not with k^2 as
+// T_k(lambda) evaluated from an approximate lambda would).
+
+constexpr int kMaxCls = 96;
+constexpr int kClsOrbitsPerThread = 32;
+constexpr int kClsOrbitsPerCta = kThreads * kClsOrbitsPerThread;
+constexpr int kClsStride = 16 * 16 + 16 * 16 + kMaxL * 16;  // V^T, Q, d[k][i]
+constexpr int kMaxMoves = 12;
+
+__device__ __forceinline__ bool orbit_decode(uint32_t o, int s, int C, uint32_t& dp, uint32_t& x0) {
+    const uint32_t nb = 1u << (s - 1);
+    if (o < nb) {
+        dp = 0;
+        x0 = ins0(o, C);
+        return true;
+    }
+    const uint32_t o2 = o - nb;
+    const uint32_t di = 1u + (o2 >> (s - 2)), ri = o2 & ((1u << (s - 2)) - 1u);
+    dp = ins0(di, C);
+    const int p = __ffs((int)dp) - 1;
+    x0 = ins0(ins0(ri, min(p, C)), max(p, C));
+    return false;
+}
+
+// signature key: dE at positions (a, b, c) = (0, 0, 0), (0, 1, 0), (0, 0, 1), (0, 1, 1),
+// each + 256 in 9 bits (never 0)
+__device__ __forceinline__ uint64_t orbit_key(const int* E, uint32_t x0, uint32_t dp, uint32_t eC) {
+    uint64_t key = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t x = x0 ^ ((j & 1) ? eC : 0u);
+        const uint32_t d = dp ^ ((j & 2) ? eC : 0u);
+        key |= (uint64_t)(E[x ^ d] - E[x] + 256) << (9 * j);
+    }
+    return key;
+}
+
+// One CTA per (walk, move): the sorted distinct keys of the walk's orbits for that move.
+__global__ void k_cls_keys(const WalkDev* __restrict__ walks, const int* __restrict__ energies,
+                           const int* __restrict__ job_walk, const int* __restrict__ job_move,
+                           unsigned long long* __restrict__ keys, uint32_t* __restrict__ ncls) {
+    const int w = job_walk[blockIdx.x], C = job_move[blockIdx.x];
+    const WalkDev& W = walks[w];
+    __shared__ unsigned long long table[512];
+    __shared__ unsigned long long arr[512];
+    __shared__ unsigned int count, overflow;
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) table[i] = 0ull;
+    if (threadIdx.x == 0) {
+        count = 0;
+        overflow = 0;
+    }
+    __syncthreads();
+    const int s = W.s;
+    const uint32_t norb = norbits(s), eC = 1u << C;
+    const int* E = energies + W.e_off;
+    for (uint32_t o = threadIdx.x; o < norb; o += blockDim.x) {
+        uint32_t dp, x0;
+        orbit_decode(o, s, C, dp, x0);
+        const unsigned long long key = orbit_key(E, x0, dp, eC);
+        uint32_t h = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> 55);
+        bool done = false;
+        for (int probe = 0; probe < 512 && !done; ++probe) {  // bounded: 512 slots
+            const unsigned long long prev = atomicCAS(&table[h], 0ull, key);
+            if (prev == 0ull || prev == key) done = true;
+            h = (h + 1u) & 511u;
+        }
+        if (!done) overflow = 1;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 512; i += blockDim.x)
+        if (table[i] != 0ull) arr[atomicAdd(&count, 1u)] = table[i];
+    __syncthreads();
+    const uint32_t n = count;
+    unsigned long long* out = keys + ((uint64_t)w * kMaxMoves + C) * kMaxCls;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        uint32_t rank = 0;
+        for (uint32_t j = 0; j < n; ++j) rank += arr[j] < arr[i] ? 1u : 0u;
+        if (rank < (uint32_t)kMaxCls) out[rank] = arr[i];
+    }
+    if (threadIdx.x == 0) ncls[(uint64_t)w * kMaxMoves + C] = overflow ? 0xffffffffu : n;
+}
+
+// 16 x 16 product by one warp: Z = X Y (row-major, padded rows of 17); each lane
+// computes 8 entries of one row
+template <typename T>
+__device__ __forceinline__ void warp_matmul(T (*Z)[17], const T (*X)[17], const T (*Y)[17], int lane) {
+    const int row = lane >> 1, c0 = (lane & 1) * 8;
+    T acc[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] = (T)0;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+        const T xv = X[row][m];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[j] += xv * Y[m][c0 + j];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 8; ++j) Z[row][c0 + j] = acc[j];
+    __syncwarp();
+}
+
+// Per walk, one warp per class of the current move: W, the eigen-decomposition of
+// A = (W + W^T)/2 (cyclic Jacobi) and Q.
+constexpr int kPrepThreads = 512;
+
+template <typename T>
+__global__ void __launch_bounds__(kPrepThreads) k_cls_prep(const WalkDev* __restrict__ walks, const WalkRec* __restrict__ recs,
+                                                      const unsigned long long* __restrict__ keys,
+                                                      const uint32_t* __restrict__ ncls, T* __restrict__ cls) {
+    const int w = blockIdx.x;
+    const WalkDev& W = walks[w];
+    const WalkRec& R = recs[w];
+    if (R.status != 0) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    typedef T Mat[16][17];
+    Mat* mats = reinterpret_cast<Mat*>(smem_raw);  // per warp: Wp, A (then U), V, Q, tmp
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T(*Wp)[17] = mats[warp * 5 + 0];
+    T(*A)[17] = mats[warp * 5 + 1];
+    T(*V)[17] = mats[warp * 5 + 2];
+    T(*Q)[17] = mats[warp * 5 + 3];
+    T(*Tm)[17] = mats[warp * 5 + 4];
+    const int C = (int)R.C, q = W.q;
+    const uint32_t nc = ncls[(uint64_t)w * kMaxMoves + C];
+    const unsigned long long* kk = keys + ((uint64_t)w * kMaxMoves + C) * kMaxCls;
+    for (uint32_t c = warp; c < nc; c += kPrepThreads / 32) {
+        const unsigned long long key = kk[c];
+        int dE0[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) dE0[j] = (int)((key >> (9 * j)) & 511ull) - 256;
+        T ce[8], cr[8];
+        uint32_t zmask = 0;
+#pragma unroll
+        for (int pos = 0; pos < 8; ++pos) {
+            const int a = pos >> 2, b = (pos >> 1) & 1, cc = pos & 1;
+            // a = 1 positions are the swap partners of (0, b ^ c, c): negated differences
+            const int dE = a == 0 ? dE0[b + 2 * cc] : -dE0[(b ^ cc) + 2 * cc];
+            double e = 1.0, r = 0.0;
+            if (dE > 0) {
+                e = exp(-0.5 * R.beta_k * (double)dE);
+                r = sqrt(1.0 - e * e);
+            }
+            ce[pos] = (T)e;
+            cr[pos] = (T)r;
+            if (dE == 0) zmask |= 1u << pos;
+        }
+        // W column by column: W applied to the unit vectors
+        if (lane < 16) {
+            Orbit<T> ob;
+            ob.setup(ce, cr, zmask);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) ob.v[j] = j == lane ? (T)1 : (T)0;
+            ob.walk();
+#pragma unroll
+            for (int i = 0; i < 16; ++i) Wp[i][lane] = ob.v[i];
+        }
+        __syncwarp();
+        for (int idx = lane; idx < 256; idx += 32) {
+            const int i = idx >> 4, j = idx & 15;
+            A[i][j] = (T)0.5 * (Wp[i][j] + Wp[j][i]);
+            V[i][j] = i == j ? (T)1 : (T)0;
+        }
+        __syncwarp();
+        // cyclic Jacobi: A' = J^T A J zeroes A[p][q]; V' = V J; stops when the
+        // off-diagonal mass is at rounding level (at most 10 sweeps)
+        const T tol = sizeof(T) == 8 ? (T)1e-28 : (T)1e-12;
+        for (int sweep = 0; sweep < 10; ++sweep) {
+            T off = (T)0;
+            for (int idx = lane; idx < 256; idx += 32) {
+                const int i = idx >> 4, j = idx & 15;
+                if (i < j) off += A[i][j] * A[i][j];
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) off += __shfl_xor_sync(0xffffffffu, off, o);
+            if (off < tol) break;  // uniform over the warp
+            for (int p = 0; p < 15; ++p) {
+                for (int qq = p + 1; qq < 16; ++qq) {
+                    const T apq = A[p][qq];
+                    if (fabs((double)apq) < 1e-300) continue;  // uniform: every lane reads the same value
+                    const T app = A[p][p], aqq = A[qq][qq];
+                    const T tau = (aqq - app) / ((T)2 * apq);
+                    const T t = (tau >= (T)0 ? (T)1 : (T)-1) / (fabs(tau) + sqrt((T)1 + tau * tau));
+                    const T c1 = (T)1 / sqrt((T)1 + t * t), s1 = t * c1;
+                    __syncwarp();
+                    if (lane < 16) {
+                        const T akp = A[lane][p], akq = A[lane][qq];
+                        A[lane][p] = c1 * akp - s1 * akq;
+                        A[lane][qq] = s1 * akp + c1 * akq;
+                    }
+                    __syncwarp();
+                    if (lane < 16) {
+                        const T apk = A[p][lane], aqk = A[qq][lane];
+                        A[p][lane] = c1 * apk - s1 * aqk;
+                        A[qq][lane] = s1 * apk + c1 * aqk;
+                        const T vkp = V[lane][p], vkq = V[lane][qq];
+                        V[lane][p] = c1 * vkp - s1 * vkq;
+                        V[lane][qq] = s1 * vkp + c1 * vkq;
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+        // d[k][i] = v_i^T U_k with U_k = W U_{k-1} = W^k V (A is free again: it holds U)
+        T* out = cls + ((uint64_t)w * kMaxCls + c) * kClsStride;
+        T(*U)[17] = A;
+        for (int idx = lane; idx < 256; idx += 32) U[idx >> 4][idx & 15] = V[idx >> 4][idx & 15];
+        if (lane < 16) out[512 + lane] = (T)1;  // d[0][i] = |v_i|^2 = 1
+        __syncwarp();
+        for (int k = 1; k < (1 << q); ++k) {
+            warp_matmul<T>(Tm, Wp, U, lane);  // U_k = W U_{k-1}
+            for (int idx = lane; idx < 256; idx += 32) U[idx >> 4][idx & 15] = Tm[idx >> 4][idx & 15];
+            __syncwarp();
+            if (lane < 16) {
+                T dk = (T)0;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) dk += V[j][lane] * U[j][lane];
+                out[512 + k * 16 + lane] = dk;
+            }
+            __syncwarp();
+        }
+        // Q = sum_{k<L} W^k = prod_{j<q} (I + W^(2^j)); Wp becomes the running square
+        for (int idx = lane; idx < 256; idx += 32) {
+            const int i = idx >> 4, j = idx & 15;
+            Q[i][j] = Wp[i][j] + (i == j ? (T)1 : (T)0);
+        }
+        __syncwarp();
+        for (int j = 1; j < q; ++j) {
+            warp_matmul<T>(Tm, Wp, Wp, lane);
+            for (int idx = lane; idx < 256; idx += 32) Wp[idx >> 4][idx & 15] = Tm[idx >> 4][idx & 15];
+            __syncwarp();
+            warp_matmul<T>(Tm, Q, Wp, lane);
+            for (int idx = lane; idx < 256; idx += 32) Q[idx >> 4][idx & 15] += Tm[idx >> 4][idx & 15];
+            __syncwarp();
+        }
+        for (int idx = lane; idx < 256; idx += 32) {
+            const int i = idx >> 4, j = idx & 15;
+            out[idx] = V[j][i];  // V^T, row i = eigenvector i
+            out[256 + idx] = Q[i][j];
+        }
+        __syncwarp();
+    }
+}
+
+// Orbit pass of algo 1: per orbit its class, y = V^T psi, the class sums of
+// y_i^2 (per warp, in a fixed order), S = Q psi written back.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_walk_step_cls(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
+                                                           const WalkRec* __restrict__ recs, const int* __restrict__ energies,
+                                                           const unsigned long long* __restrict__ keys,
+                                                           const uint32_t* __restrict__ ncls, const T* __restrict__ cls,
+                                                           T* __restrict__ states, double* __restrict__ npart) {
+    const int w = cta_walk[blockIdx.x];
+    const WalkDev& W = walks[w];
+    const WalkRec& R = recs[w];
+    if (R.status != 0) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* slots = reinterpret_cast<T*>(smem_raw);                                // [warps][kMaxCls][16]
+    T* stage_n = slots + (kThreads / 32) * kMaxCls * 16;                      // [warps][32][16]
+    int* stage_c = reinterpret_cast<int*>(stage_n + (kThreads / 32) * 32 * 16);  // [warps][32]
+    unsigned long long* skeys = reinterpret_cast<unsigned long long*>(
+        (reinterpret_cast<uintptr_t>(stage_c + (kThreads / 32) * 32) + 15) & ~(uintptr_t)15);
+    const int s = W.s, C = (int)R.C;
+    const uint32_t nc = ncls[(uint64_t)w * kMaxMoves + C];
+    for (int i = threadIdx.x; i < (kThreads / 32) * kMaxCls * 16; i += blockDim.x) slots[i] = (T)0;
+    for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) skeys[i] = keys[((uint64_t)w * kMaxMoves + C) * kMaxCls + i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t N = 1u << s;
+    const uint64_t NN = (uint64_t)N * N;
+    const uint32_t norb = norbits(s), eC = 1u << C;
+    const int* E = energies + W.e_off;
+    T* st = states + W.state_off;
+    const bool fresh = R.fresh != 0;
+    const T scale = (T)R.scale;
+    const T init = (T)(1.0 / sqrt((double)N));
+    const T* cbase = cls + (uint64_t)w * kMaxCls * kClsStride;
+    T* myslots = slots + warp * kMaxCls * 16;
+    const uint32_t first = (blockIdx.x - W.cta0) * (uint32_t)kClsOrbitsPerCta;
+    for (int it = 0; it < kClsOrbitsPerThread; ++it) {
+        const uint32_t o = first + (uint32_t)(it * kThreads) + threadIdx.x;
+        const bool active = o < norb;
+        if (!__any_sync(0xffffffffu, active)) continue;  // warp-uniform
+        uint32_t dp = 0, x0 = 0;
+        bool single = true;
+        int ci = -1;
+        if (active) {
+            single = orbit_decode(o, s, C, dp, x0);
+            const unsigned long long key = orbit_key(E, x0, dp, eC);
+            int lo = 0, hi = (int)nc - 1;  // binary search in the sorted class keys
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (skeys[mid] < key) lo = mid + 1;
+                else hi = mid;
+            }
+            ci = (nc > 0 && skeys[lo] == key) ? lo : -1;
+        }
+        T v[16];
+#pragma unroll
+        for (int pos = 0; pos < 8; ++pos) {
+            const int a = pos >> 2, b = (pos >> 1) & 1, c = pos & 1;
+            const uint32_t x = x0 ^ (a ? dp : 0u) ^ (b ? eC : 0u);
+            const uint32_t d = dp ^ (c ? eC : 0u);
+#pragma unroll
+            for (int acc = 0; acc < 2; ++acc) {
+                T val = (T)0;
+                if (ci >= 0) {
+                    if (fresh) val = (single && c == 0 && acc == 0) ? init : (T)0;
+                    else if (!(single && a == 1)) val = st[(uint64_t)acc * NN + (uint64_t)d * N + x] * scale;
+                }
+                v[SLOT(a, b, c, acc)] = val;
+            }
+        }
+        if (single) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) v[8 + j] = v[j];
+        }
+        const T wgt = single ? (T)0.5 : (T)1;
+        const T* cb = cbase + (uint64_t)(ci >= 0 ? ci : 0) * kClsStride;
+        T S[16];
+        typedef typename std::conditional<sizeof(T) == 4, float4, double2>::type VecL;
+        constexpr int VW = sizeof(VecL) / sizeof(T);  // elements per vector load
+        const VecL* cv = reinterpret_cast<const VecL*>(cb);  // class rows are 16-byte aligned
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            T y = (T)0, sq = (T)0;
+#pragma unroll
+            for (int j = 0; j < 16; j += VW) {
+                const VecL a = __ldg(cv + (i * 16 + j) / VW);
+                const VecL b = __ldg(cv + (256 + i * 16 + j) / VW);
+                const T* av = reinterpret_cast<const T*>(&a);
+                const T* bv = reinterpret_cast<const T*>(&b);
+#pragma unroll
+                for (int u = 0; u < VW; ++u) {
+                    y += av[u] * v[j + u];
+                    sq += bv[u] * v[j + u];
+                }
+            }
+            S[i] = sq;
+            stage_n[(warp * 32 + lane) * 16 + i] = wgt * y * y;
+        }
+        stage_c[warp * 32 + lane] = ci;
+        if (ci >= 0) {
+#pragma unroll
+            for (int pos = 0; pos < 8; ++pos) {
+                const int a = pos >> 2, b = (pos >> 1) & 1, c = pos & 1;
+                if (single && a == 1) continue;
+                const uint32_t x = x0 ^ (a ? dp : 0u) ^ (b ? eC : 0u);
+                const uint32_t d = dp ^ (c ? eC : 0u);
+#pragma unroll
+                for (int acc = 0; acc < 2; ++acc) st[(uint64_t)acc * NN + (uint64_t)d * N + x] = S[SLOT(a, b, c, acc)];
+            }
+        }
+        __syncwarp();
+        if (lane < 16) {  // fixed order: lanes of the warp one after the other
+            for (int l = 0; l < 32; ++l) {
+                const int cl = stage_c[warp * 32 + l];
+                if (cl >= 0) myslots[cl * 16 + lane] += stage_n[(warp * 32 + l) * 16 + lane];
+            }
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    for (uint32_t e = threadIdx.x; e < nc * 16u; e += blockDim.x) {
+        double sum = 0.0;
+        for (int wp = 0; wp < kThreads / 32; ++wp) sum += (double)slots[wp * kMaxCls * 16 + e];
+        npart[(uint64_t)blockIdx.x * kMaxCls * 16 + e] = sum;
+    }
+}
+
+// g_k of a walk from its class sums (algo 1): g_k = sum_{c,i} N_{c,i} d_{c,k,i}.
+template <typename T>
+__device__ void cls_overlaps(const WalkDev& W, uint32_t nc, const double* __restrict__ npart, const T* __restrict__ cls,
+                             int w, int L, double* g, double (*gl)[kMaxL + 1]) {
+    const int t = threadIdx.x;  // kMaxL threads
+    for (int k = 0; k < L; ++k) gl[t][k] = 0.0;
+    for (uint32_t e = t; e < nc * 16u; e += kMaxL) {
+        double Nv = 0.0;
+        for (uint32_t c = 0; c < W.ncta; ++c) Nv += npart[(uint64_t)(W.cta0 + c) * kMaxCls * 16 + e];
+        const T* d = cls + ((uint64_t)w * kMaxCls + e / 16) * kClsStride + 512 + (e & 15);
+        for (int k = 0; k < L; ++k) gl[t][k] += Nv * (double)d[k * 16];
+    }
+    __syncthreads();
+    if (t < L) {
+        double sum = 0.0;
+        for (int u = 0; u < kMaxL; ++u) sum += gl[u][t];
+        g[t] = sum;
+    }
+}
+
 // One CTA of kMaxL threads per walk.
 __global__ void k_walk_measure(const WalkDev* __restrict__ walks, WalkRec* __restrict__ recs,
                                const double* __restrict__ partial, const double* __restrict__ cos64,
-                               double* __restrict__ trace, unsigned int* __restrict__ running) {
+                               double* __restrict__ trace, unsigned int* __restrict__ running, int algo,
+                               const uint32_t* __restrict__ ncls, const void* __restrict__ cls, int cls_f64) {
     const int w = blockIdx.x;
     const WalkDev& W = walks[w];
     WalkRec& R = recs[w];
     if (R.status != 0) return;
     __shared__ double g[kMaxL], P[kMaxL];
+    __shared__ double gl[kMaxL][kMaxL + 1];
     __shared__ double n2;
     const int L = 1 << W.q;
     const int t = threadIdx.x;
-    if (t < L) {
+    if (algo == 1) {
+        const uint32_t nc = ncls[(uint64_t)w * kMaxMoves + R.C];
+        if (cls_f64) cls_overlaps<double>(W, nc, partial, (const double*)cls, w, L, g, gl);
+        else cls_overlaps<float>(W, nc, partial, (const float*)cls, w, L, g, gl);
+    } else if (t < L) {
         double sum = 0.0;
         for (uint32_t c = 0; c < W.ncta; ++c) sum += partial[(uint64_t)(W.cta0 + c) * kMaxL + t];
         g[t] = sum;
@@ -645,6 +1051,11 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
     if (!walks || nwalks == 0 || !results) return wfail(SQ_ERR_ARG, "null or empty walk list");
     if (precision != SQ_F64 && precision != SQ_F32) return wfail(SQ_ERR_ARG, "unknown precision");
     const size_t esz = precision == SQ_F64 ? 8 : 4;
+    const uint32_t algo = walks[0].algo;
+    if (algo > 1) return wfail(SQ_ERR_ARG, "unknown walk algorithm (0: per-orbit iteration, 1: orbit classes)");
+    for (uint32_t i = 1; i < nwalks; ++i)
+        if (walks[i].algo != algo) return wfail(SQ_ERR_ARG, "all walks of a batch use one algorithm");
+    const uint32_t orbits_per_cta = algo == 1 ? (uint32_t)kClsOrbitsPerCta : (uint32_t)kOrbitsPerCta;
     std::vector<WalkDev> wd(nwalks);
     std::vector<int> energies;
     std::vector<int> cta_walk;
@@ -687,7 +1098,7 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
             }
             energies.push_back(E);
         }
-        const uint32_t ncta = (norbits(d.s) + kOrbitsPerCta - 1) / kOrbitsPerCta;
+        const uint32_t ncta = (norbits(d.s) + orbits_per_cta - 1) / orbits_per_cta;
         d.cta0 = (uint32_t)cta_walk.size();
         d.ncta = ncta;
         for (uint32_t c = 0; c < ncta; ++c) cta_walk.push_back((int)i);
@@ -707,7 +1118,15 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
     double* d_cos = nullptr;
     double* d_trace = nullptr;
     unsigned int* d_running = nullptr;
+    unsigned long long* d_keys = nullptr;
+    uint32_t* d_ncls = nullptr;
+    void* d_cls = nullptr;
+    int* d_jobs = nullptr;
     auto cleanup = [&]() {
+        cudaFree(d_keys);
+        cudaFree(d_ncls);
+        cudaFree(d_cls);
+        cudaFree(d_jobs);
         cudaFree(d_walks);
         cudaFree(d_recs);
         cudaFree(d_cta);
@@ -724,7 +1143,13 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
               cudaMalloc(&d_cta, sizeof(int) * nct) == cudaSuccess &&
               cudaMalloc(&d_E, sizeof(int) * energies.size()) == cudaSuccess &&
               cudaMalloc(&d_states, esz * state_elems) == cudaSuccess &&
-              cudaMalloc(&d_partial, sizeof(double) * kMaxL * nct) == cudaSuccess &&
+              cudaMalloc(&d_partial, sizeof(double) * (algo == 1 ? (size_t)kMaxCls * 16 : (size_t)kMaxL) * nct) ==
+                  cudaSuccess &&
+              (algo == 0 ||
+               (cudaMalloc(&d_keys, sizeof(unsigned long long) * nwalks * kMaxMoves * kMaxCls) == cudaSuccess &&
+                cudaMalloc(&d_ncls, sizeof(uint32_t) * nwalks * kMaxMoves) == cudaSuccess &&
+                cudaMalloc(&d_cls, esz * nwalks * kMaxCls * kClsStride) == cudaSuccess &&
+                cudaMalloc(&d_jobs, sizeof(int) * 2 * nwalks * kMaxMoves) == cudaSuccess)) &&
               cudaMalloc(&d_cos, sizeof(double) * kMaxL) == cudaSuccess &&
               cudaMalloc(&d_running, sizeof(unsigned int)) == cudaSuccess &&
               (!p0_trace || cudaMalloc(&d_trace, sizeof(double) * trace_len) == cudaSuccess);
@@ -750,6 +1175,52 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
         k_walk_init<<<(nwalks + 127) / 128, 128, 0, st>>>(d_walks, d_recs, (int)nwalks);
         err = cudaGetLastError();
     }
+    size_t prep_smem = 0, cls_smem = 0;
+    if (err == cudaSuccess && algo == 1) {
+        // the orbit classes of every (walk, move), once per batch
+        std::vector<int> jw, jm;
+        for (uint32_t i = 0; i < nwalks; ++i)
+            for (uint32_t c = 0; c < walks[i].spins; ++c) {
+                jw.push_back((int)i);
+                jm.push_back((int)c);
+            }
+        const size_t nj = jw.size();
+        std::vector<int> jobs(jw);
+        jobs.insert(jobs.end(), jm.begin(), jm.end());
+        err = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(int) * 2 * nj, cudaMemcpyHostToDevice, st);
+        if (err == cudaSuccess) {
+            k_cls_keys<<<(unsigned)nj, kThreads, 0, st>>>(d_walks, d_E, d_jobs, d_jobs + nj, d_keys, d_ncls);
+            err = cudaGetLastError();
+        }
+        std::vector<uint32_t> nc(nwalks * kMaxMoves, 0u);
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(nc.data(), d_ncls, sizeof(uint32_t) * nc.size(), cudaMemcpyDeviceToHost, st);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+        if (err == cudaSuccess) {
+            for (size_t j = 0; j < nj; ++j)
+                if (nc[(size_t)jw[j] * kMaxMoves + jm[j]] > (uint32_t)kMaxCls) {
+                    cudaStreamDestroy(st);
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    cleanup();
+                    return wfail(SQ_ERR_UNSUPPORTED, "more orbit classes than algorithm 1 holds (96); use algorithm 0");
+                }
+            prep_smem = esz * (kPrepThreads / 32) * 5 * 16 * 17;
+            cls_smem = esz * ((kThreads / 32) * kMaxCls * 16 + (kThreads / 32) * 32 * 16) + sizeof(int) * (kThreads / 32) * 32 +
+                       16 + sizeof(unsigned long long) * kMaxCls;
+            if (precision == SQ_F64) {
+                err = cudaFuncSetAttribute(k_cls_prep<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
+                if (err == cudaSuccess)
+                    err = cudaFuncSetAttribute(k_walk_step_cls<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)cls_smem);
+            } else {
+                err = cudaFuncSetAttribute(k_cls_prep<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
+                if (err == cudaSuccess)
+                    err = cudaFuncSetAttribute(k_walk_step_cls<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)cls_smem);
+            }
+        }
+    }
     // advance every running walk one step per iteration; poll the running count
     // every `chunk` iterations
     const uint32_t chunk = 16;
@@ -758,15 +1229,27 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
     while (err == cudaSuccess && left > 0 && iter < max_cap) {
         const uint32_t q = std::min(chunk, max_cap - iter);
         for (uint32_t k = 0; k < q && err == cudaSuccess; ++k) {
-            if (precision == SQ_F64)
+            if (algo == 1) {
+                if (precision == SQ_F64) {
+                    k_cls_prep<double><<<nwalks, kPrepThreads, prep_smem, st>>>(d_walks, d_recs, d_keys, d_ncls, (double*)d_cls);
+                    k_walk_step_cls<double><<<(unsigned)nct, kThreads, cls_smem, st>>>(
+                        d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const double*)d_cls, (double*)d_states, d_partial);
+                } else {
+                    k_cls_prep<float><<<nwalks, kPrepThreads, prep_smem, st>>>(d_walks, d_recs, d_keys, d_ncls, (float*)d_cls);
+                    k_walk_step_cls<float><<<(unsigned)nct, kThreads, cls_smem, st>>>(
+                        d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const float*)d_cls, (float*)d_states, d_partial);
+                }
+            } else if (precision == SQ_F64) {
                 k_walk_step<double><<<(unsigned)nct, kThreads, 0, st>>>(d_walks, d_cta, d_recs, d_E,
                                                                         (double*)d_states, d_partial);
-            else
+            } else {
                 k_walk_step<float><<<(unsigned)nct, kThreads, 0, st>>>(d_walks, d_cta, d_recs, d_E,
                                                                        (float*)d_states, d_partial);
+            }
             err = cudaGetLastError();
             if (err != cudaSuccess) break;
-            k_walk_measure<<<nwalks, kMaxL, 0, st>>>(d_walks, d_recs, d_partial, d_cos, d_trace, d_running);
+            k_walk_measure<<<nwalks, kMaxL, 0, st>>>(d_walks, d_recs, d_partial, d_cos, d_trace, d_running, (int)algo,
+                                                     d_ncls, d_cls, precision == SQ_F64 ? 1 : 0);
             err = cudaGetLastError();
         }
         iter += q;

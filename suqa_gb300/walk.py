@@ -27,6 +27,7 @@ class QsaWalk:
     phase_qbits: int = 6
     seed: int = 1
     max_steps: int = 0
+    algo: int = 0  # 0: iterate W per orbit; 1: per orbit class (see sq_qsa_walk)
 
     @property
     def cap(self) -> int:
@@ -57,7 +58,7 @@ def run_qsa_walks(walks: list[QsaWalk], precision: str = "f32", trace: bool = Fa
     for i, w in enumerate(walks):
         J = list(w.J) + [0] * (12 - len(w.J))
         arr[i] = SqQsaWalk(w.spins, w.phase_qbits, w.stages, w.steps_per_stage, w.max_steps,
-                           (C.c_int32 * 12)(*J), 0, w.beta, w.seed)
+                           (C.c_int32 * 12)(*J), w.algo, w.beta, w.seed)
     res = (SqQsaWalkResult * n)()
     caps = [w.cap for w in walks]
     tr = np.zeros(sum(caps) if trace else 0, dtype=np.float64)
@@ -75,12 +76,12 @@ def run_qsa_walks(walks: list[QsaWalk], precision: str = "f32", trace: bool = Fa
 
 
 def ising_ring_walks(n: int, spins: int = 10, beta: float = 1.0, stages: int = 50, steps_per_stage: int = 20,
-                     phase_qbits: int = 6, seed: int = 2025, max_steps: int = 0) -> list[QsaWalk]:
+                     phase_qbits: int = 6, seed: int = 2025, max_steps: int = 0, algo: int = 0) -> list[QsaWalk]:
     """n walks on periodic Ising rings with couplings +-1 drawn uniformly and no
     field; walk k has seed seed + k and its own couplings."""
     rng = np.random.default_rng(seed)
     return [QsaWalk(spins, [int(v) for v in rng.choice([-1, 1], spins)], beta, stages, steps_per_stage,
-                    phase_qbits, seed + k, max_steps) for k in range(n)]
+                    phase_qbits, seed + k, max_steps, algo) for k in range(n)]
 
 
 def summarize(runs: list[QsaWalkRun]) -> dict:
@@ -98,14 +99,14 @@ def summarize(runs: list[QsaWalkRun]) -> dict:
 
 
 def config4_study(n_walks: int = 1024, f64_walks: int = 64, spins: int = 10, stages: int = 50,
-                  steps_per_stage: int = 20, phase_qbits: int = 6, seed: int = 2025):
+                  steps_per_stage: int = 20, phase_qbits: int = 6, seed: int = 2025, algo: int = 0):
     """1024 annealed walks on 10-spin rings (J = +-1, h = 0), beta 0 -> 1 over
     50 stages x 20 walk steps, 6-qubit walk-phase register, in FP32; the first
     f64_walks of them again in FP64, walk by walk."""
-    walks = ising_ring_walks(n_walks, spins, 1.0, stages, steps_per_stage, phase_qbits, seed)
+    walks = ising_ring_walks(n_walks, spins, 1.0, stages, steps_per_stage, phase_qbits, seed, algo=algo)
     r32, ms32 = run_qsa_walks(walks, "f32")
     out = {"config": f"{n_walks} walks, {spins}-spin Ising rings J=+-1 h=0, beta 0->1 over {stages} stages x "
-                     f"{steps_per_stage} walk steps, {phase_qbits}-qubit walk-phase register",
+                     f"{steps_per_stage} walk steps, {phase_qbits}-qubit walk-phase register, algorithm {algo}",
            "f32": summarize(r32), "f32_device_s": ms32 / 1e3,
            "f32_walk_steps_per_s": sum(r.steps for r in r32) / (ms32 / 1e3)}
     if f64_walks:
@@ -127,5 +128,7 @@ if __name__ == "__main__":
     ap.add_argument("--f64-walks", type=int, default=64)
     ap.add_argument("--stages", type=int, default=50)
     ap.add_argument("--steps-per-stage", type=int, default=20)
+    ap.add_argument("--algo", type=int, default=0, help="0: iterate W per orbit; 1: per orbit class")
     a = ap.parse_args()
-    print(json.dumps(config4_study(a.walks, a.f64_walks, stages=a.stages, steps_per_stage=a.steps_per_stage)))
+    print(json.dumps(config4_study(a.walks, a.f64_walks, stages=a.stages, steps_per_stage=a.steps_per_stage,
+                                   algo=a.algo)))

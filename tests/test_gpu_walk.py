@@ -117,3 +117,31 @@ def test_twelve_spin_rings_at_the_size_limit():
         assert (a.done, a.restarts, a.steps, a.readout) == (b.done, b.restarts, b.steps, b.readout)
         assert np.max(np.abs(a.p0 - b.p0)) < 1e-4
         assert b.done and abs(b.E) <= 12 and 0 <= b.absM <= 12
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-9), ("f32", 5e-5)])
+def test_orbit_class_algorithm_matches_the_oracle(precision, tol):
+    """Algorithm 1 (per orbit class: eigen-decomposition of (W + W^T)/2 and the
+    sum of powers of W) gives the oracle's walks."""
+    walks = _walks(20, 7, spins=(2, 8), q=(1, 7), J=(-1, 2))
+    for w in walks:
+        w.J = [v if v != 0 else 1 for v in w.J]
+        w.algo = 1
+    from suqa_gb300.walk import run_qsa_walks
+    runs, _ = run_qsa_walks(walks, precision, trace=True)
+    _check(runs, walks, tol)
+
+
+def test_orbit_class_algorithm_on_ten_spin_rings_matches_iteration():
+    from suqa_gb300.walk import ising_ring_walks, run_qsa_walks
+    w0 = ising_ring_walks(12, 10, 1.0, 3, 2, 6, seed=9)
+    w1 = ising_ring_walks(12, 10, 1.0, 3, 2, 6, seed=9, algo=1)
+    for prec, tol in (("f64", 1e-9), ("f32", 1e-4)):
+        r0, _ = run_qsa_walks(w0, prec, trace=True)
+        r1, _ = run_qsa_walks(w1, prec, trace=True)
+        same = 0
+        for a, b in zip(r0, r1):
+            if (a.done, a.restarts, a.steps, a.readout) == (b.done, b.restarts, b.steps, b.readout):
+                same += 1
+                assert np.max(np.abs(a.p0 - b.p0)) < tol
+        assert same >= (12 if prec == "f64" else 11)

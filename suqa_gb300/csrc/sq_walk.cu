@@ -732,27 +732,44 @@ __global__ void __launch_bounds__(kPrepThreads) k_cls_prep(const WalkDev* __rest
 }
 
 // Orbit pass of algo 1: per orbit its class, y = V^T psi, the class sums of
-// y_i^2 (per warp, in a fixed order), S = Q psi written back.
-template <typename T>
+// y_i^2 (per warp, in a fixed order), S = Q psi written back.  STAGED: the
+// classes' V^T and Q are copied to shared memory first (rows of kStagedStride
+// elements, an odd number of 16-byte units, so lanes reading different classes
+// fall into different bank groups); otherwise they are read through L1.
+constexpr int kStagedStride = 516;
+
+template <typename T, bool STAGED>
 __global__ void __launch_bounds__(kThreads) k_walk_step_cls(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
                                                            const WalkRec* __restrict__ recs, const int* __restrict__ energies,
                                                            const unsigned long long* __restrict__ keys,
                                                            const uint32_t* __restrict__ ncls, const T* __restrict__ cls,
-                                                           T* __restrict__ states, double* __restrict__ npart) {
+                                                           T* __restrict__ states, double* __restrict__ npart, int nslot) {
     const int w = cta_walk[blockIdx.x];
     const WalkDev& W = walks[w];
     const WalkRec& R = recs[w];
     if (R.status != 0) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* slots = reinterpret_cast<T*>(smem_raw);                                // [warps][kMaxCls][16]
-    T* stage_n = slots + (kThreads / 32) * kMaxCls * 16;                      // [warps][32][16]
+    // nslot: classes per warp slot array (the batch's largest class count)
+    T* cls_s = reinterpret_cast<T*>(smem_raw);                                // STAGED: [nslot][kStagedStride]
+    T* slots = cls_s + (STAGED ? nslot * kStagedStride : 0);                  // [warps][nslot][16]
+    T* stage_n = slots + (kThreads / 32) * nslot * 16;                        // [warps][32][16]
     int* stage_c = reinterpret_cast<int*>(stage_n + (kThreads / 32) * 32 * 16);  // [warps][32]
     unsigned long long* skeys = reinterpret_cast<unsigned long long*>(
         (reinterpret_cast<uintptr_t>(stage_c + (kThreads / 32) * 32) + 15) & ~(uintptr_t)15);
     const int s = W.s, C = (int)R.C;
     const uint32_t nc = ncls[(uint64_t)w * kMaxMoves + C];
-    for (int i = threadIdx.x; i < (kThreads / 32) * kMaxCls * 16; i += blockDim.x) slots[i] = (T)0;
+    for (int i = threadIdx.x; i < (kThreads / 32) * nslot * 16; i += blockDim.x) slots[i] = (T)0;
     for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) skeys[i] = keys[((uint64_t)w * kMaxMoves + C) * kMaxCls + i];
+    if (STAGED) {
+        typedef typename std::conditional<sizeof(T) == 4, float4, double2>::type VecS;
+        constexpr int VS = sizeof(VecS) / sizeof(T);
+        const T* src = cls + (uint64_t)w * kMaxCls * kClsStride;
+        for (uint32_t i = threadIdx.x; i < nc * (512 / VS); i += blockDim.x) {
+            const uint32_t c = i / (512 / VS), e = (i % (512 / VS)) * VS;
+            *reinterpret_cast<VecS*>(cls_s + c * kStagedStride + e) =
+                __ldg(reinterpret_cast<const VecS*>(src + (uint64_t)c * kClsStride + e));
+        }
+    }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t N = 1u << s;
@@ -764,7 +781,7 @@ __global__ void __launch_bounds__(kThreads) k_walk_step_cls(const WalkDev* __res
     const T scale = (T)R.scale;
     const T init = (T)(1.0 / sqrt((double)N));
     const T* cbase = cls + (uint64_t)w * kMaxCls * kClsStride;
-    T* myslots = slots + warp * kMaxCls * 16;
+    T* myslots = slots + warp * nslot * 16;
     const uint32_t first = (blockIdx.x - W.cta0) * (uint32_t)kClsOrbitsPerCta;
     for (int it = 0; it < kClsOrbitsPerThread; ++it) {
         const uint32_t o = first + (uint32_t)(it * kThreads) + threadIdx.x;
@@ -805,7 +822,7 @@ __global__ void __launch_bounds__(kThreads) k_walk_step_cls(const WalkDev* __res
             for (int j = 0; j < 8; ++j) v[8 + j] = v[j];
         }
         const T wgt = single ? (T)0.5 : (T)1;
-        const T* cb = cbase + (uint64_t)(ci >= 0 ? ci : 0) * kClsStride;
+        const T* cb = STAGED ? cls_s + (ci >= 0 ? ci : 0) * kStagedStride : cbase + (uint64_t)(ci >= 0 ? ci : 0) * kClsStride;
         T S[16];
         typedef typename std::conditional<sizeof(T) == 4, float4, double2>::type VecL;
         constexpr int VW = sizeof(VecL) / sizeof(T);  // elements per vector load
@@ -815,8 +832,8 @@ __global__ void __launch_bounds__(kThreads) k_walk_step_cls(const WalkDev* __res
             T y = (T)0, sq = (T)0;
 #pragma unroll
             for (int j = 0; j < 16; j += VW) {
-                const VecL a = __ldg(cv + (i * 16 + j) / VW);
-                const VecL b = __ldg(cv + (256 + i * 16 + j) / VW);
+                const VecL a = STAGED ? cv[(i * 16 + j) / VW] : __ldg(cv + (i * 16 + j) / VW);
+                const VecL b = STAGED ? cv[(256 + i * 16 + j) / VW] : __ldg(cv + (256 + i * 16 + j) / VW);
                 const T* av = reinterpret_cast<const T*>(&a);
                 const T* bv = reinterpret_cast<const T*>(&b);
 #pragma unroll
@@ -852,7 +869,7 @@ __global__ void __launch_bounds__(kThreads) k_walk_step_cls(const WalkDev* __res
     __syncthreads();
     for (uint32_t e = threadIdx.x; e < nc * 16u; e += blockDim.x) {
         double sum = 0.0;
-        for (int wp = 0; wp < kThreads / 32; ++wp) sum += (double)slots[wp * kMaxCls * 16 + e];
+        for (int wp = 0; wp < kThreads / 32; ++wp) sum += (double)slots[wp * nslot * 16 + e];
         npart[(uint64_t)blockIdx.x * kMaxCls * 16 + e] = sum;
     }
 }
@@ -1176,6 +1193,8 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
         err = cudaGetLastError();
     }
     size_t prep_smem = 0, cls_smem = 0;
+    int nslot = 1;
+    bool staged = false;
     if (err == cudaSuccess && algo == 1) {
         // the orbit classes of every (walk, move), once per batch
         std::vector<int> jw, jm;
@@ -1205,19 +1224,28 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
                     cleanup();
                     return wfail(SQ_ERR_UNSUPPORTED, "more orbit classes than algorithm 1 holds (96); use algorithm 0");
                 }
+            nslot = 1;
+            for (size_t j = 0; j < nj; ++j) nslot = std::max<int>(nslot, (int)nc[(size_t)jw[j] * kMaxMoves + jm[j]]);
             prep_smem = esz * (kPrepThreads / 32) * 5 * 16 * 17;
-            cls_smem = esz * ((kThreads / 32) * kMaxCls * 16 + (kThreads / 32) * 32 * 16) + sizeof(int) * (kThreads / 32) * 32 +
-                       16 + sizeof(unsigned long long) * kMaxCls;
+            const size_t base_smem = esz * ((kThreads / 32) * (size_t)nslot * 16 + (kThreads / 32) * 32 * 16) +
+                                     sizeof(int) * (kThreads / 32) * 32 + 16 + sizeof(unsigned long long) * kMaxCls;
+            const size_t staged_smem = base_smem + esz * (size_t)nslot * kStagedStride;
+            int optin = 0;
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0);
+            staged = precision == SQ_F32 && staged_smem <= (size_t)optin;
+            cls_smem = staged ? staged_smem : base_smem;
             if (precision == SQ_F64) {
                 err = cudaFuncSetAttribute(k_cls_prep<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
                 if (err == cudaSuccess)
-                    err = cudaFuncSetAttribute(k_walk_step_cls<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                    err = cudaFuncSetAttribute(k_walk_step_cls<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)cls_smem);
             } else {
                 err = cudaFuncSetAttribute(k_cls_prep<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
                 if (err == cudaSuccess)
-                    err = cudaFuncSetAttribute(k_walk_step_cls<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)cls_smem);
+                    err = staged ? cudaFuncSetAttribute(k_walk_step_cls<float, true>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cls_smem)
+                                 : cudaFuncSetAttribute(k_walk_step_cls<float, false>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cls_smem);
             }
         }
     }
@@ -1232,12 +1260,18 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
             if (algo == 1) {
                 if (precision == SQ_F64) {
                     k_cls_prep<double><<<nwalks, kPrepThreads, prep_smem, st>>>(d_walks, d_recs, d_keys, d_ncls, (double*)d_cls);
-                    k_walk_step_cls<double><<<(unsigned)nct, kThreads, cls_smem, st>>>(
-                        d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const double*)d_cls, (double*)d_states, d_partial);
+                    k_walk_step_cls<double, false><<<(unsigned)nct, kThreads, cls_smem, st>>>(
+                        d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const double*)d_cls, (double*)d_states, d_partial, nslot);
                 } else {
                     k_cls_prep<float><<<nwalks, kPrepThreads, prep_smem, st>>>(d_walks, d_recs, d_keys, d_ncls, (float*)d_cls);
-                    k_walk_step_cls<float><<<(unsigned)nct, kThreads, cls_smem, st>>>(
-                        d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const float*)d_cls, (float*)d_states, d_partial);
+                    if (staged)
+                        k_walk_step_cls<float, true><<<(unsigned)nct, kThreads, cls_smem, st>>>(
+                            d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const float*)d_cls, (float*)d_states, d_partial,
+                            nslot);
+                    else
+                        k_walk_step_cls<float, false><<<(unsigned)nct, kThreads, cls_smem, st>>>(
+                            d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const float*)d_cls, (float*)d_states, d_partial,
+                            nslot);
                 }
             } else if (precision == SQ_F64) {
                 k_walk_step<double><<<(unsigned)nct, kThreads, 0, st>>>(d_walks, d_cta, d_recs, d_E,

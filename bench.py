@@ -229,28 +229,37 @@ def qsa_section(n_walks, walk_steps, f64_walks=16, cpu=True, seed=2025):
     walk, h = 0, beta 0 -> 1 over 50 stages x 20 walk steps, 6-qubit walk-phase
     register, one PCG32 stream per walk): every walk capped at its first
     `walk_steps` walk steps (restarts included), FP32 for all walks, FP64 for the
-    first `f64_walks`.  FP32 work per walk step: 2^9 + 511 * 2^8 register-resident
-    orbits, each 63 applications of W (272 flops: 4 Hadamards x 16, 4 rotations x 48,
+    first `f64_walks`, with algorithm 1 (orbit classes); algorithm 0 (the per-orbit
+    iteration) runs the same FP32 walks for comparison.  Rates are also given as
+    the per-orbit iteration's flops per second: 2^9 + 511 * 2^8 orbits per walk
+    step, each 63 applications of W (272 flops: 4 Hadamards x 16, 4 rotations x 48,
     2 reflections x 8) plus 64 overlap/sum updates (48 flops)."""
     import numpy as np
     from suqa_gb300.walk import ising_ring_walks, run_qsa_walks
-    walks = ising_ring_walks(n_walks, 10, 1.0, 50, 20, 6, seed=seed, max_steps=walk_steps)
+    walks = ising_ring_walks(n_walks, 10, 1.0, 50, 20, 6, seed=seed, max_steps=walk_steps, algo=1)
     run_qsa_walks(walks[:4], "f32")  # first launch, module load
     r32, ms32 = run_qsa_walks(walks, "f32", trace=True)
     r64, ms64 = run_qsa_walks(walks[:f64_walks], "f64", trace=True)
+    walks0 = ising_ring_walks(n_walks, 10, 1.0, 50, 20, 6, seed=seed, max_steps=walk_steps, algo=0)
+    r0, ms0 = run_qsa_walks(walks0, "f32")
     st32 = sum(r.steps for r in r32)
     st64 = sum(r.steps for r in r64)
     same = [i for i, (a, b) in enumerate(zip(r32, r64)) if (a.restarts, a.steps) == (b.restarts, b.steps)]
     p0_err = max((float(np.max(np.abs(r32[i].p0 - r64[i].p0))) for i in same), default=None)
+    # flops of the per-orbit iteration (algorithm 0) per walk step: the rate either
+    # algorithm delivers, expressed as that work per second
     norb, L = (1 << 9) + ((1 << 9) - 1) * (1 << 8), 64
     flops = norb * ((L - 1) * 272 + L * 48)
     out = {"workload": f"{n_walks} walks on 10-spin Ising rings (2^21 amplitudes each), first {walk_steps} walk "
                        f"steps of the beta 0->1 anneal (50 stages x 20 steps), 6-qubit walk-phase register",
+           "algorithm": "1 (orbit classes); f32_per_orbit_iteration: algorithm 0 on the same walks",
+           "f32_per_orbit_iteration": {"walk_steps_per_s": sum(r.steps for r in r0) / (ms0 / 1e3),
+                                       "fp32_tflops": flops * sum(r.steps for r in r0) / (ms0 / 1e3) / 1e12},
            "f32": {"walk_steps_per_s": st32 / (ms32 / 1e3), "walk_steps": st32, "device_ms": ms32,
                    "restarts": int(sum(r.restarts for r in r32)),
-                   "fp32_tflops": flops * st32 / (ms32 / 1e3) / 1e12},
+                   "equivalent_fp32_tflops": flops * st32 / (ms32 / 1e3) / 1e12},
            "f64": {"walk_steps_per_s": st64 / (ms64 / 1e3), "walk_steps": st64, "device_ms": ms64,
-                   "fp64_tflops": flops * st64 / (ms64 / 1e3) / 1e12, "walks": f64_walks},
+                   "equivalent_fp64_tflops": flops * st64 / (ms64 / 1e3) / 1e12, "walks": f64_walks},
            "fp32_vs_fp64": {"walks_identical": len(same), "walks": f64_walks, "max_abs_p0_diff": p0_err},
            "flops_per_walk_step": flops}
     if cpu:

@@ -99,7 +99,7 @@ def summarize(runs: list[QsaWalkRun]) -> dict:
 
 
 def config4_study(n_walks: int = 1024, f64_walks: int = 64, spins: int = 10, stages: int = 50,
-                  steps_per_stage: int = 20, phase_qbits: int = 6, seed: int = 2025, algo: int = 0):
+                  steps_per_stage: int = 20, phase_qbits: int = 6, seed: int = 2025, algo: int = 1):
     """1024 annealed walks on 10-spin rings (J = +-1, h = 0), beta 0 -> 1 over
     50 stages x 20 walk steps, 6-qubit walk-phase register, in FP32; the first
     f64_walks of them again in FP64, walk by walk."""
@@ -128,7 +128,7 @@ if __name__ == "__main__":
     ap.add_argument("--f64-walks", type=int, default=64)
     ap.add_argument("--stages", type=int, default=50)
     ap.add_argument("--steps-per-stage", type=int, default=20)
-    ap.add_argument("--algo", type=int, default=0, help="0: iterate W per orbit; 1: per orbit class")
+    ap.add_argument("--algo", type=int, default=1, help="0: iterate W per orbit; 1: per orbit class")
     a = ap.parse_args()
     print(json.dumps(config4_study(a.walks, a.f64_walks, stages=a.stages, steps_per_stage=a.steps_per_stage,
                                    algo=a.algo)))

@@ -274,7 +274,10 @@ typedef struct sq_qsa_walk {
     uint32_t max_steps;       /* cap on steps over all attempts (0: 8 x stages x steps_per_stage) */
     int32_t J[12];            /* bond couplings, bond i joins spins i and i+1 mod s; -8..8 */
     uint32_t algo;            /* 0: iterate W per orbit; 1: per orbit class (W, eigenvectors of
-                                 (W + W^T)/2, sum of powers), at most 96 classes per move;
+                                 (W + W^T)/2, sum of powers), at most 96 classes per move, the
+                                 class data prepared once per batch for every (class, stage
+                                 temperature) when that table fits (4 GiB), else per step;
+                                 2: as 1, always prepared per walk and step;
                                  one value for the whole batch */
     double beta;              /* final inverse temperature */
     uint64_t seed;            /* PCG32 seed (pcg32::seed(seed, 1)) */

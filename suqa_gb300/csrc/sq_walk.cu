@@ -32,8 +32,12 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
+#include <map>
 #include <string>
+#include <tuple>
 #include <type_traits>
+#include <unordered_map>
 #include <vector>
 
 #include "sq.h"
@@ -61,6 +65,7 @@ struct WalkDev {
     uint32_t e_off;      // first entry of the energy table (2^s int32)
     uint32_t cta0, ncta; // CTAs of the walk in the step grid
     int dmax;            // largest |dE| of the ring
+    uint32_t slot0;      // class-table temperature slot of stage 0 (algo 1)
 };
 
 struct WalkRec {
@@ -488,13 +493,18 @@ k_walk_step(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
 // an orbit adds the 16 values (V^T psi)_i^2 to its class, g_k = sum_{c,i} N_{c,i}
 // d_{c,k,i}, and the state after reading zero is Q psi per orbit.  The d table
 // comes from the powers of W themselves (errors grow with k, not with k^2 as
-// T_k(lambda) evaluated from an approximate lambda would).
+// T_k(lambda) evaluated from an approximate lambda would).  The class data depend
+// only on (key, beta_k, q): algo 1 prepares them once per batch for every distinct
+// key and stage temperature (k_cls_table; rings with couplings +-1 have a few dozen
+// keys in all), algo 2 (and algo 1 when that table would not fit) per walk and step
+// (k_cls_prep).
 
 constexpr int kMaxCls = 96;
 constexpr int kClsOrbitsPerThread = 32;
 constexpr int kClsOrbitsPerCta = kThreads * kClsOrbitsPerThread;
 constexpr int kClsStride = 16 * 16 + 16 * 16 + kMaxL * 16;  // V^T, Q, d[k][i]
 constexpr int kMaxMoves = 12;
+constexpr uint64_t kTableBudget = 4ull << 30;  // largest batch class table (bytes)
 
 __device__ __forceinline__ bool orbit_decode(uint32_t o, int s, int C, uint32_t& dp, uint32_t& x0) {
     const uint32_t nb = 1u << (s - 1);
@@ -589,10 +599,136 @@ __device__ __forceinline__ void warp_matmul(T (*Z)[17], const T (*X)[17], const 
     __syncwarp();
 }
 
-// Per walk, one warp per class of the current move: W, the eigen-decomposition of
-// A = (W + W^T)/2 (cyclic Jacobi) and Q.
+// One class, by one warp: W (its columns are W applied to the unit vectors), the
+// eigen-decomposition of A = (W + W^T)/2 (cyclic Jacobi), the d table and Q, written
+// to out[kClsStride] as V^T, Q, d[k][i].  mats: the warp's five 16 x 17 scratch
+// matrices.  The result depends only on (key, beta_k, q).
 constexpr int kPrepThreads = 512;
 
+template <typename T>
+__device__ void prep_class(unsigned long long key, double beta_k, int q, T* __restrict__ out, T (*mats)[16][17],
+                           int lane) {
+    T(*Wp)[17] = mats[0];
+    T(*A)[17] = mats[1];
+    T(*V)[17] = mats[2];
+    T(*Q)[17] = mats[3];
+    T(*Tm)[17] = mats[4];
+    int dE0[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) dE0[j] = (int)((key >> (9 * j)) & 511ull) - 256;
+    T ce[8], cr[8];
+    uint32_t zmask = 0;
+#pragma unroll
+    for (int pos = 0; pos < 8; ++pos) {
+        const int a = pos >> 2, b = (pos >> 1) & 1, cc = pos & 1;
+        // a = 1 positions are the swap partners of (0, b ^ c, c): negated differences
+        const int dE = a == 0 ? dE0[b + 2 * cc] : -dE0[(b ^ cc) + 2 * cc];
+        double e = 1.0, r = 0.0;
+        if (dE > 0) {
+            e = exp(-0.5 * beta_k * (double)dE);
+            r = sqrt(1.0 - e * e);
+        }
+        ce[pos] = (T)e;
+        cr[pos] = (T)r;
+        if (dE == 0) zmask |= 1u << pos;
+    }
+    // W column by column: W applied to the unit vectors
+    if (lane < 16) {
+        Orbit<T> ob;
+        ob.setup(ce, cr, zmask);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) ob.v[j] = j == lane ? (T)1 : (T)0;
+        ob.walk();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) Wp[i][lane] = ob.v[i];
+    }
+    __syncwarp();
+    for (int idx = lane; idx < 256; idx += 32) {
+        const int i = idx >> 4, j = idx & 15;
+        A[i][j] = (T)0.5 * (Wp[i][j] + Wp[j][i]);
+        V[i][j] = i == j ? (T)1 : (T)0;
+    }
+    __syncwarp();
+    // cyclic Jacobi: A' = J^T A J zeroes A[p][q]; V' = V J; stops when the
+    // off-diagonal mass is at rounding level (at most 10 sweeps)
+    const T tol = sizeof(T) == 8 ? (T)1e-28 : (T)1e-12;
+    for (int sweep = 0; sweep < 10; ++sweep) {
+        T off = (T)0;
+        for (int idx = lane; idx < 256; idx += 32) {
+            const int i = idx >> 4, j = idx & 15;
+            if (i < j) off += A[i][j] * A[i][j];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) off += __shfl_xor_sync(0xffffffffu, off, o);
+        if (off < tol) break;  // uniform over the warp
+        for (int p = 0; p < 15; ++p) {
+            for (int qq = p + 1; qq < 16; ++qq) {
+                const T apq = A[p][qq];
+                if (fabs((double)apq) < 1e-300) continue;  // uniform: every lane reads the same value
+                const T app = A[p][p], aqq = A[qq][qq];
+                const T tau = (aqq - app) / ((T)2 * apq);
+                const T t = (tau >= (T)0 ? (T)1 : (T)-1) / (fabs(tau) + sqrt((T)1 + tau * tau));
+                const T c1 = (T)1 / sqrt((T)1 + t * t), s1 = t * c1;
+                __syncwarp();
+                if (lane < 16) {
+                    const T akp = A[lane][p], akq = A[lane][qq];
+                    A[lane][p] = c1 * akp - s1 * akq;
+                    A[lane][qq] = s1 * akp + c1 * akq;
+                }
+                __syncwarp();
+                if (lane < 16) {
+                    const T apk = A[p][lane], aqk = A[qq][lane];
+                    A[p][lane] = c1 * apk - s1 * aqk;
+                    A[qq][lane] = s1 * apk + c1 * aqk;
+                    const T vkp = V[lane][p], vkq = V[lane][qq];
+                    V[lane][p] = c1 * vkp - s1 * vkq;
+                    V[lane][qq] = s1 * vkp + c1 * vkq;
+                }
+                __syncwarp();
+            }
+        }
+    }
+    // d[k][i] = v_i^T U_k with U_k = W U_{k-1} = W^k V (A is free again: it holds U)
+    T(*U)[17] = A;
+    for (int idx = lane; idx < 256; idx += 32) U[idx >> 4][idx & 15] = V[idx >> 4][idx & 15];
+    if (lane < 16) out[512 + lane] = (T)1;  // d[0][i] = |v_i|^2 = 1
+    __syncwarp();
+    for (int k = 1; k < (1 << q); ++k) {
+        warp_matmul<T>(Tm, Wp, U, lane);  // U_k = W U_{k-1}
+        for (int idx = lane; idx < 256; idx += 32) U[idx >> 4][idx & 15] = Tm[idx >> 4][idx & 15];
+        __syncwarp();
+        if (lane < 16) {
+            T dk = (T)0;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) dk += V[j][lane] * U[j][lane];
+            out[512 + k * 16 + lane] = dk;
+        }
+        __syncwarp();
+    }
+    // Q = sum_{k<L} W^k = prod_{j<q} (I + W^(2^j)); Wp becomes the running square
+    for (int idx = lane; idx < 256; idx += 32) {
+        const int i = idx >> 4, j = idx & 15;
+        Q[i][j] = Wp[i][j] + (i == j ? (T)1 : (T)0);
+    }
+    __syncwarp();
+    for (int j = 1; j < q; ++j) {
+        warp_matmul<T>(Tm, Wp, Wp, lane);
+        for (int idx = lane; idx < 256; idx += 32) Wp[idx >> 4][idx & 15] = Tm[idx >> 4][idx & 15];
+        __syncwarp();
+        warp_matmul<T>(Tm, Q, Wp, lane);
+        for (int idx = lane; idx < 256; idx += 32) Q[idx >> 4][idx & 15] += Tm[idx >> 4][idx & 15];
+        __syncwarp();
+    }
+    for (int idx = lane; idx < 256; idx += 32) {
+        const int i = idx >> 4, j = idx & 15;
+        out[idx] = V[j][i];  // V^T, row i = eigenvector i
+        out[256 + idx] = Q[i][j];
+    }
+    __syncwarp();
+}
+
+// Per walk and step, one warp per class of the current move (classes at the walk's
+// current temperature; used when the batch's class table does not fit).
 template <typename T>
 __global__ void __launch_bounds__(kPrepThreads) k_cls_prep(const WalkDev* __restrict__ walks, const WalkRec* __restrict__ recs,
                                                       const unsigned long long* __restrict__ keys,
@@ -603,132 +739,36 @@ __global__ void __launch_bounds__(kPrepThreads) k_cls_prep(const WalkDev* __rest
     if (R.status != 0) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     typedef T Mat[16][17];
-    Mat* mats = reinterpret_cast<Mat*>(smem_raw);  // per warp: Wp, A (then U), V, Q, tmp
+    Mat* mats = reinterpret_cast<Mat*>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    T(*Wp)[17] = mats[warp * 5 + 0];
-    T(*A)[17] = mats[warp * 5 + 1];
-    T(*V)[17] = mats[warp * 5 + 2];
-    T(*Q)[17] = mats[warp * 5 + 3];
-    T(*Tm)[17] = mats[warp * 5 + 4];
-    const int C = (int)R.C, q = W.q;
-    const uint32_t nc = ncls[(uint64_t)w * kMaxMoves + C];
-    const unsigned long long* kk = keys + ((uint64_t)w * kMaxMoves + C) * kMaxCls;
-    for (uint32_t c = warp; c < nc; c += kPrepThreads / 32) {
-        const unsigned long long key = kk[c];
-        int dE0[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) dE0[j] = (int)((key >> (9 * j)) & 511ull) - 256;
-        T ce[8], cr[8];
-        uint32_t zmask = 0;
-#pragma unroll
-        for (int pos = 0; pos < 8; ++pos) {
-            const int a = pos >> 2, b = (pos >> 1) & 1, cc = pos & 1;
-            // a = 1 positions are the swap partners of (0, b ^ c, c): negated differences
-            const int dE = a == 0 ? dE0[b + 2 * cc] : -dE0[(b ^ cc) + 2 * cc];
-            double e = 1.0, r = 0.0;
-            if (dE > 0) {
-                e = exp(-0.5 * R.beta_k * (double)dE);
-                r = sqrt(1.0 - e * e);
-            }
-            ce[pos] = (T)e;
-            cr[pos] = (T)r;
-            if (dE == 0) zmask |= 1u << pos;
-        }
-        // W column by column: W applied to the unit vectors
-        if (lane < 16) {
-            Orbit<T> ob;
-            ob.setup(ce, cr, zmask);
-#pragma unroll
-            for (int j = 0; j < 16; ++j) ob.v[j] = j == lane ? (T)1 : (T)0;
-            ob.walk();
-#pragma unroll
-            for (int i = 0; i < 16; ++i) Wp[i][lane] = ob.v[i];
-        }
-        __syncwarp();
-        for (int idx = lane; idx < 256; idx += 32) {
-            const int i = idx >> 4, j = idx & 15;
-            A[i][j] = (T)0.5 * (Wp[i][j] + Wp[j][i]);
-            V[i][j] = i == j ? (T)1 : (T)0;
-        }
-        __syncwarp();
-        // cyclic Jacobi: A' = J^T A J zeroes A[p][q]; V' = V J; stops when the
-        // off-diagonal mass is at rounding level (at most 10 sweeps)
-        const T tol = sizeof(T) == 8 ? (T)1e-28 : (T)1e-12;
-        for (int sweep = 0; sweep < 10; ++sweep) {
-            T off = (T)0;
-            for (int idx = lane; idx < 256; idx += 32) {
-                const int i = idx >> 4, j = idx & 15;
-                if (i < j) off += A[i][j] * A[i][j];
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) off += __shfl_xor_sync(0xffffffffu, off, o);
-            if (off < tol) break;  // uniform over the warp
-            for (int p = 0; p < 15; ++p) {
-                for (int qq = p + 1; qq < 16; ++qq) {
-                    const T apq = A[p][qq];
-                    if (fabs((double)apq) < 1e-300) continue;  // uniform: every lane reads the same value
-                    const T app = A[p][p], aqq = A[qq][qq];
-                    const T tau = (aqq - app) / ((T)2 * apq);
-                    const T t = (tau >= (T)0 ? (T)1 : (T)-1) / (fabs(tau) + sqrt((T)1 + tau * tau));
-                    const T c1 = (T)1 / sqrt((T)1 + t * t), s1 = t * c1;
-                    __syncwarp();
-                    if (lane < 16) {
-                        const T akp = A[lane][p], akq = A[lane][qq];
-                        A[lane][p] = c1 * akp - s1 * akq;
-                        A[lane][qq] = s1 * akp + c1 * akq;
-                    }
-                    __syncwarp();
-                    if (lane < 16) {
-                        const T apk = A[p][lane], aqk = A[qq][lane];
-                        A[p][lane] = c1 * apk - s1 * aqk;
-                        A[qq][lane] = s1 * apk + c1 * aqk;
-                        const T vkp = V[lane][p], vkq = V[lane][qq];
-                        V[lane][p] = c1 * vkp - s1 * vkq;
-                        V[lane][qq] = s1 * vkp + c1 * vkq;
-                    }
-                    __syncwarp();
-                }
-            }
-        }
-        // d[k][i] = v_i^T U_k with U_k = W U_{k-1} = W^k V (A is free again: it holds U)
-        T* out = cls + ((uint64_t)w * kMaxCls + c) * kClsStride;
-        T(*U)[17] = A;
-        for (int idx = lane; idx < 256; idx += 32) U[idx >> 4][idx & 15] = V[idx >> 4][idx & 15];
-        if (lane < 16) out[512 + lane] = (T)1;  // d[0][i] = |v_i|^2 = 1
-        __syncwarp();
-        for (int k = 1; k < (1 << q); ++k) {
-            warp_matmul<T>(Tm, Wp, U, lane);  // U_k = W U_{k-1}
-            for (int idx = lane; idx < 256; idx += 32) U[idx >> 4][idx & 15] = Tm[idx >> 4][idx & 15];
-            __syncwarp();
-            if (lane < 16) {
-                T dk = (T)0;
-#pragma unroll
-                for (int j = 0; j < 16; ++j) dk += V[j][lane] * U[j][lane];
-                out[512 + k * 16 + lane] = dk;
-            }
-            __syncwarp();
-        }
-        // Q = sum_{k<L} W^k = prod_{j<q} (I + W^(2^j)); Wp becomes the running square
-        for (int idx = lane; idx < 256; idx += 32) {
-            const int i = idx >> 4, j = idx & 15;
-            Q[i][j] = Wp[i][j] + (i == j ? (T)1 : (T)0);
-        }
-        __syncwarp();
-        for (int j = 1; j < q; ++j) {
-            warp_matmul<T>(Tm, Wp, Wp, lane);
-            for (int idx = lane; idx < 256; idx += 32) Wp[idx >> 4][idx & 15] = Tm[idx >> 4][idx & 15];
-            __syncwarp();
-            warp_matmul<T>(Tm, Q, Wp, lane);
-            for (int idx = lane; idx < 256; idx += 32) Q[idx >> 4][idx & 15] += Tm[idx >> 4][idx & 15];
-            __syncwarp();
-        }
-        for (int idx = lane; idx < 256; idx += 32) {
-            const int i = idx >> 4, j = idx & 15;
-            out[idx] = V[j][i];  // V^T, row i = eigenvector i
-            out[256 + idx] = Q[i][j];
-        }
-        __syncwarp();
-    }
+    const uint32_t nc = ncls[(uint64_t)w * kMaxMoves + R.C];
+    const unsigned long long* kk = keys + ((uint64_t)w * kMaxMoves + R.C) * kMaxCls;
+    for (uint32_t c = warp; c < nc; c += kPrepThreads / 32)
+        prep_class<T>(kk[c], R.beta_k, W.q, cls + ((uint64_t)w * kMaxCls + c) * kClsStride, mats + warp * 5, lane);
+}
+
+// The batch's class table, once: entry e = key index * nslot + temperature slot, one
+// warp per entry.  Slot j holds (beta_j, q_j); a walk's stage k at slot slot0 + k.
+template <typename T>
+__global__ void __launch_bounds__(kPrepThreads) k_cls_table(const unsigned long long* __restrict__ gkeys,
+                                                       const double* __restrict__ slot_beta, const int* __restrict__ slot_q,
+                                                       uint32_t nslot, uint32_t nentry, T* __restrict__ tab) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    typedef T Mat[16][17];
+    Mat* mats = reinterpret_cast<Mat*>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t e = blockIdx.x * (kPrepThreads / 32) + warp;
+    if (e >= nentry) return;  // warp-uniform; no block-wide barrier follows
+    const uint32_t slot = e % nslot;
+    prep_class<T>(gkeys[e / nslot], slot_beta[slot], slot_q[slot], tab + (uint64_t)e * kClsStride, mats + warp * 5, lane);
+}
+
+// Class data of class c of the walk's current move: per-step preparation (gid null)
+// keeps it per walk; the table indexes it by key and temperature slot.
+__device__ __forceinline__ uint64_t cls_entry(const WalkDev& W, const WalkRec& R, const uint32_t* __restrict__ gid, int w,
+                                              uint32_t c) {
+    if (!gid) return (uint64_t)w * kMaxCls + c;
+    return (uint64_t)gid[((uint64_t)w * kMaxMoves + R.C) * kMaxCls + c] + W.slot0 + R.att / (uint32_t)W.per;
 }
 
 // Orbit pass of algo 1: per orbit its class, y = V^T psi, the class sums of
@@ -743,7 +783,8 @@ __global__ void __launch_bounds__(kThreads) k_walk_step_cls(const WalkDev* __res
                                                            const WalkRec* __restrict__ recs, const int* __restrict__ energies,
                                                            const unsigned long long* __restrict__ keys,
                                                            const uint32_t* __restrict__ ncls, const T* __restrict__ cls,
-                                                           T* __restrict__ states, double* __restrict__ npart, int nslot) {
+                                                           const uint32_t* __restrict__ gid, T* __restrict__ states,
+                                                           double* __restrict__ npart, int nslot) {
     const int w = cta_walk[blockIdx.x];
     const WalkDev& W = walks[w];
     const WalkRec& R = recs[w];
@@ -756,21 +797,24 @@ __global__ void __launch_bounds__(kThreads) k_walk_step_cls(const WalkDev* __res
     int* stage_c = reinterpret_cast<int*>(stage_n + (kThreads / 32) * 32 * 16);  // [warps][32]
     unsigned long long* skeys = reinterpret_cast<unsigned long long*>(
         (reinterpret_cast<uintptr_t>(stage_c + (kThreads / 32) * 32) + 15) & ~(uintptr_t)15);
+    unsigned long long* sent = skeys + kMaxCls;  // class data entry of each class
     const int s = W.s, C = (int)R.C;
     const uint32_t nc = ncls[(uint64_t)w * kMaxMoves + C];
     for (int i = threadIdx.x; i < (kThreads / 32) * nslot * 16; i += blockDim.x) slots[i] = (T)0;
     for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) skeys[i] = keys[((uint64_t)w * kMaxMoves + C) * kMaxCls + i];
+    // entry 0 always set: lanes without a class read (and discard) class 0's data
+    for (uint32_t i = threadIdx.x; i < max(nc, 1u); i += blockDim.x) sent[i] = cls_entry(W, R, gid, w, i);
+    __syncthreads();
     if (STAGED) {
         typedef typename std::conditional<sizeof(T) == 4, float4, double2>::type VecS;
         constexpr int VS = sizeof(VecS) / sizeof(T);
-        const T* src = cls + (uint64_t)w * kMaxCls * kClsStride;
         for (uint32_t i = threadIdx.x; i < nc * (512 / VS); i += blockDim.x) {
             const uint32_t c = i / (512 / VS), e = (i % (512 / VS)) * VS;
             *reinterpret_cast<VecS*>(cls_s + c * kStagedStride + e) =
-                __ldg(reinterpret_cast<const VecS*>(src + (uint64_t)c * kClsStride + e));
+                __ldg(reinterpret_cast<const VecS*>(cls + sent[c] * kClsStride + e));
         }
+        __syncthreads();
     }
-    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t N = 1u << s;
     const uint64_t NN = (uint64_t)N * N;
@@ -780,7 +824,6 @@ __global__ void __launch_bounds__(kThreads) k_walk_step_cls(const WalkDev* __res
     const bool fresh = R.fresh != 0;
     const T scale = (T)R.scale;
     const T init = (T)(1.0 / sqrt((double)N));
-    const T* cbase = cls + (uint64_t)w * kMaxCls * kClsStride;
     T* myslots = slots + warp * nslot * 16;
     const uint32_t first = (blockIdx.x - W.cta0) * (uint32_t)kClsOrbitsPerCta;
     for (int it = 0; it < kClsOrbitsPerThread; ++it) {
@@ -822,7 +865,7 @@ __global__ void __launch_bounds__(kThreads) k_walk_step_cls(const WalkDev* __res
             for (int j = 0; j < 8; ++j) v[8 + j] = v[j];
         }
         const T wgt = single ? (T)0.5 : (T)1;
-        const T* cb = STAGED ? cls_s + (ci >= 0 ? ci : 0) * kStagedStride : cbase + (uint64_t)(ci >= 0 ? ci : 0) * kClsStride;
+        const T* cb = STAGED ? cls_s + (ci >= 0 ? ci : 0) * kStagedStride : cls + sent[ci >= 0 ? ci : 0] * kClsStride;
         T S[16];
         typedef typename std::conditional<sizeof(T) == 4, float4, double2>::type VecL;
         constexpr int VW = sizeof(VecL) / sizeof(T);  // elements per vector load
@@ -876,14 +919,15 @@ __global__ void __launch_bounds__(kThreads) k_walk_step_cls(const WalkDev* __res
 
 // g_k of a walk from its class sums (algo 1): g_k = sum_{c,i} N_{c,i} d_{c,k,i}.
 template <typename T>
-__device__ void cls_overlaps(const WalkDev& W, uint32_t nc, const double* __restrict__ npart, const T* __restrict__ cls,
-                             int w, int L, double* g, double (*gl)[kMaxL + 1]) {
+__device__ void cls_overlaps(const WalkDev& W, const WalkRec& R, uint32_t nc, const double* __restrict__ npart,
+                             const T* __restrict__ cls, const uint32_t* __restrict__ gid, int w, int L, double* g,
+                             double (*gl)[kMaxL + 1]) {
     const int t = threadIdx.x;  // kMaxL threads
     for (int k = 0; k < L; ++k) gl[t][k] = 0.0;
     for (uint32_t e = t; e < nc * 16u; e += kMaxL) {
         double Nv = 0.0;
         for (uint32_t c = 0; c < W.ncta; ++c) Nv += npart[(uint64_t)(W.cta0 + c) * kMaxCls * 16 + e];
-        const T* d = cls + ((uint64_t)w * kMaxCls + e / 16) * kClsStride + 512 + (e & 15);
+        const T* d = cls + cls_entry(W, R, gid, w, e / 16) * kClsStride + 512 + (e & 15);
         for (int k = 0; k < L; ++k) gl[t][k] += Nv * (double)d[k * 16];
     }
     __syncthreads();
@@ -898,7 +942,8 @@ __device__ void cls_overlaps(const WalkDev& W, uint32_t nc, const double* __rest
 __global__ void k_walk_measure(const WalkDev* __restrict__ walks, WalkRec* __restrict__ recs,
                                const double* __restrict__ partial, const double* __restrict__ cos64,
                                double* __restrict__ trace, unsigned int* __restrict__ running, int algo,
-                               const uint32_t* __restrict__ ncls, const void* __restrict__ cls, int cls_f64) {
+                               const uint32_t* __restrict__ ncls, const void* __restrict__ cls,
+                               const uint32_t* __restrict__ gid, int cls_f64) {
     const int w = blockIdx.x;
     const WalkDev& W = walks[w];
     WalkRec& R = recs[w];
@@ -910,8 +955,8 @@ __global__ void k_walk_measure(const WalkDev* __restrict__ walks, WalkRec* __res
     const int t = threadIdx.x;
     if (algo == 1) {
         const uint32_t nc = ncls[(uint64_t)w * kMaxMoves + R.C];
-        if (cls_f64) cls_overlaps<double>(W, nc, partial, (const double*)cls, w, L, g, gl);
-        else cls_overlaps<float>(W, nc, partial, (const float*)cls, w, L, g, gl);
+        if (cls_f64) cls_overlaps<double>(W, R, nc, partial, (const double*)cls, gid, w, L, g, gl);
+        else cls_overlaps<float>(W, R, nc, partial, (const float*)cls, gid, w, L, g, gl);
     } else if (t < L) {
         double sum = 0.0;
         for (uint32_t c = 0; c < W.ncta; ++c) sum += partial[(uint64_t)(W.cta0 + c) * kMaxL + t];
@@ -1069,10 +1114,13 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
     if (precision != SQ_F64 && precision != SQ_F32) return wfail(SQ_ERR_ARG, "unknown precision");
     const size_t esz = precision == SQ_F64 ? 8 : 4;
     const uint32_t algo = walks[0].algo;
-    if (algo > 1) return wfail(SQ_ERR_ARG, "unknown walk algorithm (0: per-orbit iteration, 1: orbit classes)");
+    if (algo > 2)
+        return wfail(SQ_ERR_ARG, "unknown walk algorithm (0: per-orbit iteration, 1: orbit classes, 2: orbit classes "
+                                 "prepared per step)");
     for (uint32_t i = 1; i < nwalks; ++i)
         if (walks[i].algo != algo) return wfail(SQ_ERR_ARG, "all walks of a batch use one algorithm");
-    const uint32_t orbits_per_cta = algo == 1 ? (uint32_t)kClsOrbitsPerCta : (uint32_t)kOrbitsPerCta;
+    const bool classes = algo >= 1;
+    const uint32_t orbits_per_cta = classes ? (uint32_t)kClsOrbitsPerCta : (uint32_t)kOrbitsPerCta;
     std::vector<WalkDev> wd(nwalks);
     std::vector<int> energies;
     std::vector<int> cta_walk;
@@ -1139,7 +1187,15 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
     uint32_t* d_ncls = nullptr;
     void* d_cls = nullptr;
     int* d_jobs = nullptr;
+    uint32_t* d_gid = nullptr;
+    unsigned long long* d_gkeys = nullptr;
+    double* d_sbeta = nullptr;
+    int* d_sq = nullptr;
     auto cleanup = [&]() {
+        cudaFree(d_gid);
+        cudaFree(d_gkeys);
+        cudaFree(d_sbeta);
+        cudaFree(d_sq);
         cudaFree(d_keys);
         cudaFree(d_ncls);
         cudaFree(d_cls);
@@ -1160,12 +1216,11 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
               cudaMalloc(&d_cta, sizeof(int) * nct) == cudaSuccess &&
               cudaMalloc(&d_E, sizeof(int) * energies.size()) == cudaSuccess &&
               cudaMalloc(&d_states, esz * state_elems) == cudaSuccess &&
-              cudaMalloc(&d_partial, sizeof(double) * (algo == 1 ? (size_t)kMaxCls * 16 : (size_t)kMaxL) * nct) ==
+              cudaMalloc(&d_partial, sizeof(double) * (classes ? (size_t)kMaxCls * 16 : (size_t)kMaxL) * nct) ==
                   cudaSuccess &&
-              (algo == 0 ||
+              (!classes ||
                (cudaMalloc(&d_keys, sizeof(unsigned long long) * nwalks * kMaxMoves * kMaxCls) == cudaSuccess &&
                 cudaMalloc(&d_ncls, sizeof(uint32_t) * nwalks * kMaxMoves) == cudaSuccess &&
-                cudaMalloc(&d_cls, esz * nwalks * kMaxCls * kClsStride) == cudaSuccess &&
                 cudaMalloc(&d_jobs, sizeof(int) * 2 * nwalks * kMaxMoves) == cudaSuccess)) &&
               cudaMalloc(&d_cos, sizeof(double) * kMaxL) == cudaSuccess &&
               cudaMalloc(&d_running, sizeof(unsigned int)) == cudaSuccess &&
@@ -1195,7 +1250,9 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
     size_t prep_smem = 0, cls_smem = 0;
     int nslot = 1;
     bool staged = false;
-    if (err == cudaSuccess && algo == 1) {
+    bool tabled = false;
+    uint32_t tab_entries = 0, tab_slots = 0;
+    if (err == cudaSuccess && classes) {
         // the orbit classes of every (walk, move), once per batch
         std::vector<int> jw, jm;
         for (uint32_t i = 0; i < nwalks; ++i)
@@ -1224,28 +1281,118 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
                     cleanup();
                     return wfail(SQ_ERR_UNSUPPORTED, "more orbit classes than algorithm 1 holds (96); use algorithm 0");
                 }
+            // The class data depend only on (key, beta_k, q): one table for the batch,
+            // entry = key index * nslot + temperature slot, when it fits; otherwise
+            // (and for algo 2) per walk, prepared every step.
+            std::vector<unsigned long long> hk((size_t)nwalks * kMaxMoves * kMaxCls);
+            err = cudaMemcpyAsync(hk.data(), d_keys, sizeof(unsigned long long) * hk.size(), cudaMemcpyDeviceToHost, st);
+            if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+            std::vector<unsigned long long> gkeys;
+            std::unordered_map<unsigned long long, uint32_t> kid;
+            std::vector<uint32_t> gk((size_t)nwalks * kMaxMoves * kMaxCls, 0u);
+            std::map<std::tuple<uint64_t, uint32_t, int>, uint32_t> sched;  // (beta bits, stages, q) -> slot0
+            std::vector<double> sbeta;
+            std::vector<int> sq;
+            for (uint32_t i = 0; err == cudaSuccess && i < nwalks; ++i) {
+                for (uint32_t c = 0; c < walks[i].spins; ++c) {
+                    const size_t base = ((size_t)i * kMaxMoves + c) * kMaxCls;
+                    for (uint32_t k = 0; k < nc[(size_t)i * kMaxMoves + c]; ++k) {
+                        auto it = kid.find(hk[base + k]);
+                        if (it == kid.end()) {
+                            it = kid.emplace(hk[base + k], (uint32_t)gkeys.size()).first;
+                            gkeys.push_back(hk[base + k]);
+                        }
+                        gk[base + k] = it->second;
+                    }
+                }
+                uint64_t bbits;
+                std::memcpy(&bbits, &walks[i].beta, sizeof bbits);
+                const auto key = std::make_tuple(bbits, walks[i].stages, (int)walks[i].phase_qbits);
+                auto it = sched.find(key);
+                if (it == sched.end()) {
+                    it = sched.emplace(key, (uint32_t)sbeta.size()).first;
+                    // the stage temperatures exactly as the step loop forms them
+                    for (uint32_t j = 0; j < walks[i].stages; ++j) {
+                        sbeta.push_back((double)(j + 1) * walks[i].beta / (double)walks[i].stages);
+                        sq.push_back((int)walks[i].phase_qbits);
+                    }
+                }
+                wd[i].slot0 = it->second;
+            }
+            const uint64_t nslot_t = sbeta.size(), nentry = gkeys.size() * nslot_t;
+            size_t free_b = 0, total_b = 0;
+            cudaMemGetInfo(&free_b, &total_b);
+            const uint64_t tab_bytes = nentry * kClsStride * esz;
+            tabled = err == cudaSuccess && algo == 1 && nentry > 0 && nentry < (1ull << 31) &&
+                     tab_bytes <= std::min<uint64_t>(kTableBudget, free_b / 4);
+            if (err == cudaSuccess && tabled) {
+                for (size_t j = 0; j < gk.size(); ++j) gk[j] *= (uint32_t)nslot_t;
+                const bool aok = cudaMalloc(&d_cls, tab_bytes) == cudaSuccess &&
+                                 cudaMalloc(&d_gid, sizeof(uint32_t) * gk.size()) == cudaSuccess &&
+                                 cudaMalloc(&d_gkeys, sizeof(unsigned long long) * gkeys.size()) == cudaSuccess &&
+                                 cudaMalloc(&d_sbeta, sizeof(double) * nslot_t) == cudaSuccess &&
+                                 cudaMalloc(&d_sq, sizeof(int) * nslot_t) == cudaSuccess;
+                if (!aok) {
+                    cudaGetLastError();
+                    err = cudaErrorMemoryAllocation;
+                }
+                if (err == cudaSuccess)
+                    err = cudaMemcpyAsync(d_gid, gk.data(), sizeof(uint32_t) * gk.size(), cudaMemcpyHostToDevice, st);
+                if (err == cudaSuccess)
+                    err = cudaMemcpyAsync(d_gkeys, gkeys.data(), sizeof(unsigned long long) * gkeys.size(),
+                                          cudaMemcpyHostToDevice, st);
+                if (err == cudaSuccess)
+                    err = cudaMemcpyAsync(d_sbeta, sbeta.data(), sizeof(double) * nslot_t, cudaMemcpyHostToDevice, st);
+                if (err == cudaSuccess) err = cudaMemcpyAsync(d_sq, sq.data(), sizeof(int) * nslot_t, cudaMemcpyHostToDevice, st);
+                // slot0 joins the walk records on the device
+                if (err == cudaSuccess)
+                    err = cudaMemcpyAsync(d_walks, wd.data(), sizeof(WalkDev) * nwalks, cudaMemcpyHostToDevice, st);
+                tab_entries = (uint32_t)nentry;
+                tab_slots = (uint32_t)nslot_t;
+            } else if (err == cudaSuccess) {
+                if (cudaMalloc(&d_cls, esz * nwalks * kMaxCls * kClsStride) != cudaSuccess) {
+                    cudaGetLastError();
+                    err = cudaErrorMemoryAllocation;
+                }
+            }
             nslot = 1;
             for (size_t j = 0; j < nj; ++j) nslot = std::max<int>(nslot, (int)nc[(size_t)jw[j] * kMaxMoves + jm[j]]);
             prep_smem = esz * (kPrepThreads / 32) * 5 * 16 * 17;
             const size_t base_smem = esz * ((kThreads / 32) * (size_t)nslot * 16 + (kThreads / 32) * 32 * 16) +
-                                     sizeof(int) * (kThreads / 32) * 32 + 16 + sizeof(unsigned long long) * kMaxCls;
+                                     sizeof(int) * (kThreads / 32) * 32 + 16 + 2 * sizeof(unsigned long long) * kMaxCls;
             const size_t staged_smem = base_smem + esz * (size_t)nslot * kStagedStride;
             int optin = 0;
             cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0);
             staged = precision == SQ_F32 && staged_smem <= (size_t)optin;
             cls_smem = staged ? staged_smem : base_smem;
-            if (precision == SQ_F64) {
-                err = cudaFuncSetAttribute(k_cls_prep<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
+            if (err == cudaSuccess && precision == SQ_F64) {
+                err = tabled ? cudaFuncSetAttribute(k_cls_table<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)prep_smem)
+                             : cudaFuncSetAttribute(k_cls_prep<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)prep_smem);
                 if (err == cudaSuccess)
                     err = cudaFuncSetAttribute(k_walk_step_cls<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)cls_smem);
-            } else {
-                err = cudaFuncSetAttribute(k_cls_prep<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
+            } else if (err == cudaSuccess) {
+                err = tabled ? cudaFuncSetAttribute(k_cls_table<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)prep_smem)
+                             : cudaFuncSetAttribute(k_cls_prep<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)prep_smem);
                 if (err == cudaSuccess)
                     err = staged ? cudaFuncSetAttribute(k_walk_step_cls<float, true>,
                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cls_smem)
                                  : cudaFuncSetAttribute(k_walk_step_cls<float, false>,
                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cls_smem);
+            }
+            if (err == cudaSuccess && tabled) {
+                const unsigned grid = (tab_entries + kPrepThreads / 32 - 1) / (kPrepThreads / 32);
+                if (precision == SQ_F64)
+                    k_cls_table<double><<<grid, kPrepThreads, prep_smem, st>>>(d_gkeys, d_sbeta, d_sq, tab_slots,
+                                                                               tab_entries, (double*)d_cls);
+                else
+                    k_cls_table<float><<<grid, kPrepThreads, prep_smem, st>>>(d_gkeys, d_sbeta, d_sq, tab_slots,
+                                                                              tab_entries, (float*)d_cls);
+                err = cudaGetLastError();
             }
         }
     }
@@ -1257,21 +1404,26 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
     while (err == cudaSuccess && left > 0 && iter < max_cap) {
         const uint32_t q = std::min(chunk, max_cap - iter);
         for (uint32_t k = 0; k < q && err == cudaSuccess; ++k) {
-            if (algo == 1) {
+            if (classes) {
                 if (precision == SQ_F64) {
-                    k_cls_prep<double><<<nwalks, kPrepThreads, prep_smem, st>>>(d_walks, d_recs, d_keys, d_ncls, (double*)d_cls);
+                    if (!tabled)
+                        k_cls_prep<double><<<nwalks, kPrepThreads, prep_smem, st>>>(d_walks, d_recs, d_keys, d_ncls,
+                                                                                    (double*)d_cls);
                     k_walk_step_cls<double, false><<<(unsigned)nct, kThreads, cls_smem, st>>>(
-                        d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const double*)d_cls, (double*)d_states, d_partial, nslot);
+                        d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const double*)d_cls, d_gid, (double*)d_states,
+                        d_partial, nslot);
                 } else {
-                    k_cls_prep<float><<<nwalks, kPrepThreads, prep_smem, st>>>(d_walks, d_recs, d_keys, d_ncls, (float*)d_cls);
+                    if (!tabled)
+                        k_cls_prep<float><<<nwalks, kPrepThreads, prep_smem, st>>>(d_walks, d_recs, d_keys, d_ncls,
+                                                                                   (float*)d_cls);
                     if (staged)
                         k_walk_step_cls<float, true><<<(unsigned)nct, kThreads, cls_smem, st>>>(
-                            d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const float*)d_cls, (float*)d_states, d_partial,
-                            nslot);
+                            d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const float*)d_cls, d_gid, (float*)d_states,
+                            d_partial, nslot);
                     else
                         k_walk_step_cls<float, false><<<(unsigned)nct, kThreads, cls_smem, st>>>(
-                            d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const float*)d_cls, (float*)d_states, d_partial,
-                            nslot);
+                            d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const float*)d_cls, d_gid, (float*)d_states,
+                            d_partial, nslot);
                 }
             } else if (precision == SQ_F64) {
                 k_walk_step<double><<<(unsigned)nct, kThreads, 0, st>>>(d_walks, d_cta, d_recs, d_E,
@@ -1282,8 +1434,8 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
             }
             err = cudaGetLastError();
             if (err != cudaSuccess) break;
-            k_walk_measure<<<nwalks, kMaxL, 0, st>>>(d_walks, d_recs, d_partial, d_cos, d_trace, d_running, (int)algo,
-                                                     d_ncls, d_cls, precision == SQ_F64 ? 1 : 0);
+            k_walk_measure<<<nwalks, kMaxL, 0, st>>>(d_walks, d_recs, d_partial, d_cos, d_trace, d_running,
+                                                     classes ? 1 : 0, d_ncls, d_cls, d_gid, precision == SQ_F64 ? 1 : 0);
             err = cudaGetLastError();
         }
         iter += q;

@@ -27,7 +27,7 @@ class QsaWalk:
     phase_qbits: int = 6
     seed: int = 1
     max_steps: int = 0
-    algo: int = 0  # 0: iterate W per orbit; 1: per orbit class (see sq_qsa_walk)
+    algo: int = 0  # 0: iterate W per orbit; 1: per orbit class; 2: 1 prepared per step (see sq_qsa_walk)
 
     @property
     def cap(self) -> int:
@@ -128,7 +128,7 @@ if __name__ == "__main__":
     ap.add_argument("--f64-walks", type=int, default=64)
     ap.add_argument("--stages", type=int, default=50)
     ap.add_argument("--steps-per-stage", type=int, default=20)
-    ap.add_argument("--algo", type=int, default=1, help="0: iterate W per orbit; 1: per orbit class")
+    ap.add_argument("--algo", type=int, default=1, help="0: iterate W per orbit; 1: per orbit class; 2: classes prepared per step")
     a = ap.parse_args()
     print(json.dumps(config4_study(a.walks, a.f64_walks, stages=a.stages, steps_per_stage=a.steps_per_stage,
                                    algo=a.algo)))

@@ -83,12 +83,12 @@ def test_walk_batch_rejects_bad_arguments_before_any_device_call():
         a.update(kw)
         J = kw.get("J", [1] * 12)
         return _lib.SqQsaWalk(a["spins"], a["phase_qbits"], a["stages"], a["steps_per_stage"], a["max_steps"],
-                              (ctypes.c_int32 * 12)(*J), 0, a["beta"], a["seed"])
+                              (ctypes.c_int32 * 12)(*J), kw.get("algo", 0), a["beta"], a["seed"])
 
     for bad, msg in ((dict(spins=13), b"ring length"), (dict(spins=1), b"ring length"),
                      (dict(phase_qbits=7), b"walk-phase"), (dict(phase_qbits=0), b"walk-phase"),
                      (dict(stages=0), b"schedule"), (dict(beta=-1.0), b"beta"),
-                     (dict(J=[9] + [1] * 11), b"couplings")):
+                     (dict(J=[9] + [1] * 11), b"couplings"), (dict(algo=3), b"algorithm")):
         w[0] = walk(**bad)
         assert L.sq_qsa_walk_batch(w, 1, _lib.SQ_F32, res, None, ctypes.byref(ms)) == _lib.SQ_ERR_ARG, bad
         assert msg in L.sq_last_error(), (bad, L.sq_last_error())

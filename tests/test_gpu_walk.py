@@ -145,3 +145,24 @@ def test_orbit_class_algorithm_on_ten_spin_rings_matches_iteration():
                 same += 1
                 assert np.max(np.abs(a.p0 - b.p0)) < tol
         assert same >= (12 if prec == "f64" else 11)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_class_table_matches_per_step_preparation(precision):
+    """Algorithm 1 reads the class data from one table per batch (key x stage
+    temperature), algorithm 2 prepares them per walk and step: the same
+    arithmetic on the same inputs, so the walks agree bit for bit, with mixed
+    schedules (beta, stages, walk-phase width) and rings sharing schedules."""
+    from suqa_gb300.walk import ising_ring_walks, run_qsa_walks
+    mixed = _walks(10, 17, spins=(3, 9), q=(1, 7), J=(-1, 2))
+    for w in mixed:
+        w.J = [v if v != 0 else 1 for v in w.J]
+    rings = ising_ring_walks(6, 10, 1.0, 3, 2, 6, seed=4)
+    runs = {}
+    for algo in (1, 2):
+        for w in mixed + rings:
+            w.algo = algo
+        runs[algo], _ = run_qsa_walks(mixed + rings, precision, trace=True)
+    for a, b in zip(runs[1], runs[2]):
+        assert (a.done, a.restarts, a.steps, a.readout, a.last_p0) == (b.done, b.restarts, b.steps, b.readout, b.last_p0)
+        assert np.array_equal(a.p0, b.p0)

@@ -917,6 +917,304 @@ __global__ void __launch_bounds__(kThreads) k_walk_step_cls(const WalkDev* __res
     }
 }
 
+// FP32 orbit pass of algo 1 with the orbits sorted by class.  The CTA takes its
+// orbits in chunks of kSortChunk, one orbit per thread: coalesced loads (the next
+// chunk's in flight while this chunk's products run), a stable counting sort in
+// shared memory by q = 2 class + (8-amplitude orbit) (per-warp counts from
+// __match_any_sync, offsets over keys then warps), then each warp walks a
+// contiguous range of the sorted chunk run by run, with the run's class rows in
+// registers: lane l < 16 holds row l of V^T (y_l = v_l^T psi), lane 16 + i row i
+// of Q (S_i).  The 16 amplitudes of an orbit are one broadcast read; lanes < 16
+// keep the class sums of w y^2 in a register until the class changes (w = 1/2 for
+// 8-amplitude orbits, constant over a run).  Each class row is read once per run
+// instead of once per orbit.  S returns to the thread that loaded the orbit and
+// is stored coalesced.  Orbit classes come from a 256-slot hash of the class keys.
+constexpr int kSortChunk = kThreads;
+constexpr int kWarps = kThreads / 32;
+constexpr int kHash = 256;
+
+__device__ __forceinline__ uint32_t cls_hash(unsigned long long key) {
+    return (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> 56);
+}
+
+// Class (-1 past the walk's orbits), state index of amplitude 0 and the 16
+// amplitudes of orbit o.  Index of amplitude (a, b, c, acc): b0 ^ (a ? dp) ^
+// (b ? e_C) ^ (c ? e_C << s) ^ (acc ? 1 << 2s), the bits of (acc, d, x).
+__device__ __forceinline__ void sorted_fetch(uint32_t o, uint32_t norb, int s, int C, uint32_t eC, const int* __restrict__ E,
+                                             const unsigned long long* htab, const float* __restrict__ st, bool fresh,
+                                             float scale, float init, int& ci, bool& single, uint32_t& b0, uint32_t& dp,
+                                             float (&v)[16]) {
+    ci = -1;
+    single = true;
+    uint32_t x0 = 0;
+    dp = 0;
+    if (o < norb) {
+        single = orbit_decode(o, s, C, dp, x0);
+        const unsigned long long key = orbit_key(E, x0, dp, eC);
+        uint32_t h = cls_hash(key);
+        for (int probe = 0; probe < kHash; ++probe) {  // bounded; the table is at most 3/8 full
+            const unsigned long long e = htab[h];
+            if (e == 0ull) break;
+            if ((e >> 8) == key) {
+                ci = (int)(e & 255ull);
+                break;
+            }
+            h = (h + 1u) & (kHash - 1);
+        }
+    }
+    b0 = (dp << s) | x0;
+    const uint32_t mc = eC << s, macc = 1u << (2 * s);
+#pragma unroll
+    for (int pos = 0; pos < 8; ++pos) {
+        const int a = pos >> 2, b = (pos >> 1) & 1, c = pos & 1;
+        const uint32_t i0 = b0 ^ (a ? dp : 0u) ^ (b ? eC : 0u) ^ (c ? mc : 0u);
+#pragma unroll
+        for (int acc = 0; acc < 2; ++acc) {
+            float val = 0.f;
+            if (ci >= 0) {
+                if (fresh) val = (single && c == 0 && acc == 0) ? init : 0.f;
+                else if (!(single && a == 1)) val = st[i0 ^ (acc ? macc : 0u)] * scale;
+            }
+            v[SLOT(a, b, c, acc)] = val;
+        }
+    }
+    if (single) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[8 + j] = v[j];
+    }
+}
+
+__device__ __forceinline__ void sorted_row(const float* vrow, f2 (&v)[8]) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const ulonglong2 q = *reinterpret_cast<const ulonglong2*>(vrow + 4 * u);
+        v[2 * u] = q.x;
+        v[2 * u + 1] = q.y;
+    }
+}
+
+// row . v with the pairs (2m, 2m+1) in packed f32x2: two chains of four, then the halves
+__device__ __forceinline__ float sorted_dot(const f2 (&r)[8], const f2 (&v)[8]) {
+    f2 ea = mul2(r[0], v[0]), eb = mul2(r[1], v[1]);
+#pragma unroll
+    for (int m = 1; m < 4; ++m) {
+        ea = fma2(r[2 * m], v[2 * m], ea);
+        eb = fma2(r[2 * m + 1], v[2 * m + 1], eb);
+    }
+    float x, y;
+    up2(add2(ea, eb), x, y);
+    return x + y;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
+                                                               const WalkRec* __restrict__ recs, const int* __restrict__ energies,
+                                                               const unsigned long long* __restrict__ keys,
+                                                               const uint32_t* __restrict__ ncls, const float* __restrict__ cls,
+                                                               const uint32_t* __restrict__ gid, float* __restrict__ states,
+                                                               double* __restrict__ npart, int nslot) {
+    const int w = cta_walk[blockIdx.x];
+    const WalkDev& W = walks[w];
+    const WalkRec& R = recs[w];
+    if (R.status != 0) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    // nslot: classes per slot array (the batch's largest class count, <= kMaxCls = 96);
+    // nk = 2 nslot sort keys, at most 6 per lane of one warp
+    const int nk = 2 * nslot;
+    float* cls_s = reinterpret_cast<float*>(smem_raw);              // [nslot][512]: V^T rows, then Q rows
+    float* slots = cls_s + nslot * 512;                              // [warps][nslot][16]
+    float* vbuf = slots + kWarps * nslot * 16;                       // [kSortChunk][16] amplitudes, sorted
+    float* sbuf = vbuf + kSortChunk * 16;                            // [kSortChunk][16] S, sorted
+    unsigned long long* htab = reinterpret_cast<unsigned long long*>(sbuf + kSortChunk * 16);  // [kHash] key << 8 | class
+    unsigned long long* sent = htab + kHash;                         // [kMaxCls] class data entries
+    int* wcnt = reinterpret_cast<int*>(sent + kMaxCls);              // [warps][nk] counts, then positions
+    int* kend = wcnt + kWarps * nk;                                  // [nk] end of each key's run
+    int* nact_s = kend + nk;
+    unsigned char* csort = reinterpret_cast<unsigned char*>(nact_s + 4);  // [kSortChunk] key of each sorted orbit
+    const int s = W.s, C = (int)R.C;
+    const uint32_t nc = ncls[(uint64_t)w * kMaxMoves + C];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < kWarps * nslot * 16; i += kThreads) slots[i] = 0.f;
+    for (int i = threadIdx.x; i < kHash; i += kThreads) htab[i] = 0ull;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < nc; i += kThreads) {
+        const unsigned long long key = keys[((uint64_t)w * kMaxMoves + C) * kMaxCls + i];
+        uint32_t h = cls_hash(key);
+        for (int probe = 0; probe < kHash; ++probe) {  // distinct keys, nc <= 96 < kHash: always placed
+            if (atomicCAS(&htab[h], 0ull, (key << 8) | (unsigned long long)i) == 0ull) break;
+            h = (h + 1u) & (kHash - 1);
+        }
+    }
+    // entry 0 always set: lanes without a class never read class data, but keep it valid
+    for (uint32_t i = threadIdx.x; i < max(nc, 1u); i += kThreads) sent[i] = cls_entry(W, R, gid, w, i);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < nc * 128u; i += kThreads) {
+        const uint32_t c = i >> 7, e = (i & 127u) * 4u;
+        *reinterpret_cast<float4*>(cls_s + c * 512 + e) = __ldg(reinterpret_cast<const float4*>(cls + sent[c] * kClsStride + e));
+    }
+    const uint32_t norb = norbits(s), eC = 1u << C;
+    const uint32_t mc = eC << s, macc = 1u << (2 * s);
+    const int* E = energies + W.e_off;
+    float* st = states + W.state_off;
+    const bool fresh = R.fresh != 0;
+    const float scale = (float)R.scale;
+    const float init = (float)(1.0 / sqrt((double)(1u << s)));
+    float* myslots = slots + warp * nslot * 16;
+    const uint32_t first = (blockIdx.x - W.cta0) * (uint32_t)kClsOrbitsPerCta;
+    constexpr int kChunks = kClsOrbitsPerCta / kSortChunk;
+    const int row = lane & 15, part = lane >> 4;  // part 0: V^T row, 1: Q row
+
+    int ci_n;
+    bool single_n;
+    uint32_t b0_n, dp_n;
+    float vn[16];
+    sorted_fetch(first + threadIdx.x, norb, s, C, eC, E, htab, st, fresh, scale, init, ci_n, single_n, b0_n, dp_n, vn);
+    for (int k = 0; k < kChunks; ++k) {
+        const uint32_t cbase = first + (uint32_t)(k * kSortChunk);
+        if (cbase >= norb) break;  // uniform over the CTA
+        const int ci = ci_n;
+        const bool single = single_n;
+        const uint32_t b0 = b0_n, dp = dp_n;
+        const int q = ci >= 0 ? 2 * ci + (single ? 1 : 0) : -1;
+        // per-warp key counts; the first lane of each key group writes its size
+        for (int c = lane; c < nk; c += 32) wcnt[warp * nk + c] = 0;
+        __syncwarp();
+        const unsigned grp = __match_any_sync(0xffffffffu, q);
+        const int rank = __popc(grp & ((1u << lane) - 1u));
+        if (q >= 0 && rank == 0) wcnt[warp * nk + q] = __popc(grp);
+        __syncthreads();
+        if (warp == 0) {  // positions: keys in order, warps in order within a key
+            int tot[6];
+#pragma unroll
+            for (int j = 0; j < 6; ++j) {
+                const int c = lane * 6 + j;
+                int run = 0;
+                if (c < nk) {
+                    for (int wp = 0; wp < kWarps; ++wp) {
+                        const int t = wcnt[wp * nk + c];
+                        wcnt[wp * nk + c] = run;
+                        run += t;
+                    }
+                }
+                tot[j] = run;
+            }
+            int lsum = 0;
+#pragma unroll
+            for (int j = 0; j < 6; ++j) lsum += tot[j];
+            int incl = lsum;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += y;
+            }
+            int base = incl - lsum;
+#pragma unroll
+            for (int j = 0; j < 6; ++j) {
+                const int c = lane * 6 + j;
+                if (c < nk) {
+                    for (int wp = 0; wp < kWarps; ++wp) wcnt[wp * nk + c] += base;
+                    kend[c] = base + tot[j];
+                }
+                base += tot[j];
+            }
+            if (lane == 31) *nact_s = incl;
+        }
+        __syncthreads();
+        int pos = -1;
+        if (q >= 0) {
+            pos = wcnt[warp * nk + q] + rank;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                *reinterpret_cast<float4*>(vbuf + pos * 16 + 4 * u) = make_float4(vn[4 * u], vn[4 * u + 1], vn[4 * u + 2], vn[4 * u + 3]);
+            csort[pos] = (unsigned char)q;
+        }
+        __syncthreads();
+        if (k + 1 < kChunks)  // the next chunk's loads overlap this chunk's products
+            sorted_fetch(cbase + kSortChunk + threadIdx.x, norb, s, C, eC, E, htab, st, fresh, scale, init, ci_n, single_n,
+                         b0_n, dp_n, vn);
+        {
+            const int nact = *nact_s;
+            const int p1 = nact * (warp + 1) / kWarps;
+            int p = nact * warp / kWarps;
+            int cur = -1;
+            float nacc = 0.f;
+            f2 r[8];
+#pragma unroll
+            for (int m = 0; m < 8; ++m) r[m] = 0ull;
+            while (p < p1) {  // one run (one key) per iteration; uniform over the warp
+                const int qq = csort[p];
+                const int e = max(min(kend[qq], p1), p + 1);  // p lies in its key's run: kend[qq] > p
+                const float wt = (qq & 1) ? 0.5f : 1.f;
+                if ((qq >> 1) != cur) {
+                    if (cur >= 0 && part == 0) myslots[cur * 16 + row] += nacc;
+                    nacc = 0.f;
+                    cur = qq >> 1;
+                    const ulonglong2* rp = reinterpret_cast<const ulonglong2*>(cls_s + cur * 512 + lane * 16);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const ulonglong2 t = rp[u];
+                        r[2 * u] = t.x;
+                        r[2 * u + 1] = t.y;
+                    }
+                }
+                for (; p + 4 <= e; p += 4) {
+                    f2 v0[8], v1[8], v2[8], v3[8];
+                    sorted_row(vbuf + p * 16, v0);
+                    sorted_row(vbuf + p * 16 + 16, v1);
+                    sorted_row(vbuf + p * 16 + 32, v2);
+                    sorted_row(vbuf + p * 16 + 48, v3);
+                    const float y0 = sorted_dot(r, v0), y1 = sorted_dot(r, v1);
+                    const float y2 = sorted_dot(r, v2), y3 = sorted_dot(r, v3);
+                    if (part == 0) {
+                        nacc += wt * y0 * y0;
+                        nacc += wt * y1 * y1;
+                        nacc += wt * y2 * y2;
+                        nacc += wt * y3 * y3;
+                    } else {
+                        sbuf[p * 16 + row] = y0;
+                        sbuf[p * 16 + 16 + row] = y1;
+                        sbuf[p * 16 + 32 + row] = y2;
+                        sbuf[p * 16 + 48 + row] = y3;
+                    }
+                }
+                for (; p < e; ++p) {
+                    f2 v0[8];
+                    sorted_row(vbuf + p * 16, v0);
+                    const float y0 = sorted_dot(r, v0);
+                    if (part == 0) nacc += wt * y0 * y0;
+                    else sbuf[p * 16 + row] = y0;
+                }
+            }
+            if (cur >= 0 && part == 0) myslots[cur * 16 + row] += nacc;
+        }
+        __syncthreads();
+        if (q >= 0) {
+            float S[16];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float4 t = *reinterpret_cast<const float4*>(sbuf + pos * 16 + 4 * u);
+                S[4 * u] = t.x;
+                S[4 * u + 1] = t.y;
+                S[4 * u + 2] = t.z;
+                S[4 * u + 3] = t.w;
+            }
+#pragma unroll
+            for (int pp = 0; pp < 8; ++pp) {
+                const int a = pp >> 2, b = (pp >> 1) & 1, c = pp & 1;
+                if (single && a == 1) continue;
+                const uint32_t i0 = b0 ^ (a ? dp : 0u) ^ (b ? eC : 0u) ^ (c ? mc : 0u);
+                st[i0] = S[SLOT(a, b, c, 0)];
+                st[i0 ^ macc] = S[SLOT(a, b, c, 1)];
+            }
+        }
+    }
+    __syncthreads();
+    for (uint32_t e = threadIdx.x; e < nc * 16u; e += blockDim.x) {
+        double sum = 0.0;
+        for (int wp = 0; wp < kWarps; ++wp) sum += (double)slots[wp * nslot * 16 + e];
+        npart[(uint64_t)blockIdx.x * kMaxCls * 16 + e] = sum;
+    }
+}
+
 // g_k of a walk from its class sums (algo 1): g_k = sum_{c,i} N_{c,i} d_{c,k,i}.
 template <typename T>
 __device__ void cls_overlaps(const WalkDev& W, const WalkRec& R, uint32_t nc, const double* __restrict__ npart,
@@ -1249,7 +1547,7 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
     }
     size_t prep_smem = 0, cls_smem = 0;
     int nslot = 1;
-    bool staged = false;
+    bool staged = false, sorted = false;
     bool tabled = false;
     uint32_t tab_entries = 0, tab_slots = 0;
     if (err == cudaSuccess && classes) {
@@ -1361,10 +1659,15 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
             const size_t base_smem = esz * ((kThreads / 32) * (size_t)nslot * 16 + (kThreads / 32) * 32 * 16) +
                                      sizeof(int) * (kThreads / 32) * 32 + 16 + 2 * sizeof(unsigned long long) * kMaxCls;
             const size_t staged_smem = base_smem + esz * (size_t)nslot * kStagedStride;
+            const size_t sorted_smem =
+                sizeof(float) * ((size_t)nslot * 512 + (size_t)kWarps * nslot * 16 + 2 * (size_t)kSortChunk * 16) +
+                sizeof(unsigned long long) * (kHash + kMaxCls) + sizeof(int) * ((size_t)(kWarps + 1) * 2 * nslot + 4) +
+                kSortChunk;
             int optin = 0;
             cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0);
-            staged = precision == SQ_F32 && staged_smem <= (size_t)optin;
-            cls_smem = staged ? staged_smem : base_smem;
+            sorted = precision == SQ_F32 && sorted_smem <= (size_t)optin;
+            staged = !sorted && precision == SQ_F32 && staged_smem <= (size_t)optin;
+            cls_smem = sorted ? sorted_smem : staged ? staged_smem : base_smem;
             if (err == cudaSuccess && precision == SQ_F64) {
                 err = tabled ? cudaFuncSetAttribute(k_cls_table<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     (int)prep_smem)
@@ -1379,10 +1682,12 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
                              : cudaFuncSetAttribute(k_cls_prep<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     (int)prep_smem);
                 if (err == cudaSuccess)
-                    err = staged ? cudaFuncSetAttribute(k_walk_step_cls<float, true>,
-                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cls_smem)
-                                 : cudaFuncSetAttribute(k_walk_step_cls<float, false>,
-                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cls_smem);
+                    err = sorted   ? cudaFuncSetAttribute(k_walk_step_sorted, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                          (int)cls_smem)
+                          : staged ? cudaFuncSetAttribute(k_walk_step_cls<float, true>,
+                                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cls_smem)
+                                   : cudaFuncSetAttribute(k_walk_step_cls<float, false>,
+                                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cls_smem);
             }
             if (err == cudaSuccess && tabled) {
                 const unsigned grid = (tab_entries + kPrepThreads / 32 - 1) / (kPrepThreads / 32);
@@ -1416,7 +1721,11 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
                     if (!tabled)
                         k_cls_prep<float><<<nwalks, kPrepThreads, prep_smem, st>>>(d_walks, d_recs, d_keys, d_ncls,
                                                                                    (float*)d_cls);
-                    if (staged)
+                    if (sorted)
+                        k_walk_step_sorted<<<(unsigned)nct, kThreads, cls_smem, st>>>(
+                            d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const float*)d_cls, d_gid, (float*)d_states,
+                            d_partial, nslot);
+                    else if (staged)
                         k_walk_step_cls<float, true><<<(unsigned)nct, kThreads, cls_smem, st>>>(
                             d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const float*)d_cls, d_gid, (float*)d_states,
                             d_partial, nslot);

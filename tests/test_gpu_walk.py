@@ -166,3 +166,15 @@ def test_class_table_matches_per_step_preparation(precision):
     for a, b in zip(runs[1], runs[2]):
         assert (a.done, a.restarts, a.steps, a.readout, a.last_p0) == (b.done, b.restarts, b.steps, b.readout, b.last_p0)
         assert np.array_equal(a.p0, b.p0)
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-9), ("f32", 5e-5)])
+def test_orbit_class_algorithm_with_many_classes(precision, tol):
+    """5-spin rings with couplings +-1, +-2 have 76-78 classes per move: FP32
+    then takes the orbit pass that reads every class through its own lane
+    (the class-sorted pass holds at most about 75 classes in shared memory)."""
+    from suqa_gb300.walk import QsaWalk, run_qsa_walks
+    rings = [[-2, 1, 1, -2, -2], [-1, -2, -1, -2, 2], [1, 1, -2, -1, -2], [2, -1, -2, -1, 1], [2, 2, -1, 2, -1]]
+    walks = [QsaWalk(5, J, 0.5 + 0.3 * k, 3, 3, 1 + k, 700 + k, algo=1) for k, J in enumerate(rings)]
+    runs, _ = run_qsa_walks(walks, precision, trace=True)
+    _check(runs, walks, tol)

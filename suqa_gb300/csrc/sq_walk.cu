@@ -937,20 +937,53 @@ __device__ __forceinline__ uint32_t cls_hash(unsigned long long key) {
     return (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> 56);
 }
 
-// Class (-1 past the walk's orbits), state index of amplitude 0 and the 16
-// amplitudes of orbit o.  Index of amplitude (a, b, c, acc): b0 ^ (a ? dp) ^
-// (b ? e_C) ^ (c ? e_C << s) ^ (acc ? 1 << 2s), the bits of (acc, d, x).
-__device__ __forceinline__ void sorted_fetch(uint32_t o, uint32_t norb, int s, int C, uint32_t eC, const int* __restrict__ E,
-                                             const unsigned long long* htab, const float* __restrict__ st, bool fresh,
-                                             float scale, float init, int& ci, bool& single, uint32_t& b0, uint32_t& dp,
-                                             float (&v)[16]) {
-    ci = -1;
-    single = true;
-    uint32_t x0 = 0;
-    dp = 0;
-    if (o < norb) {
-        single = orbit_decode(o, s, C, dp, x0);
-        const unsigned long long key = orbit_key(E, x0, dp, eC);
+// Orbit o of the chunk in two halves, so that no instruction waits on the loads
+// before this chunk's products have run: sorted_issue decodes the orbit and
+// issues its loads (the 8 energies of its key, its 16 amplitudes, read even on a
+// fresh start and for orbits past the walk's end, whose indices stay inside the
+// walk's state, and then dropped), sorted_finish forms the key, looks up
+// the class (-1 past the end) and the amplitudes.  State index of amplitude
+// (a, b, c, acc): b0 ^ (a ? dp) ^ (b ? e_C) ^ (c ? e_C << s) ^ (acc ? 1 << 2s),
+// the bits of (acc, d, x).
+struct SortedLoad {
+    uint32_t b0, dp;
+    bool active, single;
+    int e[8];
+    float raw[16];
+};
+
+__device__ __forceinline__ void sorted_issue(uint32_t o, uint32_t norb, int s, int C, uint32_t eC, const int* __restrict__ E,
+                                             const float* __restrict__ st, SortedLoad& L) {
+    uint32_t x0 = 0, dp = 0;
+    L.active = o < norb;
+    L.single = true;
+    if (L.active) L.single = orbit_decode(o, s, C, dp, x0);
+    L.b0 = (dp << s) | x0;
+    L.dp = dp;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {  // the terms of orbit_key: dE at x = x0 ^ (j&1 ? e_C), d = dp ^ (j&2 ? e_C)
+        const uint32_t x = x0 ^ ((j & 1) ? eC : 0u);
+        const uint32_t d = dp ^ ((j & 2) ? eC : 0u);
+        L.e[2 * j] = __ldg(E + (x ^ d));
+        L.e[2 * j + 1] = __ldg(E + x);
+    }
+    const uint32_t mc = eC << s, macc = 1u << (2 * s);
+#pragma unroll
+    for (int pos = 0; pos < 8; ++pos) {
+        const int a = pos >> 2, b = (pos >> 1) & 1, c = pos & 1;
+        const uint32_t i0 = L.b0 ^ (a ? dp : 0u) ^ (b ? eC : 0u) ^ (c ? mc : 0u);
+#pragma unroll
+        for (int acc = 0; acc < 2; ++acc) L.raw[SLOT(a, b, c, acc)] = st[i0 ^ (acc ? macc : 0u)];
+    }
+}
+
+__device__ __forceinline__ int sorted_finish(const SortedLoad& L, const unsigned long long* htab, bool fresh, float scale,
+                                             float init, float (&v)[16]) {
+    int ci = -1;
+    if (L.active) {
+        unsigned long long key = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) key |= (unsigned long long)(L.e[2 * j] - L.e[2 * j + 1] + 256) << (9 * j);
         uint32_t h = cls_hash(key);
         for (int probe = 0; probe < kHash; ++probe) {  // bounded; the table is at most 3/8 full
             const unsigned long long e = htab[h];
@@ -962,26 +995,23 @@ __device__ __forceinline__ void sorted_fetch(uint32_t o, uint32_t norb, int s, i
             h = (h + 1u) & (kHash - 1);
         }
     }
-    b0 = (dp << s) | x0;
-    const uint32_t mc = eC << s, macc = 1u << (2 * s);
 #pragma unroll
     for (int pos = 0; pos < 8; ++pos) {
-        const int a = pos >> 2, b = (pos >> 1) & 1, c = pos & 1;
-        const uint32_t i0 = b0 ^ (a ? dp : 0u) ^ (b ? eC : 0u) ^ (c ? mc : 0u);
+        const int a = pos >> 2, c = pos & 1;
 #pragma unroll
         for (int acc = 0; acc < 2; ++acc) {
-            float val = 0.f;
-            if (ci >= 0) {
-                if (fresh) val = (single && c == 0 && acc == 0) ? init : 0.f;
-                else if (!(single && a == 1)) val = st[i0 ^ (acc ? macc : 0u)] * scale;
-            }
-            v[SLOT(a, b, c, acc)] = val;
+            const int j = SLOT(a, (pos >> 1) & 1, c, acc);
+            float val;
+            if (fresh) val = (L.single && c == 0 && acc == 0) ? init : 0.f;
+            else val = (L.single && a == 1) ? 0.f : L.raw[j] * scale;
+            v[j] = val;
         }
     }
-    if (single) {
+    if (L.single) {
 #pragma unroll
         for (int j = 0; j < 8; ++j) v[8 + j] = v[j];
     }
+    return ci;
 }
 
 __device__ __forceinline__ void sorted_row(const float* vrow, f2 (&v)[8]) {
@@ -1026,9 +1056,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
     float* sbuf = vbuf + kSortChunk * 16;                            // [kSortChunk][16] S, sorted
     unsigned long long* htab = reinterpret_cast<unsigned long long*>(sbuf + kSortChunk * 16);  // [kHash] key << 8 | class
     unsigned long long* sent = htab + kHash;                         // [kMaxCls] class data entries
-    int* wcnt = reinterpret_cast<int*>(sent + kMaxCls);              // [warps][nk] counts, then positions
-    int* kend = wcnt + kWarps * nk;                                  // [nk] end of each key's run
-    int* nact_s = kend + nk;
+    int* wcnt = reinterpret_cast<int*>(sent + kMaxCls);              // [warps][nk] counts, then offsets within a key
+    int* kstart = wcnt + kWarps * nk;                                // [nk] start of each key's run
+    int* kend = kstart + nk;                                         // [nk] end of each key's run
+    int* wsum = kend + nk;                                           // [warps] key totals per warp of the scan
+    int* nact_s = wsum + kWarps;
     unsigned char* csort = reinterpret_cast<unsigned char*>(nact_s + 4);  // [kSortChunk] key of each sorted orbit
     const int s = W.s, C = (int)R.C;
     const uint32_t nc = ncls[(uint64_t)w * kMaxMoves + C];
@@ -1054,6 +1086,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
     const uint32_t norb = norbits(s), eC = 1u << C;
     const uint32_t mc = eC << s, macc = 1u << (2 * s);
     const int* E = energies + W.e_off;
+    const int kslot = threadIdx.x;  // the sort key this thread scans
     float* st = states + W.state_off;
     const bool fresh = R.fresh != 0;
     const float scale = (float)R.scale;
@@ -1063,17 +1096,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
     constexpr int kChunks = kClsOrbitsPerCta / kSortChunk;
     const int row = lane & 15, part = lane >> 4;  // part 0: V^T row, 1: Q row
 
-    int ci_n;
-    bool single_n;
-    uint32_t b0_n, dp_n;
-    float vn[16];
-    sorted_fetch(first + threadIdx.x, norb, s, C, eC, E, htab, st, fresh, scale, init, ci_n, single_n, b0_n, dp_n, vn);
+    SortedLoad ld;
+    sorted_issue(first + threadIdx.x, norb, s, C, eC, E, st, ld);
     for (int k = 0; k < kChunks; ++k) {
         const uint32_t cbase = first + (uint32_t)(k * kSortChunk);
         if (cbase >= norb) break;  // uniform over the CTA
-        const int ci = ci_n;
-        const bool single = single_n;
-        const uint32_t b0 = b0_n, dp = dp_n;
+        float vn[16];
+        const int ci = sorted_finish(ld, htab, fresh, scale, init, vn);
+        const bool single = ld.single;
+        const uint32_t b0 = ld.b0, dp = ld.dp;
         const int q = ci >= 0 ? 2 * ci + (single ? 1 : 0) : -1;
         // per-warp key counts; the first lane of each key group writes its size
         for (int c = lane; c < nk; c += 32) wcnt[warp * nk + c] = 0;
@@ -1082,46 +1113,38 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
         const int rank = __popc(grp & ((1u << lane) - 1u));
         if (q >= 0 && rank == 0) wcnt[warp * nk + q] = __popc(grp);
         __syncthreads();
-        if (warp == 0) {  // positions: keys in order, warps in order within a key
-            int tot[6];
-#pragma unroll
-            for (int j = 0; j < 6; ++j) {
-                const int c = lane * 6 + j;
-                int run = 0;
-                if (c < nk) {
-                    for (int wp = 0; wp < kWarps; ++wp) {
-                        const int t = wcnt[wp * nk + c];
-                        wcnt[wp * nk + c] = run;
-                        run += t;
-                    }
-                }
-                tot[j] = run;
+        // positions: keys in order, warps in order within a key; thread t scans key t
+        int tot = 0;
+        if (kslot < nk) {
+            for (int wp = 0; wp < kWarps; ++wp) {
+                const int t = wcnt[wp * nk + kslot];
+                wcnt[wp * nk + kslot] = tot;
+                tot += t;
             }
-            int lsum = 0;
+        }
+        int incl = tot;
 #pragma unroll
-            for (int j = 0; j < 6; ++j) lsum += tot[j];
-            int incl = lsum;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, incl, d);
-                if (lane >= d) incl += y;
-            }
-            int base = incl - lsum;
-#pragma unroll
-            for (int j = 0; j < 6; ++j) {
-                const int c = lane * 6 + j;
-                if (c < nk) {
-                    for (int wp = 0; wp < kWarps; ++wp) wcnt[wp * nk + c] += base;
-                    kend[c] = base + tot[j];
-                }
-                base += tot[j];
-            }
-            if (lane == 31) *nact_s = incl;
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += y;
+        }
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        if (kslot < nk) {
+            int base = incl - tot;
+            for (int wp = 0; wp < warp; ++wp) base += wsum[wp];
+            kstart[kslot] = base;
+            kend[kslot] = base + tot;
+        }
+        if (threadIdx.x == 0) {
+            int n = 0;
+            for (int wp = 0; wp < kWarps; ++wp) n += wsum[wp];
+            *nact_s = n;
         }
         __syncthreads();
         int pos = -1;
         if (q >= 0) {
-            pos = wcnt[warp * nk + q] + rank;
+            pos = kstart[q] + wcnt[warp * nk + q] + rank;
 #pragma unroll
             for (int u = 0; u < 4; ++u)
                 *reinterpret_cast<float4*>(vbuf + pos * 16 + 4 * u) = make_float4(vn[4 * u], vn[4 * u + 1], vn[4 * u + 2], vn[4 * u + 3]);
@@ -1129,8 +1152,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
         }
         __syncthreads();
         if (k + 1 < kChunks)  // the next chunk's loads overlap this chunk's products
-            sorted_fetch(cbase + kSortChunk + threadIdx.x, norb, s, C, eC, E, htab, st, fresh, scale, init, ci_n, single_n,
-                         b0_n, dp_n, vn);
+            sorted_issue(cbase + kSortChunk + threadIdx.x, norb, s, C, eC, E, st, ld);
         {
             const int nact = *nact_s;
             const int p1 = nact * (warp + 1) / kWarps;
@@ -1661,8 +1683,8 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
             const size_t staged_smem = base_smem + esz * (size_t)nslot * kStagedStride;
             const size_t sorted_smem =
                 sizeof(float) * ((size_t)nslot * 512 + (size_t)kWarps * nslot * 16 + 2 * (size_t)kSortChunk * 16) +
-                sizeof(unsigned long long) * (kHash + kMaxCls) + sizeof(int) * ((size_t)(kWarps + 1) * 2 * nslot + 4) +
-                kSortChunk;
+                sizeof(unsigned long long) * (kHash + kMaxCls) +
+                sizeof(int) * ((size_t)(kWarps + 2) * 2 * nslot + kWarps + 4) + kSortChunk;
             int optin = 0;
             cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0);
             sorted = precision == SQ_F32 && sorted_smem <= (size_t)optin;

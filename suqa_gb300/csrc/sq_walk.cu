@@ -66,6 +66,8 @@ struct WalkDev {
     uint32_t cta0, ncta; // CTAs of the walk in the step grid
     int dmax;            // largest |dE| of the ring
     uint32_t slot0;      // class-table temperature slot of stage 0 (algo 1)
+    uint32_t jplane[5];  // bit planes of J_b + joff over the bonds b < s
+    int joff, jnp;       // offset making every J_b + joff >= 0; planes in use
 };
 
 struct WalkRec {
@@ -932,6 +934,7 @@ __global__ void __launch_bounds__(kThreads) k_walk_step_cls(const WalkDev* __res
 constexpr int kSortChunk = kThreads;
 constexpr int kWarps = kThreads / 32;
 constexpr int kHash = 256;
+constexpr int kRow = 20;  // floats per sorted row: 16 amplitudes, rows 5 bank groups apart
 
 __device__ __forceinline__ uint32_t cls_hash(unsigned long long key) {
     return (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> 56);
@@ -939,20 +942,45 @@ __device__ __forceinline__ uint32_t cls_hash(unsigned long long key) {
 
 // Orbit o of the chunk in two halves, so that no instruction waits on the loads
 // before this chunk's products have run: sorted_issue decodes the orbit and
-// issues its loads (the 8 energies of its key, its 16 amplitudes, read even on a
-// fresh start and for orbits past the walk's end, whose indices stay inside the
-// walk's state, and then dropped), sorted_finish forms the key, looks up
-// the class (-1 past the end) and the amplitudes.  State index of amplitude
+// issues its loads (its 16 amplitudes, read even on a fresh start and for orbits
+// past the walk's end, whose indices stay inside the walk's state, and then
+// dropped) after forming its class key, sorted_finish looks up the class (-1 past
+// the end) and scales the amplitudes.  State index of amplitude
 // (a, b, c, acc): b0 ^ (a ? dp) ^ (b ? e_C) ^ (c ? e_C << s) ^ (acc ? 1 << 2s),
 // the bits of (acc, d, x).
 struct SortedLoad {
     uint32_t b0, dp;
     bool active, single;
-    int e[8];
+    unsigned long long key;
     float raw[16];
 };
 
-__device__ __forceinline__ void sorted_issue(uint32_t o, uint32_t norb, int s, int C, uint32_t eC, const int* __restrict__ E,
+// The ring's bonds for the class keys without the energy table: flipping the spins
+// of d changes the sign of s_b s_{b+1} exactly on the bonds that cross the border of
+// d, m = d ^ rot(d), so E(x ^ d) - E(x) = 2 sum_{b in m} J_b s_b s_{b+1}(x)
+//   = 2 J(m) - 4 J(m & (x ^ rot(x))),  J(mask) = sum of J_b over the bonds in mask,
+// from bit planes of J_b + joff: sum_k 2^k popc(mask & plane_k) - joff popc(mask).
+struct RingBonds {
+    uint32_t plane[5];
+    int np, off, s;
+    uint32_t smask;
+};
+
+__device__ __forceinline__ int bond_sum(uint32_t m, const RingBonds& B) {
+    int t = 0;
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+        if (k < B.np) t += __popc(m & B.plane[k]) << k;
+    return t - B.off * __popc(m);
+}
+
+__device__ __forceinline__ int ring_dE(uint32_t x, uint32_t d, const RingBonds& B) {
+    const uint32_t m = (d ^ ((d >> 1) | (d << (B.s - 1)))) & B.smask;
+    const uint32_t bx = (x ^ ((x >> 1) | (x << (B.s - 1)))) & B.smask;
+    return 2 * bond_sum(m, B) - 4 * bond_sum(m & bx, B);
+}
+
+__device__ __forceinline__ void sorted_issue(uint32_t o, uint32_t norb, int s, int C, uint32_t eC, const RingBonds& B,
                                              const float* __restrict__ st, SortedLoad& L) {
     uint32_t x0 = 0, dp = 0;
     L.active = o < norb;
@@ -960,12 +988,12 @@ __device__ __forceinline__ void sorted_issue(uint32_t o, uint32_t norb, int s, i
     if (L.active) L.single = orbit_decode(o, s, C, dp, x0);
     L.b0 = (dp << s) | x0;
     L.dp = dp;
+    L.key = 0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {  // the terms of orbit_key: dE at x = x0 ^ (j&1 ? e_C), d = dp ^ (j&2 ? e_C)
+    for (int j = 0; j < 4; ++j) {  // orbit_key's terms: dE at x = x0 ^ (j&1 ? e_C), d = dp ^ (j&2 ? e_C)
         const uint32_t x = x0 ^ ((j & 1) ? eC : 0u);
         const uint32_t d = dp ^ ((j & 2) ? eC : 0u);
-        L.e[2 * j] = __ldg(E + (x ^ d));
-        L.e[2 * j + 1] = __ldg(E + x);
+        L.key |= (unsigned long long)(ring_dE(x, d, B) + 256) << (9 * j);
     }
     const uint32_t mc = eC << s, macc = 1u << (2 * s);
 #pragma unroll
@@ -981,9 +1009,7 @@ __device__ __forceinline__ int sorted_finish(const SortedLoad& L, const unsigned
                                              float init, float (&v)[16]) {
     int ci = -1;
     if (L.active) {
-        unsigned long long key = 0;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) key |= (unsigned long long)(L.e[2 * j] - L.e[2 * j + 1] + 256) << (9 * j);
+        const unsigned long long key = L.key;
         uint32_t h = cls_hash(key);
         for (int probe = 0; probe < kHash; ++probe) {  // bounded; the table is at most 3/8 full
             const unsigned long long e = htab[h];
@@ -1052,9 +1078,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
     const int nk = 2 * nslot;
     float* cls_s = reinterpret_cast<float*>(smem_raw);              // [nslot][512]: V^T rows, then Q rows
     float* slots = cls_s + nslot * 512;                              // [warps][nslot][16]
-    float* vbuf = slots + kWarps * nslot * 16;                       // [kSortChunk][16] amplitudes, sorted
-    float* sbuf = vbuf + kSortChunk * 16;                            // [kSortChunk][16] S, sorted
-    unsigned long long* htab = reinterpret_cast<unsigned long long*>(sbuf + kSortChunk * 16);  // [kHash] key << 8 | class
+    float* vbuf = slots + kWarps * nslot * 16;                       // [kSortChunk][kRow] amplitudes, sorted
+    float* sbuf = vbuf + kSortChunk * kRow;                          // [kSortChunk][kRow] S, sorted
+    unsigned long long* htab = reinterpret_cast<unsigned long long*>(sbuf + kSortChunk * kRow);  // [kHash] key << 8 | class
     unsigned long long* sent = htab + kHash;                         // [kMaxCls] class data entries
     int* wcnt = reinterpret_cast<int*>(sent + kMaxCls);              // [warps][nk] counts, then offsets within a key
     int* kstart = wcnt + kWarps * nk;                                // [nk] start of each key's run
@@ -1085,7 +1111,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
     }
     const uint32_t norb = norbits(s), eC = 1u << C;
     const uint32_t mc = eC << s, macc = 1u << (2 * s);
-    const int* E = energies + W.e_off;
+    RingBonds bonds;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) bonds.plane[k] = W.jplane[k];
+    bonds.np = W.jnp;
+    bonds.off = W.joff;
+    bonds.s = s;
+    bonds.smask = (1u << s) - 1u;
     const int kslot = threadIdx.x;  // the sort key this thread scans
     float* st = states + W.state_off;
     const bool fresh = R.fresh != 0;
@@ -1097,7 +1129,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
     const int row = lane & 15, part = lane >> 4;  // part 0: V^T row, 1: Q row
 
     SortedLoad ld;
-    sorted_issue(first + threadIdx.x, norb, s, C, eC, E, st, ld);
+    sorted_issue(first + threadIdx.x, norb, s, C, eC, bonds, st, ld);
     for (int k = 0; k < kChunks; ++k) {
         const uint32_t cbase = first + (uint32_t)(k * kSortChunk);
         if (cbase >= norb) break;  // uniform over the CTA
@@ -1147,12 +1179,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
             pos = kstart[q] + wcnt[warp * nk + q] + rank;
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                *reinterpret_cast<float4*>(vbuf + pos * 16 + 4 * u) = make_float4(vn[4 * u], vn[4 * u + 1], vn[4 * u + 2], vn[4 * u + 3]);
+                *reinterpret_cast<float4*>(vbuf + pos * kRow + 4 * u) = make_float4(vn[4 * u], vn[4 * u + 1], vn[4 * u + 2], vn[4 * u + 3]);
             csort[pos] = (unsigned char)q;
         }
         __syncthreads();
         if (k + 1 < kChunks)  // the next chunk's loads overlap this chunk's products
-            sorted_issue(cbase + kSortChunk + threadIdx.x, norb, s, C, eC, E, st, ld);
+            sorted_issue(cbase + kSortChunk + threadIdx.x, norb, s, C, eC, bonds, st, ld);
         {
             const int nact = *nact_s;
             const int p1 = nact * (warp + 1) / kWarps;
@@ -1180,10 +1212,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
                 }
                 for (; p + 4 <= e; p += 4) {
                     f2 v0[8], v1[8], v2[8], v3[8];
-                    sorted_row(vbuf + p * 16, v0);
-                    sorted_row(vbuf + p * 16 + 16, v1);
-                    sorted_row(vbuf + p * 16 + 32, v2);
-                    sorted_row(vbuf + p * 16 + 48, v3);
+                    sorted_row(vbuf + p * kRow, v0);
+                    sorted_row(vbuf + (p + 1) * kRow, v1);
+                    sorted_row(vbuf + (p + 2) * kRow, v2);
+                    sorted_row(vbuf + (p + 3) * kRow, v3);
                     const float y0 = sorted_dot(r, v0), y1 = sorted_dot(r, v1);
                     const float y2 = sorted_dot(r, v2), y3 = sorted_dot(r, v3);
                     if (part == 0) {
@@ -1192,18 +1224,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
                         nacc += wt * y2 * y2;
                         nacc += wt * y3 * y3;
                     } else {
-                        sbuf[p * 16 + row] = y0;
-                        sbuf[p * 16 + 16 + row] = y1;
-                        sbuf[p * 16 + 32 + row] = y2;
-                        sbuf[p * 16 + 48 + row] = y3;
+                        sbuf[p * kRow + row] = y0;
+                        sbuf[(p + 1) * kRow + row] = y1;
+                        sbuf[(p + 2) * kRow + row] = y2;
+                        sbuf[(p + 3) * kRow + row] = y3;
                     }
                 }
                 for (; p < e; ++p) {
                     f2 v0[8];
-                    sorted_row(vbuf + p * 16, v0);
+                    sorted_row(vbuf + p * kRow, v0);
                     const float y0 = sorted_dot(r, v0);
                     if (part == 0) nacc += wt * y0 * y0;
-                    else sbuf[p * 16 + row] = y0;
+                    else sbuf[p * kRow + row] = y0;
                 }
             }
             if (cur >= 0 && part == 0) myslots[cur * 16 + row] += nacc;
@@ -1213,7 +1245,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
             float S[16];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                const float4 t = *reinterpret_cast<const float4*>(sbuf + pos * 16 + 4 * u);
+                const float4 t = *reinterpret_cast<const float4*>(sbuf + pos * kRow + 4 * u);
                 S[4 * u] = t.x;
                 S[4 * u + 1] = t.y;
                 S[4 * u + 2] = t.z;
@@ -1472,6 +1504,17 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
         d.trace_off = trace_len;
         d.e_off = (uint32_t)energies.size();
         d.dmax = 2 * sumJ;
+        int jmin = 0, jmax = 0;
+        for (uint32_t b = 0; b < a.spins; ++b) jmin = std::min(jmin, (int)a.J[b]);
+        d.joff = -jmin;
+        for (uint32_t b = 0; b < a.spins; ++b) jmax = std::max(jmax, (int)a.J[b] + d.joff);
+        d.jnp = 0;
+        while (d.jnp < 5 && (jmax >> d.jnp) != 0) ++d.jnp;  // J_b + joff <= 16: 5 planes at most
+        for (int k = 0; k < 5; ++k) {
+            d.jplane[k] = 0;
+            for (uint32_t b = 0; b < a.spins; ++b)
+                if ((((int)a.J[b] + d.joff) >> k) & 1) d.jplane[k] |= 1u << b;
+        }
         const uint32_t N = 1u << a.spins;
         for (uint32_t x = 0; x < N; ++x) {
             int E = 0;
@@ -1682,7 +1725,7 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
                                      sizeof(int) * (kThreads / 32) * 32 + 16 + 2 * sizeof(unsigned long long) * kMaxCls;
             const size_t staged_smem = base_smem + esz * (size_t)nslot * kStagedStride;
             const size_t sorted_smem =
-                sizeof(float) * ((size_t)nslot * 512 + (size_t)kWarps * nslot * 16 + 2 * (size_t)kSortChunk * 16) +
+                sizeof(float) * ((size_t)nslot * 512 + (size_t)kWarps * nslot * 16 + 2 * (size_t)kSortChunk * kRow) +
                 sizeof(unsigned long long) * (kHash + kMaxCls) +
                 sizeof(int) * ((size_t)(kWarps + 2) * 2 * nslot + kWarps + 4) + kSortChunk;
             int optin = 0;

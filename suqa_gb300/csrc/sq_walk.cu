@@ -1063,7 +1063,7 @@ __device__ __forceinline__ float sorted_dot(const f2 (&r)[8], const f2 (&v)[8]) 
 }
 
 __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
-                                                               const WalkRec* __restrict__ recs, const int* __restrict__ energies,
+                                                               const WalkRec* __restrict__ recs,
                                                                const unsigned long long* __restrict__ keys,
                                                                const uint32_t* __restrict__ ncls, const float* __restrict__ cls,
                                                                const uint32_t* __restrict__ gid, float* __restrict__ states,
@@ -1788,7 +1788,7 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
                                                                                    (float*)d_cls);
                     if (sorted)
                         k_walk_step_sorted<<<(unsigned)nct, kThreads, cls_smem, st>>>(
-                            d_walks, d_cta, d_recs, d_E, d_keys, d_ncls, (const float*)d_cls, d_gid, (float*)d_states,
+                            d_walks, d_cta, d_recs, d_keys, d_ncls, (const float*)d_cls, d_gid, (float*)d_states,
                             d_partial, nslot);
                     else if (staged)
                         k_walk_step_cls<float, true><<<(unsigned)nct, kThreads, cls_smem, st>>>(

@@ -250,6 +250,9 @@ def qsa_section(n_walks, walk_steps, f64_walks=16, cpu=True, seed=2025):
     # algorithm delivers, expressed as that work per second
     norb, L = (1 << 9) + ((1 << 9) - 1) * (1 << 8), 64
     flops = norb * ((L - 1) * 272 + L * 48)
+    # algorithm 1's own work per walk step: per orbit V^T psi and Q psi (2 x 16 x 16
+    # multiply-adds); the state (2^21 amplitudes) is read and written once
+    cls_flops = norb * 2 * 16 * 16 * 2
     out = {"workload": f"{n_walks} walks on 10-spin Ising rings (2^21 amplitudes each), first {walk_steps} walk "
                        f"steps of the beta 0->1 anneal (50 stages x 20 steps), 6-qubit walk-phase register",
            "algorithm": "1 (orbit classes); f32_per_orbit_iteration: algorithm 0 on the same walks",
@@ -257,11 +260,13 @@ def qsa_section(n_walks, walk_steps, f64_walks=16, cpu=True, seed=2025):
                                        "fp32_tflops": flops * sum(r.steps for r in r0) / (ms0 / 1e3) / 1e12},
            "f32": {"walk_steps_per_s": st32 / (ms32 / 1e3), "walk_steps": st32, "device_ms": ms32,
                    "restarts": int(sum(r.restarts for r in r32)),
-                   "equivalent_fp32_tflops": flops * st32 / (ms32 / 1e3) / 1e12},
+                   "equivalent_fp32_tflops": flops * st32 / (ms32 / 1e3) / 1e12,
+                   "own_fp32_tflops": cls_flops * st32 / (ms32 / 1e3) / 1e12,
+                   "state_hbm_gbs": 2 * 4 * (1 << 21) * st32 / (ms32 / 1e3) / 1e9},
            "f64": {"walk_steps_per_s": st64 / (ms64 / 1e3), "walk_steps": st64, "device_ms": ms64,
                    "equivalent_fp64_tflops": flops * st64 / (ms64 / 1e3) / 1e12, "walks": f64_walks},
            "fp32_vs_fp64": {"walks_identical": len(same), "walks": f64_walks, "max_abs_p0_diff": p0_err},
-           "flops_per_walk_step": flops}
+           "flops_per_walk_step": flops, "own_flops_per_walk_step": cls_flops}
     if cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import qsa_walk as qw

@@ -22,12 +22,15 @@
 // applies W L-1 times without touching memory.  Orbits with d' = 0 have 8
 // amplitudes; they run duplicated in the 16 registers and count half.
 //
-// Per step (one launch of k_walk_step and one of k_walk_measure):
+// Per step (algo 0: one launch of k_walk_step and one of k_walk_measure):
 //   k_walk_step     every orbit: load psi (scaled by the last normalisation, or
 //                   the initial state), L-1 applications of W, per-k warp sums
 //                   of <psi, v_k> accumulated in FP64, store sum_k v_k;
 //   k_walk_measure  per walk: g_k, P(m), the register readout with q draws,
 //                   restart on a nonzero value, the next move and temperature.
+// algo 1 and 2 work per orbit class instead (the section "Orbit classes" below):
+// k_cls_keys and k_cls_table once per batch (or k_cls_prep every step), then
+// k_walk_step_sorted (FP32) or k_walk_step_cls and k_walk_measure per step.
 // k_walk_readout reads the spins of every completed walk.
 #include <algorithm>
 #include <cmath>
@@ -488,7 +491,7 @@ k_walk_step(const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk,
 // ---------------------------------------------------------------------------
 // Orbit classes (algo 1).  W on an orbit depends only on the energy differences
 // at its four a = 0 positions (the a = 1 ones are their negatives), and a step
-// has few distinct such signatures (62-69 among 131,328 orbits of a 10-spin
+// has few distinct such signatures (62-71 among 131,328 orbits of a 10-spin
 // ring).  Per class: W (16 x 16), A = (W + W^T)/2 = V diag(lambda) V^T,
 // Q = sum_{k<L} W^k and d_{k,i} = v_i^T W^k v_i.  W is real orthogonal, so
 // <psi, W^k psi> = psi^T T_k(A) psi (T_k: Chebyshev) and T_k(lambda_i) = d_{k,i}:

@@ -178,3 +178,17 @@ def test_orbit_class_algorithm_with_many_classes(precision, tol):
     walks = [QsaWalk(5, J, 0.5 + 0.3 * k, 3, 3, 1 + k, 700 + k, algo=1) for k, J in enumerate(rings)]
     runs, _ = run_qsa_walks(walks, precision, trace=True)
     _check(runs, walks, tol)
+
+
+def test_orbit_class_algorithm_refuses_rings_with_too_many_classes():
+    """An 8-spin ring with couplings in -3..3 has 130-338 classes per move, more than
+    algorithm 1 holds (96): the call fails with SQ_ERR_UNSUPPORTED and the same
+    walk runs with algorithm 0."""
+    from suqa_gb300._lib import SqUnsupported
+    from suqa_gb300.walk import QsaWalk, run_qsa_walks
+    w = QsaWalk(8, [1, 1, 2, 3, -3, -2, 2, 3], 1.0, 2, 2, 3, 5, algo=1)
+    with pytest.raises(SqUnsupported, match="orbit classes"):
+        run_qsa_walks([w], "f32")
+    w.algo = 0
+    runs, _ = run_qsa_walks([w], "f64", trace=True)
+    _check(runs, [w], 1e-10)

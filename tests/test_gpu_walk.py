@@ -172,7 +172,7 @@ def test_class_table_matches_per_step_preparation(precision):
 def test_orbit_class_algorithm_with_many_classes(precision, tol):
     """5-spin rings with couplings +-1, +-2 have 76-78 classes per move: FP32
     then takes the orbit pass that reads every class through its own lane
-    (the class-sorted pass holds at most about 75 classes in shared memory)."""
+    (the class-sorted pass holds at most 71 classes in shared memory)."""
     from suqa_gb300.walk import QsaWalk, run_qsa_walks
     rings = [[-2, 1, 1, -2, -2], [-1, -2, -1, -2, 2], [1, 1, -2, -1, -2], [2, -1, -2, -1, 1], [2, 2, -1, 2, -1]]
     walks = [QsaWalk(5, J, 0.5 + 0.3 * k, 3, 3, 1 + k, 700 + k, algo=1) for k, J in enumerate(rings)]

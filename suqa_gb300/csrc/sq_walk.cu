@@ -1845,6 +1845,8 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
     if (e1) cudaEventDestroy(e1);
     if (st) cudaStreamDestroy(st);
     cleanup();
+    if (err == cudaErrorMemoryAllocation)
+        return wfail(SQ_ERR_NOMEM, "device allocation for the walk batch's class data failed");
     if (err != cudaSuccess) return wfail(SQ_ERR_CUDA, std::string("walk batch: ") + cudaGetErrorString(err));
     for (uint32_t i = 0; i < nwalks; ++i) {
         const WalkRec& R = rec[i];

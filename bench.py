@@ -455,15 +455,7 @@ def main():
 
     # FP64 fused multiply-add rate of the CUDA cores (the pass kernel's own pipe;
     # DGEMM above runs on the FP64 tensor path)
-    fma_gops = None
-    try:
-        import ctypes
-        from suqa_gb300 import _lib
-        g = ctypes.c_double()
-        if _lib.load().sq_fp64_fma_rate(ctypes.byref(g), None) == 0:
-            fma_gops = g.value
-    except Exception:
-        pass
+    fma_gops = fp64_fma_rate()
     fp64_ins = fp64_instructions(gates, n) * args.steps if args.precision == "f64" else None
 
     peaks = {}
@@ -491,7 +483,7 @@ def main():
                               "peak_gops": fma_gops,
                               "frac": (fp64_ins / (kms / 1e3) / 1e9 / fma_gops) if (fp64_ins and kms > 0 and fma_gops)
                               else None,
-                              "peak_source": "sq_fp64_fma_rate: independent DFMA chains on every SM, measured in "
+                              "peak_source": "sqb_fp64_fma_rate (libsq_probe.so): independent DFMA chains on every SM, measured in "
                                              "this run (of measured)"}}
 
     # secondary: the same circuit with FP32 amplitudes (FP64 reductions)
@@ -622,6 +614,21 @@ class _DeviceArray:
 
     def __init__(self, ptr, n):
         self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 3}
+
+
+def fp64_fma_rate():
+    """FP64 FMA instructions per second (G/s) of this GPU's CUDA cores, from the
+    benchmark's probe library (suqa_gb300/_build/libsq_probe.so), or None."""
+    import ctypes
+    try:
+        lib = ctypes.CDLL(os.path.join(ROOT, "suqa_gb300", "_build", "libsq_probe.so"))
+        lib.sqb_fp64_fma_rate.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_float)]
+        g = ctypes.c_double()
+        if lib.sqb_fp64_fma_rate(ctypes.byref(g), None) == 0:
+            return g.value
+    except OSError:
+        pass
+    return None
 
 
 def traffic_per_launch():

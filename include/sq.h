@@ -134,9 +134,6 @@ typedef struct sq_stats {
                               Pauli rotation on the amplitudes it touches, 0 for X/CX/MCX/SWAP) */
 } sq_stats;
 int sq_get_stats(const sq_state* s, sq_stats* out);
-/* FP64 fused multiply-add rate of the current device's CUDA cores (independent
- * chains on every SM), in G operations/s: the ceiling of the FP64 tile pass. */
-int sq_fp64_fma_rate(double* gops, float* kernel_ms);
 int sq_reset_stats(sq_state* s);
 /* Kernel timing: when enabled, every pass launch is bracketed by CUDA events on
  * the state's stream; sq_kernel_time() synchronizes and returns the summed
@@ -326,7 +323,10 @@ int sq_mlp_train_step(sq_mlp* n, const float* x, const float* targets, const flo
  * launches needing more are rejected with SQ_ERR_ARG.  All calls share it:
  * calls whose kernels overlap on the GPU race; calls ordered on one stream are
  * safe.  The first call on a device performs a one-time set-up on it and
- * should come before any stream capture. */
+ * should come before any stream capture.  re and im must be 16-byte aligned
+ * (element-aligned for states narrower than one 16-byte vector) and out_p01
+ * 8-byte aligned; misaligned pointers are rejected with SQ_ERR_ARG before any
+ * launch. */
 int sq_qubit_probs_noalloc(const void* re, const void* im, uint32_t n, int precision, uint32_t q,
                            double* out_p01, void* stream);
 

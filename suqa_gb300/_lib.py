@@ -84,7 +84,6 @@ _SIGS = {
     "sq_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "sq_set_fusion": (C.c_int, [C.c_void_p, C.c_int]),
     "sq_set_tile_qubits": (C.c_int, [C.c_void_p, C.c_int]),
-    "sq_fp64_fma_rate": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_float)]),
     "sq_upload": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "sq_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "sq_init_state": (C.c_int, [C.c_void_p]),

@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                      "-I" + INCLUDE, "-I" + CSRC]
 
-LIB_SOURCES = ["sq_engine.cu", "sq_noalloc.cu", "sq_batch.cu", "sq_mlp.cu", "sq_evo.cu", "sq_walk.cu", "sq_probe.cu"] + [
+LIB_SOURCES = ["sq_engine.cu", "sq_noalloc.cu", "sq_batch.cu", "sq_mlp.cu", "sq_evo.cu", "sq_walk.cu"] + [
     "sq_batch_%s_m%d.cu" % (t, m) for t in ("f32", "f64") for m in (0, 1, 2)]
 
 
@@ -69,6 +69,17 @@ def build_libsq(force=False):
     if force or jobs or not os.path.exists(lib):
         _run([nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"])
     return lib
+
+
+def build_probe(force=False):
+    """libsq_probe.so: the benchmark's device characterisation (FP64 FMA rate),
+    kept out of libsq's product ABI."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(CSRC, "bench_probe.cu")
+    out = os.path.join(BUILD, "libsq_probe.so")
+    if force or not _newer(out, [src]):
+        _run([nvcc()] + NVCC_FLAGS + ["-shared", src, "-o", out, "-lcudart"])
+    return out
 
 
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-w", "-I" + SHIM_INCLUDE, "-I" + INCLUDE]
@@ -136,6 +147,7 @@ def build_tfim_drivers(force=False):
 
 def build_all(force=False):
     lib = build_libsq(force)
+    build_probe(force)
     build_dropin(force)
     build_tfim_drivers(force)
     return lib

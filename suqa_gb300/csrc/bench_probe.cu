@@ -1,16 +1,17 @@
+// Benchmark support, not part of libsq's product ABI: built as its own library
+// (libsq_probe.so) that only the benchmark and its test load.
+//
 // Device characterisation: the FP64 fused multiply-add rate of the CUDA cores
 // (not the FP64 tensor path that DGEMM uses), the ceiling of the FP64 tile
 // pass, whose gates are DADD/DMUL/DFMA streams.
 #include <algorithm>
 #include <string>
 
-#include "sq.h"
-
-namespace sqi {
-void set_error(const char* msg);
-}
+#include <cuda_runtime.h>
 
 namespace {
+
+std::string g_probe_err;
 
 constexpr int kChains = 8;
 
@@ -30,10 +31,14 @@ __global__ void k_fp64_fma_rate(double* out, double a, double b, int iters) {
 
 }  // namespace
 
-extern "C" int sq_fp64_fma_rate(double* gops, float* kernel_ms) {
+extern "C" const char* sqb_last_error(void) { return g_probe_err.c_str(); }
+
+// FP64 FMA instructions per second of the current device (independent chains on
+// every SM), in G/s; returns 0, 1 (bad argument) or 2 (CUDA error).
+extern "C" int sqb_fp64_fma_rate(double* gops, float* kernel_ms) {
     if (!gops) {
-        sqi::set_error("null output");
-        return SQ_ERR_ARG;
+        g_probe_err = "null output";
+        return 1;
     }
     int dev = 0, nsm = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -59,10 +64,10 @@ extern "C" int sq_fp64_fma_rate(double* gops, float* kernel_ms) {
     if (e1) cudaEventDestroy(e1);
     cudaFree(out);
     if (e != cudaSuccess) {
-        sqi::set_error((std::string("fp64 rate probe: ") + cudaGetErrorString(e)).c_str());
-        return SQ_ERR_CUDA;
+        g_probe_err = std::string("fp64 rate probe: ") + cudaGetErrorString(e);
+        return 2;
     }
     *gops = (double)blocks * threads * iters * kChains / (ms * 1e-3) / 1e9;
     if (kernel_ms) *kernel_ms = ms;
-    return SQ_OK;
+    return 0;
 }

@@ -89,6 +89,19 @@ extern "C" int sq_qubit_probs_noalloc(const void* re, const void* im, uint32_t n
     if (n < 1 || n > 33) return fail(SQ_ERR_ARG, "qubit count must be in 1..33");
     if (q >= n) return fail(SQ_ERR_ARG, "qubit index out of range");
     if (precision != SQ_F64 && precision != SQ_F32) return fail(SQ_ERR_ARG, "unknown precision");
+    // The reduction reads 16-byte vectors (two doubles or four floats) whenever a
+    // tile holds at least one vector; raw pointers from another runtime (a view
+    // with a storage offset, say) may not be aligned for that, and a misaligned
+    // vector load would end the CUDA context.  Reject them here, before any launch.
+    {
+        const size_t esz = precision == SQ_F64 ? 8 : 4;
+        const uint32_t kt = n < 10 ? n : 10;
+        const size_t need = ((size_t)1 << kt) * esz >= 16 ? 16 : esz;
+        if (((uintptr_t)re | (uintptr_t)im) % need != 0)
+            return fail(SQ_ERR_ARG, need == 16 ? "re and im must be 16-byte aligned"
+                                               : "re and im must be aligned to the element size");
+        if ((uintptr_t)out_p01 % 8 != 0) return fail(SQ_ERR_ARG, "out_p01 must be 8-byte aligned");
+    }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return fail(SQ_ERR_NODEVICE, "no usable CUDA device");

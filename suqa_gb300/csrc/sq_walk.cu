@@ -1731,8 +1731,10 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
                 sizeof(float) * ((size_t)nslot * 512 + (size_t)kWarps * nslot * 16 + 2 * (size_t)kSortChunk * kRow) +
                 sizeof(unsigned long long) * (kHash + kMaxCls) +
                 sizeof(int) * ((size_t)(kWarps + 2) * 2 * nslot + kWarps + 4) + kSortChunk;
-            int optin = 0;
-            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0);
+            int optin = 0, cur_dev = 0;
+            if (err == cudaSuccess) err = cudaGetDevice(&cur_dev);  // the device the walks run on
+            if (err == cudaSuccess)
+                err = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cur_dev);
             sorted = precision == SQ_F32 && sorted_smem <= (size_t)optin;
             staged = !sorted && precision == SQ_F32 && staged_smem <= (size_t)optin;
             cls_smem = sorted ? sorted_smem : staged ? staged_smem : base_smem;

@@ -106,7 +106,15 @@ void suqa::allocate_state(uint Dim) {
     deallocate_state();
     uint n = 0;
     while ((1U << n) < Dim) ++n;
-    check(sq_state_create(&g_state, n, default_precision()));
+    const int rc = sq_state_create(&g_state, n, default_precision());
+    if (rc == SQ_ERR_NODEVICE) {
+        // Without a usable GPU there is nothing to run on: say so and end with the
+        // status code rather than an uncaught exception (the drivers allocate the
+        // state before they open any output file).
+        std::fprintf(stderr, "suqa (libsq): %s; the gate engine needs a GPU\n", sq_last_error());
+        std::exit(SQ_ERR_NODEVICE);
+    }
+    check(rc);
     void *re = nullptr, *im = nullptr;
     check(sq_state_ptrs(g_state, &re, &im));
     state.vecsize = Dim;

@@ -173,12 +173,16 @@ def test_tile_size_does_not_change_results(precision):
 
 
 def test_fp64_fma_rate_probe_reports_a_rate():
-    """The FP64 FMA-rate probe (the tile pass's ceiling in bench.py) runs and gives a
-    plausible rate: more than 50 G instructions/s, less than the nominal SM count x
-    clock x 2 per SM per cycle bound with room (1 T/s)."""
+    """The benchmark's FP64 FMA-rate probe (libsq_probe.so, the tile pass's
+    ceiling in bench.py) runs and gives a plausible rate: more than 50 G
+    instructions/s, less than the nominal SM count x clock x 2 per SM per cycle
+    bound with room (1 T/s)."""
     import ctypes
+    import os
     from suqa_gb300 import _lib
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(_lib.LIB_PATH), "libsq_probe.so"))
+    lib.sqb_fp64_fma_rate.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_float)]
     g = ctypes.c_double()
     ms = ctypes.c_float()
-    assert _lib.load().sq_fp64_fma_rate(ctypes.byref(g), ctypes.byref(ms)) == 0
+    assert lib.sqb_fp64_fma_rate(ctypes.byref(g), ctypes.byref(ms)) == 0
     assert 50.0 < g.value < 1000.0 and ms.value > 0

@@ -180,6 +180,18 @@ def test_orbit_class_algorithm_with_many_classes(precision, tol):
     _check(runs, walks, tol)
 
 
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-9), ("f32", 5e-5)])
+def test_orbit_class_keys_with_wide_couplings(precision, tol):
+    """Couplings of magnitude 8 use all five bit planes of the register-formed
+    class keys (J_b + offset up to 16); few classes, so FP32 takes the
+    class-sorted pass.  The walks must still be the oracle's."""
+    from suqa_gb300.walk import QsaWalk, run_qsa_walks
+    rings = [[8, -8, 8, -8, 8, 8], [-8, -8, 8, 8, -8, 8], [8, 8, 8, 8, 8, 8], [-8, 8, -8, 8, -8, 8]]
+    walks = [QsaWalk(6, J, 0.04 + 0.03 * k, 3, 3, 2 + k, 810 + k, algo=1) for k, J in enumerate(rings)]
+    runs, _ = run_qsa_walks(walks, precision, trace=True)
+    _check(runs, walks, tol)
+
+
 def test_orbit_class_algorithm_refuses_rings_with_too_many_classes():
     """An 8-spin ring with couplings in -3..3 has 130-338 classes per move, more than
     algorithm 1 holds (96): the call fails with SQ_ERR_UNSUPPORTED and the same

@@ -147,9 +147,9 @@ def qms_section(n_chains, steps, seed=2024):
     4096-chain workload (spins 4-10, energy register 4-6 qubits, J = 1,
     h ~ U[0.5, 1.5], beta ~ U[0.2, 2.0], dt = 0.1, one PCG32 stream per chain),
     run as resumable batches (segments of 2 steps replayed from a CUDA graph;
-    FP32 with autotuned CTA sizes) in FP32 and FP64, against the host-driven
-    plain GPU chain (the drop-in qms driver on the libsq state API) on a 7-spin,
-    5-energy-qubit ring."""
+    FP32 with autotuned CTA sizes) in FP32 and FP64; then the host-driven plain
+    GPU chain (the drop-in qms driver on the libsq state API) on a 7-spin,
+    5-energy-qubit ring against a batch of chains of that same configuration."""
     import numpy as np
     from suqa_gb300.batch import Batch, TfimChain, run_tfim_batch
     rng = np.random.default_rng(seed)
@@ -198,30 +198,91 @@ def qms_section(n_chains, steps, seed=2024):
                            "amplitude_error_chains": len(amp_err), "energy_by_ring_length": per_group}
     for b in batches.values():
         b.close()
-    # plain GPU chain: one chain, one launch per fused gate group, host sync per measurement
+    # Like-for-like comparator.  The plain GPU chain is the drop-in qms driver
+    # (host-driven, one libsq state, host sync per measurement) on one 7-spin ring
+    # with a 5-qubit energy register (13 qubits); its rate is the driver's own
+    # timer around the Metropolis loop (no process start, device set-up or initial
+    # state).  The batched rate is the same chain configuration (spins, register,
+    # beta, h, window), 1024 chains with their own seeds, FP32, in one batch.
+    plain_steps = 50
     exe = os.path.join(ROOT, "suqa_gb300", "_build", "qms_tfim_s7")
-    plain_steps = 4
     env = dict(os.environ, TFIM_J="1.0", TFIM_H="1.0")
     t0 = time.perf_counter()
     cp = subprocess.run([exe, "1.0", str(plain_steps), "1", "5", "/tmp/suqa_plain_chain.txt", "--seed", "5",
                          "--ene-min", "-14", "--ene-max", "14", "--thermalization", "0"], env=env,
                         capture_output=True, text=True)
-    dt = time.perf_counter() - t0
+    wall = time.perf_counter() - t0
     if os.path.exists("/tmp/suqa_plain_chain.txt"):
         os.remove("/tmp/suqa_plain_chain.txt")
-    plain = plain_steps / dt if cp.returncode == 0 else None
-    # the same chain run by the batch engine has identical outcomes, hence the same
-    # number of phase estimations: the per-estimation rate removes the seed-dependent
-    # length of the restoration loops from the comparison
-    same1, _ = run_tfim_batch([TfimChain(spins=7, ene_qbits=5, steps=plain_steps, beta=1.0, h=1.0, ene_min=-14.0,
-                                         ene_max=14.0, thermalization=0, seed=5)], "f64")
-    plain_pe = same1[0].phase_estimations / dt if cp.returncode == 0 else None
-    f32_pe = out["f32"]["phase_estimations_per_step"] * out["f32"]["chain_steps_per_s"]
-    out["plain_gpu_chain"] = {"steps_per_s": plain, "phase_estimations_per_s": plain_pe,
-                              "config": "7 spins, 5 energy qubits (13 qubits), FP64, host-driven (libsq state API)"}
-    out["batched_f32_over_plain_steps"] = (out["f32"]["chain_steps_per_s"] / plain) if plain else None
-    out["batched_f32_over_plain_phase_estimations"] = (f32_pe / plain_pe) if plain_pe else None
+    loop_s = _chain_loop_seconds(cp.stdout) if cp.returncode == 0 else None
+    plain = plain_steps / loop_s if loop_s else None
+    same_cfg = [TfimChain(spins=7, ene_qbits=5, steps=steps, beta=1.0, h=1.0, ene_min=-14.0, ene_max=14.0,
+                          thermalization=0, seed=5 + k) for k in range(n_chains)]
+    tb = time.perf_counter()
+    bs = Batch(same_cfg, "f32", segment_steps=2, use_graph=True, autotune=True)
+    tb1 = time.perf_counter()
+    ms_same = bs.run(steps)
+    wall_same = time.perf_counter() - tb1
+    rs = bs.results()
+    bs.close()
+    batched_same = n_chains * steps / (ms_same / 1e3)
+    batched_same_wall = n_chains * steps / wall_same
+    # phase estimations per step differ between chains (restoration loops): the
+    # per-estimation rates remove that from the comparison (the batch engine's FP64
+    # chain with the plain chain's seed has the plain chain's outcomes, hence its
+    # number of phase estimations)
+    plain_pe_rate = None
+    if loop_s:
+        same50, _ = run_tfim_batch([TfimChain(spins=7, ene_qbits=5, steps=plain_steps, beta=1.0, h=1.0,
+                                              ene_min=-14.0, ene_max=14.0, thermalization=0, seed=5)], "f64")
+        plain_pe_rate = same50[0].phase_estimations / loop_s
+    batched_pe_rate = sum(x.phase_estimations for x in rs) / (ms_same / 1e3)
+    out["plain_gpu_chain"] = {"steps_per_s": plain, "steps": plain_steps, "loop_s": loop_s,
+                              "process_wall_s": wall, "phase_estimations_per_s": plain_pe_rate,
+                              "timer": "the driver's own timer around its Metropolis loop",
+                              "config": "7 spins, 5 energy qubits (13 qubits), beta 1, h 1, FP64, host-driven "
+                                        "(libsq state API, drop-in qms driver)"}
+    out["batched_same_config_f32"] = {"chain_steps_per_s_device": batched_same,
+                                      "chain_steps_per_s_wall": batched_same_wall,
+                                      "chains": n_chains, "steps": steps, "device_ms": ms_same,
+                                      "setup_s": tb1 - tb, "phase_estimations_per_s": batched_pe_rate}
+    out["batched_f32_over_plain_steps"] = (batched_same / plain) if plain else None
+    out["batched_f32_over_plain_steps_wall"] = (batched_same_wall / plain) if plain else None
+    out["batched_f32_over_plain_phase_estimations"] = (batched_pe_rate / plain_pe_rate) if plain_pe_rate else None
     return out
+
+
+def _chain_loop_seconds(stdout):
+    """Seconds of the Metropolis loop from the qms driver's 'chain loop: N steps
+    in T s' line."""
+    for ln in stdout.splitlines():
+        if ln.startswith("chain loop:"):
+            return float(ln.split(" in ")[1].split()[0])
+    return None
+
+
+def config1_section():
+    """Config 1: the triangle (3 spins, 4 energy qubits + acceptance = 8 qubits),
+    beta 1, 200 steps, seed 42, window [-1, 3], 20 thermalisation steps, through the
+    drop-in qms driver on the GPU; the rate is the driver's own loop timer."""
+    exe = os.path.join(ROOT, "suqa_gb300", "_build", "qms")
+    outp = "/tmp/suqa_config1.txt"
+    if os.path.exists(outp):
+        os.remove(outp)
+    cp = subprocess.run([exe, "1.0", "200", "1", "4", outp, "--seed", "42", "--ene-min", "-1", "--ene-max", "3",
+                         "--thermalization", "20"], capture_output=True, text=True)
+    loop_s = _chain_loop_seconds(cp.stdout) if cp.returncode == 0 else None
+    rows = 0
+    if os.path.exists(outp):
+        rows = sum(1 for ln in open(outp) if ln and not ln.startswith("#"))
+        os.remove(outp)
+    acc = None
+    for ln in cp.stdout.splitlines():
+        if "acceptance:" in ln:
+            acc = ln.split("acceptance:")[1].strip()
+    return {"workload": "triangle QMS, 8 qubits FP64, beta 1, 200 steps, seed 42 (drop-in qms driver)",
+            "steps_per_s": 200 / loop_s if loop_s else None, "loop_s": loop_s, "rows_written": rows,
+            "acceptance": acc, "rc": cp.returncode}
 
 
 def qsa_section(n_walks, walk_steps, f64_walks=16, cpu=True, seed=2025):
@@ -293,8 +354,10 @@ def run_reference_arm(args, rank, world):
         if i >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
+    from suqa_gb300.workloads import algorithmic_bytes
+    ms_per_step = algorithmic_bytes(gates, args.n, bpa) / (value * 1e9) * 1e3  # whole circuit at this rate
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "impl": "reference",
             "dtype": args.precision, "data": "synthetic",
             "config": {"workload": f"random circuit, {args.n} qubits {args.precision.upper()}, "
                                    f"{args.gates} gates, measure every 100", "n_qubits": args.n},
@@ -408,19 +471,29 @@ def main():
     # an even number of steps, so both pipelines finish together
     pipe_steps = args.steps + (args.steps & 1)
     pipe_bits = [None] * pipe_steps
+    # per step and state: events around the upload, the circuit and the download
+    # on the state's stream, so the end-to-end time can be attributed
+    pipe_ev = [None] * pipe_steps
 
-    def pipeline(stx, ore, oim, steps):
+    def pipeline(stx, strm, ore, oim, steps):
         for i in steps:
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            ev[0].record(strm)
             stx.upload(h_re.data_ptr(), h_im.data_ptr())
+            ev[1].record(strm)
             pipe_bits[i] = apply_circuit(stx, gates)
+            stx.flush()
+            ev[2].record(strm)
             stx.download(ore.data_ptr(), oim.data_ptr())
+            ev[3].record(strm)
+            pipe_ev[i] = ev
 
     barrier()
     e4 = torch.cuda.Event(enable_timing=True)
     e5 = torch.cuda.Event(enable_timing=True)
     e4.record(stream)
-    workers = [threading.Thread(target=pipeline, args=(st, o_re, o_im, range(0, pipe_steps, 2))),
-               threading.Thread(target=pipeline, args=(st2, o2_re, o2_im, range(1, pipe_steps, 2)))]
+    workers = [threading.Thread(target=pipeline, args=(st, stream, o_re, o_im, range(0, pipe_steps, 2))),
+               threading.Thread(target=pipeline, args=(st2, s2, o2_re, o2_im, range(1, pipe_steps, 2)))]
     for w in workers:
         w.start()
     for w in workers:
@@ -431,6 +504,17 @@ def main():
     ms_e2e = e4.elapsed_time(e5) / pipe_steps
     e2e_value = alg * world / (ms_e2e / 1e3) / 1e9
     pipe_ok = all(b == bits_all[0] for b in pipe_bits + bits_all)
+    up_ms = [e[0].elapsed_time(e[1]) for e in pipe_ev]
+    cir_ms = [e[1].elapsed_time(e[2]) for e in pipe_ev]
+    down_ms = [e[2].elapsed_time(e[3]) for e in pipe_ev]
+    state_b = (1 << n) * bpa
+    e2e_parts = {"upload_ms_median": statistics.median(up_ms), "upload_ms_max": max(up_ms),
+                 "upload_gbs_median": state_b / (statistics.median(up_ms) / 1e3) / 1e9,
+                 "circuit_ms_median": statistics.median(cir_ms), "circuit_ms_max": max(cir_ms),
+                 "download_ms_median": statistics.median(down_ms), "download_ms_max": max(down_ms),
+                 "download_gbs_median": state_b / (statistics.median(down_ms) / 1e3) / 1e9,
+                 "note": "device-side intervals on each state's stream; a circuit interval includes the "
+                         "waits for its measurements' host decisions"}
     st2.close()
     del o2_re, o2_im
 
@@ -496,7 +580,28 @@ def main():
         h32r = torch.from_numpy(r32).pin_memory()
         h32i = torch.from_numpy(i32).pin_memory()
         st32.upload(h32r.data_ptr(), h32i.data_ptr())
-        apply_circuit(st32, gates)
+        bits32 = apply_circuit(st32, gates)
+        # FP32 against the FP64 result of the same circuit from the same state
+        # (o_re, o_im hold the FP64 state after one application, bits_all[0] its
+        # measured bits): flipped measurement bits, and the amplitude error when
+        # every bit agrees
+        d32r = torch.empty(1 << n, dtype=torch.float32).pin_memory()
+        d32i = torch.empty(1 << n, dtype=torch.float32).pin_memory()
+        st32.download(d32r.data_ptr(), d32i.data_ptr())
+        flipped = sum(1 for a, b in zip(bits32, bits_all[0]) if a != b)
+        fp32_err = None
+        if flipped == 0:
+            r64 = o_re.numpy()
+            i64 = o_im.numpy()
+            dr = d32r.numpy().astype(np.float64) - r64
+            di = d32i.numpy().astype(np.float64) - i64
+            nrm = math.sqrt(float(np.dot(r64, r64)) + float(np.dot(i64, i64)))
+            amax = float(np.sqrt(np.max(r64 * r64 + i64 * i64)))
+            emax = float(np.sqrt(np.max(dr * dr + di * di)))
+            fp32_err = {"normwise_rel": math.sqrt(float(np.dot(dr, dr)) + float(np.dot(di, di))) / nrm,
+                        "max_abs_over_max_amplitude": emax / amax}
+            del dr, di
+        del d32r, d32i
         st32.flush()
         torch.cuda.synchronize()
         st32.set_timing(True)
@@ -512,6 +617,10 @@ def main():
         k32, l32, b32 = st32.kernel_time()
         alg32 = algorithmic_bytes(gates, n, 8)
         fp32_line = {"value": alg32 / (ms32 / 1e3) / 1e9, "unit": "GB/s", "ms_per_step": ms32,
+                     "vs_fp64": {"measured_bits": len(bits32), "flipped_bits": flipped,
+                                 "amplitude_error": fp32_err,
+                                 "against": "the FP64 GPU result of the same circuit and initial state (FP64 is "
+                                            "the oracle-pinned path)"},
                      "gates_per_s": len([g for g in gates if g[0] != "measure"]) / (ms32 / 1e3),
                      "pass_kernel_gbs": b32 / (k32 / 1e3) / 1e9 if k32 > 0 else None}
         st32.close()
@@ -566,6 +675,7 @@ def main():
     qms = None
     if rank == 0 and not args.skip_qms:
         qms = qms_section(args.qms_chains, args.qms_steps)
+        qms["config1_triangle"] = config1_section()
     qsa = None
     if rank == 0 and not args.skip_qsa:
         qsa = qsa_section(args.qsa_walks, args.qsa_steps, cpu=not args.skip_cpu)
@@ -593,7 +703,8 @@ def main():
                         "mode": "pipelined: two states on two streams and host threads, each step uploads "
                                 "its input, runs the circuit, downloads its state",
                         "steps": pipe_steps,
-                        "same_measured_bits": pipe_ok},
+                        "same_measured_bits": pipe_ok,
+                        "parts": e2e_parts},
                 "e2e_serial": {"value": alg * world / (ms_e2e_serial / 1e3) / 1e9, "unit": "GB/s",
                                "ms_per_step": ms_e2e_serial, "mode": "one state: upload, circuit, download in turn"},
                 "roofline": roofline,

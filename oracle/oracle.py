@@ -324,9 +324,11 @@ class Pcg32:
 
 def apply_circuit(ost: "OracleState", gates):
     """Applies a benchmark circuit (suqa_gb300.workloads.random_circuit form) on the
-    oracle; used only for CPU-baseline timing."""
+    oracle (CPU-baseline timing, parity of the full-size benchmark circuit);
+    returns the measured bits."""
     L = load()
     p = ost.p
+    bits = []
     for g in gates:
         k = g[0]
         if k == "x":
@@ -343,4 +345,5 @@ def apply_circuit(ost: "OracleState", gates):
         elif k == "ptp":
             L.or_apply_pauli(p, len(g[1]), _u32arr(g[1]), _u32arr(g[2]), g[3], 0, 0)
         elif k == "measure":
-            L.or_measure_qbit(p, g[1], g[2])
+            bits.append(int(L.or_measure_qbit(p, g[1], g[2])))
+    return bits

@@ -58,6 +58,16 @@ RUNS = [
                                 "--thermalization", "2"], {"TFIM_J": "1.0", "TFIM_H": "1.2"}),
     ("tfim_s6", "qms_tfim_s6", ["2.0", "12", "1", "5", "{out}", "--seed", "13", "--ene-min", "-9", "--ene-max", "9",
                                 "--thermalization", "1"], {"TFIM_J": "1.0", "TFIM_H": "0.5"}),
+    # 7-10 spins with the 6-qubit energy register (14-17 qubits); the reference CPU
+    # build needs 20 s to 2 min per run, so the runs are short
+    ("tfim_s7_e6", "qms_tfim_s7", ["1.1", "12", "1", "6", "{out}", "--seed", "21", "--ene-min", "-14", "--ene-max",
+                                   "14", "--thermalization", "0"], {"TFIM_J": "1.0", "TFIM_H": "0.9"}),
+    ("tfim_s8_e6", "qms_tfim_s8", ["0.6", "6", "1", "6", "{out}", "--seed", "22", "--ene-min", "-16", "--ene-max",
+                                   "16", "--thermalization", "0"], {"TFIM_J": "1.0", "TFIM_H": "1.3"}),
+    ("tfim_s9_e6", "qms_tfim_s9", ["1.7", "6", "1", "6", "{out}", "--seed", "23", "--ene-min", "-18", "--ene-max",
+                                   "18", "--thermalization", "0"], {"TFIM_J": "1.0", "TFIM_H": "0.6"}),
+    ("tfim_s10_e6", "qms_tfim_s10", ["1.0", "3", "1", "6", "{out}", "--seed", "24", "--ene-min", "-20", "--ene-max",
+                                     "20", "--thermalization", "0"], {"TFIM_J": "1.0", "TFIM_H": "1.0"}),
 ]
 
 
@@ -107,11 +117,18 @@ def gate_fixtures():
     np.savez_compressed(os.path.join(HERE, "gates_results.npz"), **arrays)
 
 
-def run_fixtures():
+def run_fixtures(only=None):
+    """Runs the reference drivers of RUNS (or the named subset, merged into the
+    existing manifest) and records their output files."""
     rdir = os.path.join(HERE, "runs")
     os.makedirs(rdir, exist_ok=True)
     manifest = {}
+    mpath = os.path.join(rdir, "manifest.json")
+    if only and os.path.exists(mpath):
+        manifest = json.load(open(mpath))
     for name, exe, args, env in RUNS:
+        if only and name not in only:
+            continue
         out = os.path.join(rdir, f"{name}.txt")
         for p in (out, out + "_revcounts"):
             if os.path.exists(p):
@@ -166,6 +183,10 @@ def pcg_fixture():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) > 2 and sys.argv[1] == "--runs":  # regenerate only the named run fixtures
+        build_reference()
+        run_fixtures(sys.argv[2:])
+        sys.exit(0)
     build_reference()
     gate_fixtures()
     run_fixtures()

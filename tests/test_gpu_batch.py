@@ -1,6 +1,8 @@
 """Batched QMS chains on the device against the reference CPU qms driver built
 with the same transverse-field Ising plugin (fixtures tests/golden/runs/tfim_*):
 the written (E, A) rows must be identical, in FP64."""
+import re
+
 import numpy as np
 import pytest
 
@@ -12,7 +14,7 @@ pytestmark = pytest.mark.gpu
 def chain_from_manifest(name):
     man = golden_io.run_manifest()[name]
     a = man["args"]
-    spins = int(name.split("_s")[1])
+    spins = int(re.match(r"tfim_s(\d+)", name).group(1))
     kv = {a[i]: a[i + 1] for i in range(5, len(a) - 1) if a[i].startswith("--")}
     from suqa_gb300.batch import TfimChain
     return TfimChain(spins=spins, ene_qbits=int(a[3]), steps=int(a[1]), beta=float(a[0]),
@@ -32,7 +34,8 @@ def fmt(xs):
     return ["%.16g" % x for x in xs]
 
 
-@pytest.mark.parametrize("name", ["tfim_s4", "tfim_s5", "tfim_s6"])
+@pytest.mark.parametrize("name", ["tfim_s4", "tfim_s5", "tfim_s6", "tfim_s7_e6", "tfim_s8_e6", "tfim_s9_e6",
+                                  "tfim_s10_e6"])
 def test_batched_chain_matches_reference_run(name):
     from suqa_gb300.batch import run_tfim_batch
     c = chain_from_manifest(name)
@@ -254,3 +257,26 @@ def test_uneven_lengths_and_fp64_autotune():
             with pytest.raises(Exception):
                 b.state(i)  # a chain that never ran has no state yet
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_reference_chains_of_every_ring_length_in_one_batch(precision):
+    """The seven reference runs (rings of 4-10 spins, energy registers of 4-6
+    qubits: 9 to 17 qubits, every storage mode) as one batch: each chain writes
+    the reference's rows.  FP32 must reproduce the same rows too: every
+    measurement of these runs has a probability margin far above FP32 rounding."""
+    from suqa_gb300.batch import run_tfim_batch
+    names = ["tfim_s4", "tfim_s5", "tfim_s6", "tfim_s7_e6", "tfim_s8_e6", "tfim_s9_e6", "tfim_s10_e6"]
+    chains = [chain_from_manifest(n) for n in names]
+    runs, _ = run_tfim_batch(chains, precision)
+    for name, c, r in zip(names, chains, runs):
+        E, A = r.reference_rows(c.steps)
+        wE, wA = _golden_rows(name)
+        if precision == "f64":
+            assert fmt(E) == wE and fmt(A) == wA, name
+        else:
+            # FP32 energies come from the same integer register read-outs; the
+            # observable is an average of measured spins: identical when every
+            # outcome is
+            assert [float(x) for x in wE] == [float(x) for x in fmt(E)], name
+            assert [float(x) for x in wA] == [float(x) for x in fmt(A)], name

@@ -18,7 +18,8 @@ BUILD = os.path.join(ROOT, "suqa_gb300", "_build")
 def run_driver(name, tmp_path):
     man = golden_io.run_manifest()[name]
     out = str(tmp_path / f"{name}.txt")
-    exe = os.path.join(BUILD, man["driver"] if not name.startswith("tfim") else "qms_tfim_s" + name.split("_s")[1])
+    exe = os.path.join(BUILD, man["driver"] if not name.startswith("tfim")
+                       else "qms_tfim_s" + re.match(r"tfim_s(\d+)", name).group(1))
     argv = [exe] + [a.replace("{out}", out) for a in man["args"]]
     env = dict(os.environ)
     env.update(man["env"])
@@ -51,7 +52,7 @@ def test_evo_probabilities_match_reference(tmp_path):
     assert np.max(np.abs(got - want)) < 1e-11
 
 
-@pytest.mark.parametrize("name", ["tfim_s4", "tfim_s5", "tfim_s6"])
+@pytest.mark.parametrize("name", ["tfim_s4", "tfim_s5", "tfim_s6", "tfim_s7_e6"])
 def test_qms_tfim_drivers_match_reference_output(name, tmp_path):
     """The host-driven drop-in path with the TFIM ring plugin."""
     man, out, stdout = run_driver(name, tmp_path)

@@ -79,6 +79,14 @@ int sq_set_fusion(sq_state* s, int enabled);
  * and precision; else 6 .. 13 in FP64, 6 .. 14 in FP32).  A tuning knob: results
  * do not depend on it beyond floating-point summation order. */
 int sq_set_tile_qubits(sq_state* s, int k);
+/* How multi-tile passes move tiles between HBM and shared memory (no
+ * counterpart in the reference; a tuning knob, results are identical):
+ * 1 (default) = bulk asynchronous copies (cp.async.bulk on the TMA engine), one
+ * per run of contiguous amplitudes, completion on an mbarrier whose waits are
+ * bounded (a pass that gives up sets an error word that the next synchronising
+ * call reports as SQ_ERR_CUDA); 0 = 16-byte vector loads and stores through
+ * registers. */
+int sq_set_staging(sq_state* s, int mode);
 
 /* --- state utilities: src/suqa.cu:70-111 --- */
 int sq_init_state(sq_state* s);                   /* suqa::init_state */
@@ -106,6 +114,26 @@ int sq_apply_phase_list(sq_state* s, uint32_t q0, uint32_t q_size, const double*
  * P = (x)_k paulis[k] on qubits[k], paulis 1=X 2=Y 3=Z; k in 1..32 */
 int sq_apply_pauli_rotation(sq_state* s, uint32_t k, const uint32_t* qubits, const uint32_t* paulis,
                             double phase, uint64_t gc, int flags);
+
+/* --- dense blocks (no counterpart in the reference: its gates are applied one
+ * kernel at a time, include/suqa_kernels.cuh:82-526) ---
+ * Applies a 2^k x 2^k complex matrix U (row-major, u_re[r * 2^k + c]) to qubits
+ * qubits[0..k-1] (index bit b of U <-> qubits[b]), k in 1..5, on the elements
+ * where every bit of gc is set (gc disjoint from the qubits).  U is applied as
+ * given (no unitarity check).  FP32 states of 2^12 amplitudes or more run it on
+ * the tensor cores (tcgen05, TF32 three-term split: ~2^-21 relative per
+ * product), otherwise on the CUDA cores in FP64 arithmetic.  States need at
+ * least 5 qubits. */
+int sq_apply_unitary(sq_state* s, uint32_t k, const uint32_t* qubits, const double* u_re, const double* u_im,
+                     uint64_t gc);
+/* Automatic dense blocks (FP32 states): runs of consecutive gates on at most
+ * five qubits with at least min_gates gates (uncontrolled X gates not counted)
+ * are multiplied into one matrix on the host (FP64) and applied as one dense
+ * block.  0 (default) disables it. */
+int sq_set_dense_fusion(sq_state* s, int min_gates);
+/* Engine for dense blocks: 0 (default) tensor cores where the state allows,
+ * 1 CUDA cores. */
+int sq_set_dense_engine(sq_state* s, int engine);
 
 /* --- measurement: src/suqa.cu:673-727 --- */
 /* p1 = sum |a_i|^2 over bit q set; c = (r < p1); zero the other branch; rescale

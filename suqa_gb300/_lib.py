@@ -84,6 +84,7 @@ _SIGS = {
     "sq_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "sq_set_fusion": (C.c_int, [C.c_void_p, C.c_int]),
     "sq_set_tile_qubits": (C.c_int, [C.c_void_p, C.c_int]),
+    "sq_set_staging": (C.c_int, [C.c_void_p, C.c_int]),
     "sq_upload": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "sq_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "sq_init_state": (C.c_int, [C.c_void_p]),
@@ -99,6 +100,10 @@ _SIGS = {
     "sq_apply_phase_list": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_double), C.c_uint64]),
     "sq_apply_pauli_rotation": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                           C.c_double, C.c_uint64, C.c_int]),
+    "sq_apply_unitary": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double), C.c_uint64]),
+    "sq_set_dense_fusion": (C.c_int, [C.c_void_p, C.c_int]),
+    "sq_set_dense_engine": (C.c_int, [C.c_void_p, C.c_int]),
     "sq_measure_qbit": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double, C.POINTER(C.c_uint32)]),
     "sq_prob_filter": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.POINTER(C.c_double)]),
     "sq_apply_qms_w": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, C.c_double]),

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -39,7 +40,12 @@ struct HostOp {
     double c = 0.0, s = 0.0;
     std::vector<double> tab;        // complex pairs (PLIST: cos/sin, W: f1/f2)
     uint8_t gdefer = 0;             // its scale factor is kept in sq_state::gscale
+    // OP_DENSE: 2^k x 2^k complex matrix (re, im interleaved, [out][in]) on the
+    // qubits of flip, index bit b = the b-th lowest qubit of flip
+    std::vector<double> dense;
 };
+
+using cplx = std::complex<double>;
 
 inline int popc(uint64_t x) { return __builtin_popcountll(x); }
 
@@ -70,6 +76,16 @@ struct sq_state {
     // renormalisations of measurement and vnormalize; it is applied to memory
     // (one fused scale) before any read-out and when it drifts far from 1.
     double gscale = 1.0;
+    int staging = 1;                // multi-tile passes move tiles by bulk asynchronous copies
+    // dense blocks: automatic fusion threshold (0 = off), engine (0 tensor cores
+    // where possible, 1 CUDA cores), and the per-launch operand ring
+    int dense_fusion = 0;
+    int dense_engine = 0;
+    void* dense_dev = nullptr;      // kDenseSlots x kMaxDensePerPass x 32 KiB
+    void* dense_host = nullptr;     // pinned mirror
+    cudaEvent_t dense_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool dense_ev_used[4] = {false, false, false, false};
+    uint32_t dense_slot = 0;
     int nsm = 1;
     int max_grid = 1;
     std::vector<std::pair<uint64_t, int>> occ_cache;  // (block << 32 | smem) -> resident CTAs per SM
@@ -152,17 +168,255 @@ int launch_pass_t(sq_state* s, const sqk::PassArgs& a, const sqk::Prog& p, int g
     return SQ_OK;
 }
 
+// ---- dense blocks ---------------------------------------------------------
+constexpr int kDenseSlots = 4;
+constexpr int kMaxDensePerPass = 8;
+constexpr size_t kDenseBlockBytes = 32768;  // one dense op's data in a launch
+
+uint64_t deposit64(uint64_t j, uint64_t m) {
+    uint64_t r = 0;
+    for (int b = 0; m; ++b) {
+        const uint64_t low = m & (~m + 1ull);
+        if ((j >> b) & 1ull) r |= low;
+        m ^= low;
+    }
+    return r;
+}
+uint32_t extract64(uint64_t g, uint64_t m) {
+    uint32_t r = 0;
+    for (int b = 0; m; ++b) {
+        const uint64_t low = m & (~m + 1ull);
+        if (g & low) r |= 1u << b;
+        m ^= low;
+    }
+    return r;
+}
+
+// Qubits an op reads or writes.
+uint64_t op_support(const HostOp& h) { return h.flip | h.cmask | h.zy; }
+
+// Ops whose stored action can be folded into a dense block.
+bool op_fusable(const HostOp& h) {
+    return (h.kind == sqk::OP_SWAPP || h.kind == sqk::OP_YP || h.kind == sqk::OP_HP || h.kind == sqk::OP_PAULI ||
+            h.kind == sqk::OP_PHASE) &&
+           h.tab.empty();
+}
+
+// Applies a queued op, in the form the pass kernel applies it (the factors of
+// uncontrolled H and Pauli rotations stay in the global scale), to v, a vector
+// over the qubits of bm (index bit b = the b-th lowest qubit of bm) holding
+// every qubit the op touches.
+void apply_stored(const HostOp& h, uint64_t bm, std::vector<cplx>& v) {
+    const uint32_t D = (uint32_t)v.size();
+    const cplx I(0.0, 1.0);
+    auto ipow = [&](int k) -> cplx {
+        switch (k & 3) {
+            case 0: return cplx(1.0, 0.0);
+            case 1: return I;
+            case 2: return cplx(-1.0, 0.0);
+            default: return -I;
+        }
+    };
+    const bool deferred = h.cmask == 0ull && h.gdefer;
+    const bool cbig = std::fabs(h.c) >= std::fabs(h.s);
+    const double u = (h.kind == sqk::OP_PAULI && deferred) ? (cbig ? h.s / h.c : h.c / h.s) : 0.0;
+    auto rot = [&](cplx a, cplx b, int k) -> cplx {
+        const cplx ib = ipow(k) * b;
+        if (deferred) return cbig ? a + u * ib : u * a + ib;
+        return h.c * a + h.s * ib;
+    };
+    if (h.kind == sqk::OP_PHASE) {
+        for (uint32_t j = 0; j < D; ++j)
+            if ((deposit64(j, bm) & h.cmask) == h.cval) v[j] *= cplx(h.c, h.s);
+        return;
+    }
+    if (h.kind == sqk::OP_PAULI && h.flip == 0ull) {  // all-Z string: diagonal
+        for (uint32_t j = 0; j < D; ++j) {
+            const uint64_t G = deposit64(j, bm);
+            if (!deferred && (G & h.cmask) != h.cval) continue;
+            v[j] = rot(v[j], v[j], (1 + 2 * (popc(G & h.zy) & 1)) & 3);
+        }
+        return;
+    }
+    const uint64_t low = h.flip & (~h.flip + 1ull);
+    const int fz = popc(h.flip & h.zy) & 1;
+    for (uint32_t j = 0; j < D; ++j) {
+        const uint64_t G = deposit64(j, bm);
+        if ((G & low) || (G & h.cmask) != h.cval) continue;
+        const uint32_t j1 = extract64(G ^ h.flip, bm);
+        const cplx a0 = v[j], a1 = v[j1];
+        switch (h.kind) {
+            case sqk::OP_SWAPP: v[j] = a1; v[j1] = a0; break;
+            case sqk::OP_YP: v[j1] = I * a0; v[j] = -I * a1; break;
+            case sqk::OP_HP:
+                if (h.cmask == 0ull) {
+                    v[j] = a0 + a1;
+                    v[j1] = a0 - a1;
+                } else {
+                    v[j] = 0.7071067811865475 * (a0 + a1);
+                    v[j1] = 0.7071067811865475 * (a0 - a1);
+                }
+                break;
+            default: {  // OP_PAULI with X/Y factors
+                const int pz0 = popc(G & h.zy) & 1;
+                const int k1 = (1 + h.ny + 2 * pz0) & 3, k0 = (1 + h.ny + 2 * (pz0 ^ fz)) & 3;
+                v[j] = rot(a0, a1, k0);
+                v[j1] = rot(a1, a0, k1);
+            }
+        }
+    }
+}
+
+// Replaces runs of at least min_weight fusable ops on at most five qubits by one
+// dense op each (uncontrolled X gates weigh 0: the pass's index frame moves them
+// for free).
+std::vector<HostOp> fuse_dense(std::vector<HostOp>&& ops, int min_weight) {
+    std::vector<HostOp> out;
+    out.reserve(ops.size());
+    size_t i = 0;
+    auto weight = [](const HostOp& h) {
+        return (h.kind == sqk::OP_SWAPP && h.cmask == 0ull && popc(h.flip) == 1) ? 0 : 1;
+    };
+    while (i < ops.size()) {
+        if (!op_fusable(ops[i]) || popc(op_support(ops[i])) > sqk::kDenseQubits) {
+            out.push_back(std::move(ops[i++]));
+            continue;
+        }
+        uint64_t un = op_support(ops[i]);
+        int w = weight(ops[i]);
+        size_t j = i + 1;
+        while (j < ops.size() && op_fusable(ops[j]) && popc(un | op_support(ops[j])) <= sqk::kDenseQubits) {
+            un |= op_support(ops[j]);
+            w += weight(ops[j]);
+            ++j;
+        }
+        if (w >= min_weight && j - i >= 2) {
+            const uint32_t D = 1u << popc(un);
+            HostOp d;
+            d.kind = sqk::OP_DENSE;
+            d.flip = un;
+            d.dense.assign(2 * (size_t)D * D, 0.0);
+            std::vector<cplx> col(D);
+            for (uint32_t c = 0; c < D; ++c) {
+                std::fill(col.begin(), col.end(), cplx(0.0, 0.0));
+                col[c] = 1.0;
+                for (size_t k = i; k < j; ++k) apply_stored(ops[k], un, col);
+                for (uint32_t r = 0; r < D; ++r) {
+                    d.dense[2 * ((size_t)r * D + c)] = col[r].real();
+                    d.dense[2 * ((size_t)r * D + c) + 1] = col[r].imag();
+                }
+            }
+            out.push_back(std::move(d));
+        } else {
+            for (size_t k = i; k < j; ++k) out.push_back(std::move(ops[k]));
+        }
+        i = j;
+    }
+    return out;
+}
+
+float tf32_high_host(float x) {
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    b &= 0xFFFFE000u;
+    float r;
+    std::memcpy(&r, &b, 4);
+    return r;
+}
+
+// Writes one dense op's launch data into dst (kDenseBlockBytes): the op's matrix
+// (on its k qubits, tile positions pos[0..k-1] ascending) extended by the identity
+// to the five tile positions of bm5 (ascending), either as the tensor-core B
+// operand (TF32 high and low parts, core-matrix layout) or as a 32 x 32 complex
+// FP64 matrix for the CUDA-core path.
+void write_dense_block(const HostOp& h, uint32_t opmask_local, uint32_t bm5, bool tc, unsigned char* dst) {
+    const int k = popc(h.flip);
+    const uint32_t Dk = 1u << k;
+    // for each of the five block bits: which bit of the op's index it is, or -1
+    int src[5];
+    {
+        int b = 0, ob = 0;
+        for (uint32_t m = bm5; m; m &= m - 1u, ++b) {
+            const uint32_t low = m & (~m + 1u);
+            src[b] = (opmask_local & low) ? ob++ : -1;
+        }
+    }
+    auto split = [&](uint32_t j5, uint32_t& jop, uint32_t& jx) {
+        jop = 0;
+        jx = 0;
+        for (int b = 0; b < 5; ++b) {
+            const uint32_t bit = (j5 >> b) & 1u;
+            if (src[b] >= 0) jop |= bit << src[b];
+            else jx |= bit << b;
+        }
+    };
+    auto U5 = [&](uint32_t jo, uint32_t ji) -> cplx {
+        uint32_t oo, ox, io, ix;
+        split(jo, oo, ox);
+        split(ji, io, ix);
+        if (ox != ix) return cplx(0.0, 0.0);
+        return cplx(h.dense[2 * ((size_t)oo * Dk + io)], h.dense[2 * ((size_t)oo * Dk + io) + 1]);
+    };
+    if (!tc) {
+        double* out = reinterpret_cast<double*>(dst);
+        for (uint32_t jo = 0; jo < 32; ++jo)
+            for (uint32_t ji = 0; ji < 32; ++ji) {
+                const cplx u = U5(jo, ji);
+                out[2 * (jo * 32 + ji)] = u.real();
+                out[2 * (jo * 32 + ji) + 1] = u.imag();
+            }
+        return;
+    }
+    float* hi = reinterpret_cast<float*>(dst);
+    float* lo = hi + 4096;
+    for (uint32_t n = 0; n < 64; ++n)
+        for (uint32_t kk = 0; kk < 64; ++kk) {
+            const cplx u = U5(n & 31u, kk & 31u);
+            const int ro = (int)(n >> 5), ri = (int)(kk >> 5);
+            // D[c][n] = sum_k A[c][k] B[k][n], A = (Re x, Im x), D = (Re y, Im y)
+            const double val = (ro == 0) ? (ri == 0 ? u.real() : -u.imag()) : (ri == 0 ? u.imag() : u.real());
+            const float f = (float)val;
+            const float fh = tf32_high_host(f);
+            const size_t off = (size_t)(kk >> 3) * 512 + (n >> 3) * 64 + ((kk & 7) >> 2) * 32 + (n & 7) * 4 + (kk & 3);
+            hi[off] = fh;
+            lo[off] = (float)(val - (double)fh);
+        }
+}
+
+int ensure_dense_ring(sq_state* s) {
+    if (s->dense_dev) return SQ_OK;
+    const size_t bytes = (size_t)kDenseSlots * kMaxDensePerPass * kDenseBlockBytes;
+    if (cudaMalloc(&s->dense_dev, bytes) != cudaSuccess || cudaMallocHost(&s->dense_host, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SQ_ERR_NOMEM, "allocation of the dense-block buffers failed");
+    }
+    for (int i = 0; i < kDenseSlots; ++i) SQ_CUDA(cudaEventCreateWithFlags(&s->dense_ev[i], cudaEventDisableTiming));
+    return SQ_OK;
+}
+
 // Executes ops[i0, i1) as one pass, with an optional reduction at its end.
 int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, int red, uint64_t rmask,
              uint64_t rval) {
     const int n = (int)s->n;
     uint64_t need = 0;
-    for (size_t i = i0; i < i1; ++i) need |= ops[i].flip;
+    int ndense = 0;
+    for (size_t i = i0; i < i1; ++i) {
+        need |= ops[i].flip;
+        if (ops[i].kind == sqk::OP_DENSE) ++ndense;
+    }
     int K = s->kp;
     const int needbits = popc(need | 3ull);
     if ((int)s->n > small_max(s) && needbits > K) K = needbits;
+    // dense blocks: FP32 tiles of 2^12 amplitudes (two CTAs per SM with the
+    // tensor-core operands); FP64 (CUDA-core path, with a scratch copy of the
+    // tile) at most 2^12
+    if (ndense && (int)s->n > small_max(s)) K = std::max(needbits, 12);
     if (K > n) K = n;
     if (K > tile_cap(s)) return fail(SQ_ERR_UNSUPPORTED, "gate touches too many qubits for one tile");
+    if (ndense && s->prec == SQ_F64 && K > 12)
+        return fail(SQ_ERR_UNSUPPORTED, "dense block in a pass whose tile exceeds 12 qubits (FP64)");
+    if (ndense && K < sqk::kDenseQubits) return fail(SQ_ERR_UNSUPPORTED, "dense blocks need states of 5 qubits or more");
+    const bool dense_tc = ndense && s->prec == SQ_F32 && K >= 12 && s->dense_engine == 0;
     // contiguous low block L, then the high tile qubits
     int L = K;
     while (L > 0 && L + popc(L >= 64 ? 0 : (need >> L)) > K) --L;
@@ -184,6 +438,13 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     a.partials = s->d_partials;
     a.result = s->d_result;
     a.ticket = s->d_ticket;
+    a.err = reinterpret_cast<unsigned int*>(s->d_result + 3);
+    // bulk staging for multi-tile passes whose runs are whole 16-byte units of at
+    // least 128 bytes (shorter runs cost more per copy than they save)
+    {
+        const uint64_t rb = ((uint64_t)1 << L) * s->esz;
+        a.stage = (s->staging && K < n && rb % 16 == 0 && rb >= 128) ? 1 : 0;
+    }
     int nhb = 0;
     for (int b = L; b < n; ++b)
         if ((high >> b) & 1ull) a.hb[nhb++] = (uint8_t)b;
@@ -228,9 +489,19 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     // parity, collapse and reduction conditions) and the store writes every
     // element back to its logical position.  Passes with table ops (W, phase
     // lists: index-valued lookups) keep xm = 0.
-    bool frame_ok = true;
+    bool frame_ok = ndense == 0;  // dense blocks read the tile in logical order
     for (size_t i = i0; i < i1; ++i)
         if (ops[i].kind == sqk::OP_W || ops[i].kind == sqk::OP_PLIST) frame_ok = false;
+    unsigned char* dslot = nullptr;
+    int dslot_i = -1;
+    int dcount = 0;
+    if (ndense) {
+        int rc = ensure_dense_ring(s);
+        if (rc) return rc;
+        dslot_i = (int)(s->dense_slot++ % kDenseSlots);
+        if (s->dense_ev_used[dslot_i]) SQ_CUDA(cudaEventSynchronize(s->dense_ev[dslot_i]));  // its last launch is done
+        dslot = static_cast<unsigned char*>(s->dense_host) + (size_t)dslot_i * kMaxDensePerPass * kDenseBlockBytes;
+    }
     uint32_t xm = 0;       // tile-local frame
     uint64_t xg = 0;       // the same in global qubit positions
     uint32_t tabpos = 0;
@@ -300,15 +571,37 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
             std::memcpy(&p.tab[2 * tabpos], h.tab.data(), h.tab.size() * sizeof(double));
             tabpos += (uint32_t)(h.tab.size() / 2);
         }
+        if (h.kind == sqk::OP_DENSE) {
+            // extend the op's qubits to five tile bits with the lowest free ones
+            uint32_t bm5 = lf;
+            for (int b = 0; b < K && popc(bm5) < sqk::kDenseQubits; ++b)
+                if (!((bm5 | lcm) >> b & 1u)) bm5 |= 1u << b;
+            if (popc(bm5) != sqk::kDenseQubits) return fail(SQ_ERR_UNSUPPORTED, "no room for a dense block in the tile");
+            o.lflip = bm5;
+            o.tab = (uint32_t)dcount;
+            write_dense_block(h, lf, bm5, dense_tc, dslot + (size_t)dcount * kDenseBlockBytes);
+            ++dcount;
+        }
     }
 
     p.xm = xm;
+    p.ndense = dcount;
     p.rswap = (red == 1 && (xm & p.lrm)) ? 1 : 0;
     if (red == 2) p.lrv ^= xm & p.lrm;
     p.defer = p.defer >= 2 ? 1 : 0;  // deferring one factor costs as much as it saves
     const bool single = (K == n);
     const int block = single ? (K >= 10 ? 1024 : (K >= 8 ? 256 : 128)) : 256;
-    const size_t smem = tile_smem(s, K, L);
+    size_t smem = tile_smem(s, K, L);
+    if (dcount) {
+        // the dense work area: tensor-core operands (A chunk + B), or the scratch tile
+        a.dense_off = (uint32_t)((smem + 127) & ~(size_t)127);
+        smem = a.dense_off + (dense_tc ? (size_t)2 * 32768 : (size_t)2 * ((size_t)1 << K) * s->esz);
+        a.dense_tc = dense_tc ? 1 : 0;
+        const size_t bytes = (size_t)dcount * kDenseBlockBytes;
+        void* dev = static_cast<unsigned char*>(s->dense_dev) + (size_t)dslot_i * kMaxDensePerPass * kDenseBlockBytes;
+        SQ_CUDA(cudaMemcpyAsync(dev, dslot, bytes, cudaMemcpyHostToDevice, s->stream));
+        a.dense = dev;
+    }
     int occ = 0;
     {
         const int orc = s->prec == SQ_F64 ? resident_ctas<double>(s, block, smem, &occ)
@@ -334,6 +627,10 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     int rc = (s->prec == SQ_F64) ? launch_pass_t<double>(s, a, p, grid, block, smem)
                                  : launch_pass_t<float>(s, a, p, grid, block, smem);
     if (rc) return rc;
+    if (dcount) {
+        SQ_CUDA(cudaEventRecord(s->dense_ev[dslot_i], s->stream));
+        s->dense_ev_used[dslot_i] = true;
+    }
     if (s->timing) {
         SQ_CUDA(cudaEventRecord(e1, s->stream));
         s->ev_open.push_back({e0, e1});
@@ -353,6 +650,7 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
                 case sqk::OP_PLIST: fl += 6.0 * amps; break;
                 case sqk::OP_W: fl += 6.0 * amps; break;
                 case sqk::OP_COLLAPSE: case sqk::OP_SCALE: fl += 2.0 * amps; break;
+                case sqk::OP_DENSE: fl += 8.0 * sqk::kDenseDim * amps; break;  // 32 complex MACs per amplitude
                 default: break;
             }
         }
@@ -366,19 +664,32 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     return SQ_OK;
 }
 
+// The kernels' error word (d_result[3], copied with a reduction's result into
+// h_result[3]): a bounded wait inside a pass that gave up.
+int device_error(sq_state* s) {
+    unsigned int e = 0;
+    std::memcpy(&e, &s->h_result[3], sizeof(e));
+    if (e == 0u) return SQ_OK;
+    return fail(SQ_ERR_CUDA, "a pass kernel gave up waiting for its tile copies (error word " + std::to_string(e) + ")");
+}
+
 // Applies every queued op; with red != 0 the last pass also reduces and the
 // result is copied into s->h_result (synchronously).
 int flush(sq_state* s, int red = 0, uint64_t rmask = 0, uint64_t rval = 0) {
     std::vector<HostOp> ops;
     ops.swap(s->pending);
+    if (s->dense_fusion > 0 && s->prec == SQ_F32 && s->n >= (uint32_t)sqk::kDenseQubits && !ops.empty())
+        ops = fuse_dense(std::move(ops), s->dense_fusion);
     size_t i = 0;
     const int kcap = ((int)s->n <= small_max(s)) ? (int)s->n : std::max(s->kp, std::min(tile_cap(s), (int)s->n));
     while (i < ops.size()) {
         size_t j = i;
         uint64_t need = 0;
         uint32_t tab = 0;
+        int nd = 0;
         while (j < ops.size()) {
             const HostOp& h = ops[j];
+            if (h.kind == sqk::OP_DENSE && nd == kMaxDensePerPass) break;
             const uint64_t nn = need | h.flip;
             const int bits = popc(nn | 3ull);
             const bool fits_tile = ((int)s->n <= small_max(s)) ? true : (bits <= s->kp || (j == i && bits <= kcap));
@@ -388,6 +699,7 @@ int flush(sq_state* s, int red = 0, uint64_t rmask = 0, uint64_t rval = 0) {
             if (tab + h.tab.size() / 2 > (size_t)sqk::kMaxTab) break;
             need = nn;
             tab += (uint32_t)(h.tab.size() / 2);
+            if (h.kind == sqk::OP_DENSE) ++nd;
             ++j;
         }
         const bool last = (j == ops.size());
@@ -400,8 +712,10 @@ int flush(sq_state* s, int red = 0, uint64_t rmask = 0, uint64_t rval = 0) {
         if (rc) return rc;
     }
     if (red) {
-        SQ_CUDA(cudaMemcpyAsync(s->h_result, s->d_result, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        SQ_CUDA(cudaMemcpyAsync(s->h_result, s->d_result, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
         SQ_CUDA(cudaStreamSynchronize(s->stream));
+        int rc = device_error(s);
+        if (rc) return rc;
     }
     return SQ_OK;
 }
@@ -487,6 +801,8 @@ int sq_state_create(sq_state** out, uint32_t n, int precision) {
     }
     s->own_stream = true;
     cudaMemsetAsync(s->d_ticket, 0, sizeof(unsigned int), s->stream);
+    cudaMemsetAsync(s->d_result, 0, 4 * sizeof(double), s->stream);
+    std::memset(s->h_result, 0, 4 * sizeof(double));
     int rc = sq_init_state(s);
     if (rc) {
         sq_state_destroy(s);
@@ -509,6 +825,10 @@ int sq_state_destroy(sq_state* s) {
     if (s->d_result) cudaFree(s->d_result);
     if (s->d_ticket) cudaFree(s->d_ticket);
     if (s->h_result) cudaFreeHost(s->h_result);
+    for (auto e : s->dense_ev)
+        if (e) cudaEventDestroy(e);
+    if (s->dense_dev) cudaFree(s->dense_dev);
+    if (s->dense_host) cudaFreeHost(s->dense_host);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return SQ_OK;
@@ -556,14 +876,23 @@ int sq_synchronize(sq_state* s) {
     if (!s) return fail(SQ_ERR_ARG, "null state");
     int rc = flush(s);
     if (rc) return rc;
+    SQ_CUDA(cudaMemcpyAsync(&s->h_result[3], s->d_result + 3, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     SQ_CUDA(cudaStreamSynchronize(s->stream));
-    return SQ_OK;
+    return device_error(s);
 }
 
 int sq_set_fusion(sq_state* s, int enabled) {
     if (!s) return fail(SQ_ERR_ARG, "null state");
     int rc = flush(s);
     s->fusion = enabled ? 1 : 0;
+    return rc;
+}
+
+int sq_set_staging(sq_state* s, int mode) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    if (mode != 0 && mode != 1) return fail(SQ_ERR_ARG, "staging mode must be 0 (registers) or 1 (bulk copies)");
+    int rc = flush(s);
+    s->staging = mode;
     return rc;
 }
 
@@ -916,6 +1245,63 @@ int sq_apply_pauli_rotation(sq_state* s, uint32_t k, const uint32_t* qubits, con
     rc = enqueue(s, std::move(h));
     if (rc || !defer) return rc;
     return scale_by(s, f);
+}
+
+int sq_apply_unitary(sq_state* s, uint32_t k, const uint32_t* qubits, const double* u_re, const double* u_im,
+                     uint64_t gc) {
+    if (!s || !qubits || !u_re || !u_im) return fail(SQ_ERR_ARG, "null argument");
+    if (k < 1 || k > (uint32_t)sqk::kDenseQubits) return fail(SQ_ERR_ARG, "dense blocks act on 1 to 5 qubits");
+    if (s->n < (uint32_t)sqk::kDenseQubits) return fail(SQ_ERR_UNSUPPORTED, "dense blocks need states of 5 qubits or more");
+    int rc = check_mask(s, gc);
+    if (rc) return rc;
+    uint64_t m = 0;
+    for (uint32_t b = 0; b < k; ++b) {
+        if ((rc = check_q(s, qubits[b]))) return rc;
+        if (m >> qubits[b] & 1ull) return fail(SQ_ERR_ARG, "repeated qubit in a dense block");
+        m |= 1ull << qubits[b];
+    }
+    if (gc & m) return fail(SQ_ERR_ARG, "global control mask overlaps the block's qubits");
+    // caller's index bit b is qubits[b]; stored index bit b is the b-th lowest qubit
+    uint32_t pos[5];
+    for (uint32_t b = 0; b < k; ++b) pos[b] = (uint32_t)popc(m & ((1ull << qubits[b]) - 1ull));
+    const uint32_t D = 1u << k;
+    auto to_stored = [&](uint32_t j) {
+        uint32_t r = 0;
+        for (uint32_t b = 0; b < k; ++b)
+            if ((j >> b) & 1u) r |= 1u << pos[b];
+        return r;
+    };
+    HostOp h;
+    h.kind = sqk::OP_DENSE;
+    h.flip = m;
+    h.cmask = gc;
+    h.cval = gc;
+    h.skm = gc;
+    h.skv = gc;
+    h.dense.assign(2 * (size_t)D * D, 0.0);
+    for (uint32_t r = 0; r < D; ++r)
+        for (uint32_t c = 0; c < D; ++c) {
+            const size_t o = (size_t)to_stored(r) * D + to_stored(c);
+            h.dense[2 * o] = u_re[(size_t)r * D + c];
+            h.dense[2 * o + 1] = u_im[(size_t)r * D + c];
+        }
+    return enqueue(s, std::move(h));
+}
+
+int sq_set_dense_fusion(sq_state* s, int min_gates) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    if (min_gates < 0) return fail(SQ_ERR_ARG, "min_gates must be >= 0");
+    int rc = flush(s);
+    s->dense_fusion = min_gates;
+    return rc;
+}
+
+int sq_set_dense_engine(sq_state* s, int engine) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    if (engine != 0 && engine != 1) return fail(SQ_ERR_ARG, "dense engine must be 0 (tensor cores) or 1 (CUDA cores)");
+    int rc = flush(s);
+    s->dense_engine = engine;
+    return rc;
 }
 
 int sq_apply_qms_w(sq_state* s, uint32_t q_acc, uint64_t mask_enew, uint32_t shift, uint32_t E_old,

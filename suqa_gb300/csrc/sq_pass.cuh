@@ -33,7 +33,8 @@ enum OpKind : uint8_t {
     OP_PLIST = 5,     // a *= tab[(g >> shift) & zy] where (g & cmask) != 0
     OP_W = 6,         // QMS acceptance rotation, (f1, f2) = tab[(g0 & zy) >> shift]
     OP_COLLAPSE = 7,  // keep (g & cmask) == cval scaled by s, zero the rest
-    OP_SCALE = 8      // a *= s everywhere
+    OP_SCALE = 8,     // a *= s everywhere
+    OP_DENSE = 9      // 32 x 32 complex matrix on the five tile bits of lflip (sq_dense.cuh)
 };
 
 // One gate in tile-local form (144 bytes).  For pair operations the pairs are
@@ -66,7 +67,7 @@ struct Prog {
     int nops;
     int red;             // 0 none, 1 measurement split by rmask, 2 filter (g & rmask) == rval
     int defer;           // 1: uniform H / rotations defer their scale factor
-    int pad;
+    int ndense;          // OP_DENSE ops in the list
     uint64_t rmask, rval;
     uint32_t lrm, lrv;   // tile-local part of rmask / rval
     uint64_t orm, orv;   // part outside the tile
@@ -86,11 +87,80 @@ struct PassArgs {
     double* partials; // 2 per CTA
     double* result;   // 2 doubles
     unsigned int* ticket;
+    unsigned int* err;  // error word (bulk staging only): set when a bounded wait gives up
     int K, L;
     int store;        // 0 for a reduction-only pass
-    int pad;
+    int stage;        // 1: tiles move by bulk asynchronous copies (runs of 2^L elements), 0: through registers
     uint8_t hb[kMaxHigh];  // global positions of the tile qubits >= L
+    const void* dense;     // OP_DENSE data of this launch (op.tab selects a 32 KiB block)
+    int dense_tc;          // 1: dense ops on the tensor cores (FP32, tiles >= 2^12), 0: CUDA cores
+    uint32_t dense_off;    // byte offset of the dense work area in dynamic shared memory
 };
+
+// ---- bulk asynchronous copies (the TMA engine's cp.async.bulk) and mbarriers
+constexpr unsigned int kErrStageWait = 1u;   // a tile load did not complete in time
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                     smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0u;
+}
+// Waits for the phase with the given parity to complete, for at most kWaitLimitNs;
+// false (and the error word set) when it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, unsigned int* err,
+                                                  unsigned int code) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (global_ns() - t0 > kWaitLimitNs) {
+            if (err) atomicOr(err, code);
+            return false;
+        }
+    }
+    return true;
+}
+// global -> shared, completion counted in bytes on the mbarrier
+__device__ __forceinline__ void bulk_load(void* sdst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(sdst)),
+        "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+// shared -> global, tracked by this thread's bulk groups
+__device__ __forceinline__ void bulk_store(void* gdst, const void* ssrc, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(smem_u32(ssrc)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// orders this thread's generic-proxy shared-memory accesses with later async-proxy ones
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 
 template <typename T> struct VecT;
 template <> struct VecT<double> { typedef double2 type; static constexpr int W = 2; };
@@ -201,6 +271,12 @@ __device__ __forceinline__ void block_reduce2(double& a, double& b, double (*sh)
     __syncthreads();
 }
 
+}  // namespace sqk
+
+#include "sq_dense.cuh"
+
+namespace sqk {
+
 template <typename T>
 __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs a,
                                                const __grid_constant__ Prog p) {
@@ -223,7 +299,32 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
             if ((h >> j) & 1u) o |= 1ull << a.hb[j];
         offs[h] = o;
     }
+    // bulk staging: warp 0 issues one asynchronous copy per run of 2^L elements
+    // (re and im) against an mbarrier, and writes tiles back the same way; the
+    // host enables it only when a run is a multiple of 16 bytes
+    const bool bulk = a.stage != 0;
+    const uint32_t run_bytes = (1u << L) * (uint32_t)sizeof(T);
+    __shared__ __align__(8) uint64_t stage_bar;
+    uint32_t stage_phase = 0u;
+    // dense ops: mbarriers, and on the tensor-core path a 64-column TMEM accumulator
+    // held by warp 0 for the whole launch
+    __shared__ __align__(16) DenseSmem dsm;
+    const bool dense_tc = p.ndense > 0 && a.dense_tc != 0 && sizeof(T) == 4;
+    uint32_t ph_b = 0u, ph_mma = 0u;
+    int b_loaded = -1;
+    unsigned char* dbuf = smem_raw + a.dense_off;
+    if (threadIdx.x == 0) {
+        if (bulk) mbar_init(&stage_bar, 1u);
+        if (dense_tc) {
+            mbar_init(&dsm.bar_b, 1u);
+            mbar_init(&dsm.bar_mma, 1u);
+        }
+        if (bulk || dense_tc) asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (dense_tc && threadIdx.x < 32) tmem_alloc(&dsm.tmem, kDenseTmemCols);
+    tc_fence_before();
     __syncthreads();
+    tc_fence_after();
 
     T* gre = reinterpret_cast<T*>(a.re);
     T* gim = reinterpret_cast<T*>(a.im);
@@ -246,7 +347,30 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
         if (!any) continue;  // uniform over the CTA
 
         // ---- load the tile (16-byte vectors, runs of 2^L contiguous elements)
-        if ((1u << L) >= (uint32_t)W) {
+        if (bulk) {
+            if (threadIdx.x < 32) {
+                bulk_wait_read_all();  // this lane's stores of the previous tile have read the buffer
+                __syncwarp();
+                if (threadIdx.x == 0) mbar_arrive_expect_tx(&stage_bar, 2u * TS * (uint32_t)sizeof(T));
+                __syncwarp();
+                for (uint32_t h = threadIdx.x; h < nh; h += 32) {
+                    const uint64_t g = base | offs[h];
+                    bulk_load(sre + (h << L), gre + g, run_bytes, &stage_bar);
+                    bulk_load(sim + (h << L), gim + g, run_bytes, &stage_bar);
+                }
+            }
+            const bool ok = mbar_wait_bounded(&stage_bar, stage_phase, a.err, kErrStageWait);
+            if (__syncthreads_or(!ok)) {
+                // give the copies in flight a second bounded wait, then leave
+                mbar_wait_bounded(&stage_bar, stage_phase, nullptr, 0u);
+                if (threadIdx.x < 32) {
+                    bulk_wait_all();
+                    if (dense_tc) tmem_dealloc(dsm.tmem, kDenseTmemCols);
+                }
+                return;
+            }
+            stage_phase ^= 1u;
+        } else if ((1u << L) >= (uint32_t)W) {
             for (uint32_t v = threadIdx.x; v < TS / W; v += blockDim.x) {
                 const uint32_t t = v * W;
                 const uint64_t g = base | offs[t >> L] | (t & lowmask);
@@ -280,7 +404,25 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
             }
             const int kind = op.kind;
             const uint32_t lcm = op.lcm, lcv = op.lcv;
-            if (kind <= OP_PAULI && !(kind == OP_PAULI && op.lflip == 0u) || kind == OP_W) {
+            if (kind == OP_DENSE) {
+                bool ok = true;
+                if constexpr (sizeof(T) == 4) {
+                    if (dense_tc)
+                        ok = dense_tc_apply(sre, TS, op, reinterpret_cast<const float*>(a.dense), dbuf, dsm, ph_b,
+                                            ph_mma, b_loaded, a.err);
+                    else
+                        dense_cc<T>(sre, TS, op, reinterpret_cast<const double*>(a.dense) + (size_t)op.tab * 4096u,
+                                    reinterpret_cast<T*>(dbuf), dsm);
+                } else {
+                    dense_cc<T>(sre, TS, op, reinterpret_cast<const double*>(a.dense) + (size_t)op.tab * 4096u,
+                                reinterpret_cast<T*>(dbuf), dsm);
+                }
+                if (!ok) {  // a bounded wait gave up: nothing in flight is left behind
+                    if (bulk && threadIdx.x < 32) bulk_wait_all();
+                    if (threadIdx.x < 32) tmem_dealloc(dsm.tmem, kDenseTmemCols);
+                    return;
+                }
+            } else if (kind <= OP_PAULI && !(kind == OP_PAULI && op.lflip == 0u) || kind == OP_W) {
                 const uint32_t lp = op.lpair, lf = op.lflip;
                 // pairs (t0, t0 ^ lf) with bit lp of t0 clear and its control bits
                 // equal to lcv, enumerated directly (none if lp is a control bit
@@ -475,7 +617,20 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
         if (a.store) {
             const bool scaled = sigma != 1.0;
             const uint32_t xm = p.xm;
-            if ((1u << L) >= (uint32_t)W) {
+            if (bulk && !scaled && (xm & lowmask) == 0u) {
+                // the frame only permutes whole runs: logical run h is physical run h ^ xh
+                fence_proxy_async_smem();
+                __syncthreads();
+                if (threadIdx.x < 32) {
+                    const uint32_t xh = xm >> L;
+                    for (uint32_t h = threadIdx.x; h < nh; h += 32) {
+                        const uint64_t g = base | offs[h];
+                        bulk_store(gre + g, sre + ((h ^ xh) << L), run_bytes);
+                        bulk_store(gim + g, sim + ((h ^ xh) << L), run_bytes);
+                    }
+                    bulk_commit();
+                }
+            } else if ((1u << L) >= (uint32_t)W) {
                 const uint32_t xv = xm & ~(uint32_t)(W - 1), xe = xm & (uint32_t)(W - 1);
                 for (uint32_t v = threadIdx.x; v < TS / W; v += blockDim.x) {
                     const uint32_t t = v * W;
@@ -502,7 +657,17 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                 }
             }
         }
+        if (bulk) fence_proxy_async_smem();  // before the next tile's copies overwrite the buffer
         __syncthreads();
+    }
+    if (bulk && threadIdx.x < 32) bulk_wait_all();  // stores complete before the CTA leaves
+    if (dense_tc) {
+        tc_fence_before();
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            tc_fence_after();
+            tmem_dealloc(dsm.tmem, kDenseTmemCols);
+        }
     }
 
     if (!p.red) return;

@@ -96,6 +96,32 @@ class State:
         """Tile size of the fused passes (0: default)."""
         check(self.L.sq_set_tile_qubits(self.h, k))
 
+    def apply_unitary(self, qubits, u):
+        """A 2^k x 2^k complex matrix on qubits (index bit b <-> qubits[b]), k <= 5,
+        under the current global control mask."""
+        u = np.asarray(u, dtype=np.complex128)
+        k = len(qubits)
+        if u.shape != (1 << k, 1 << k):
+            raise ValueError("matrix shape does not match the qubit count")
+        re = np.ascontiguousarray(u.real)
+        im = np.ascontiguousarray(u.imag)
+        qs = (C.c_uint32 * k)(*qubits)
+        check(self.L.sq_apply_unitary(self.h, k, qs, re.ctypes.data_as(C.POINTER(C.c_double)),
+                                      im.ctypes.data_as(C.POINTER(C.c_double)), self.gc_mask))
+
+    def set_dense_fusion(self, min_gates: int):
+        """FP32: fuse runs of >= min_gates gates on <= 5 qubits into dense blocks (0 off)."""
+        check(self.L.sq_set_dense_fusion(self.h, min_gates))
+
+    def set_dense_engine(self, engine: int):
+        """Dense blocks on the tensor cores (0, default) or the CUDA cores (1)."""
+        check(self.L.sq_set_dense_engine(self.h, engine))
+
+    def set_staging(self, mode: int):
+        """Tile staging of multi-tile passes: 1 bulk asynchronous copies (default),
+        0 vector loads and stores through registers."""
+        check(self.L.sq_set_staging(self.h, mode))
+
     def get_state(self) -> np.ndarray:
         N = self.size()
         re = np.empty(N, dtype=np.float64)

@@ -18,7 +18,7 @@ def _ph(x):
     return float.fromhex(x) if ("0x" in x or "0X" in x) else float(x)
 
 
-def run_script(lines, precision="f64", fusion=True):
+def run_script(lines, precision="f64", fusion=True, dense_fusion=0):
     st = None
     out = []
     it = iter(lines)
@@ -33,6 +33,8 @@ def run_script(lines, precision="f64", fusion=True):
                 st.close()
             st = State(int(a[0]), precision)
             st.set_fusion(fusion)
+            if dense_fusion:
+                st.set_dense_fusion(dense_fusion)
             continue
         if cmd == "setstate":
             vals = np.array([float.fromhex(v) for v in next(it).split()])

@@ -172,6 +172,30 @@ def test_tile_size_does_not_change_results(precision):
             st.set_tile_qubits(3)
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("n,k", [(16, 10), (18, 12), (21, 0), (23, 11)])
+def test_bulk_staging_is_bit_identical_to_register_staging(precision, n, k):
+    """Multi-tile passes move tiles by bulk asynchronous copies (runs of 2^L
+    amplitudes, completion on an mbarrier) or through registers; the arithmetic
+    is the same, so the measured bits and every amplitude must be identical.
+    The circuits hold X gates on low and high qubits (index frames with and
+    without a part below L), controlled gates and measurements."""
+    from suqa_gb300 import State
+    from suqa_gb300.workloads import apply_circuit, random_circuit
+    gates = random_circuit(n, 160, seed=40 + n, measure_every=40)
+    results = []
+    for mode in (0, 1):
+        with State(n, precision) as st:
+            st.set_tile_qubits(k)
+            st.set_staging(mode)
+            st.apply_h(list(range(n)))
+            bits = apply_circuit(st, gates)
+            st.synchronize()
+            results.append((bits, st.get_state()))
+    assert results[0][0] == results[1][0]
+    assert np.array_equal(results[0][1], results[1][1])
+
+
 def test_fp64_fma_rate_probe_reports_a_rate():
     """The benchmark's FP64 FMA-rate probe (libsq_probe.so, the tile pass's
     ceiling in bench.py) runs and gives a plausible rate: more than 50 G

@@ -570,6 +570,56 @@ def main():
                               "peak_source": "sqb_fp64_fma_rate (libsq_probe.so): independent DFMA chains on every SM, measured in "
                                              "this run (of measured)"}}
 
+    # secondary: the same FP64 circuit with double-float arithmetic (hi + lo FP32
+    # pairs on the FP32 pipe, doubles in memory), against the FP64-arithmetic result
+    # of the same circuit and state (o_re, o_im; bits_all[0])
+    df_line = None
+    if args.precision == "f64" and rank == 0:
+        st.set_double_float(True)
+        st.upload(h_re.data_ptr(), h_im.data_ptr())
+        bits_df = apply_circuit(st, gates)
+        dfr = torch.empty_like(o_re).pin_memory()
+        dfi = torch.empty_like(o_im).pin_memory()
+        st.download(dfr.data_ptr(), dfi.data_ptr())
+        flipped_df = sum(1 for x, y in zip(bits_df, bits_all[0]) if x != y)
+        df_err = None
+        if flipped_df == 0:
+            r64, i64 = o_re.numpy(), o_im.numpy()
+            dr = dfr.numpy() - r64
+            di = dfi.numpy() - i64
+            nrm = math.sqrt(float(np.dot(r64, r64)) + float(np.dot(i64, i64)))
+            amax = float(np.sqrt(np.max(r64 * r64 + i64 * i64)))
+            df_err = {"normwise_rel": math.sqrt(float(np.dot(dr, dr)) + float(np.dot(di, di))) / nrm,
+                      "max_abs_over_max_amplitude": float(np.sqrt(np.max(dr * dr + di * di))) / amax}
+            del dr, di
+        del dfr, dfi
+        for _ in range(args.warmup):
+            apply_circuit(st, gates)
+        st.flush()
+        torch.cuda.synchronize()
+        st.set_timing(True)
+        st.kernel_time()
+        d0, d1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        d0.record(stream)
+        for _ in range(args.steps):
+            apply_circuit(st, gates)
+        st.flush()
+        d1.record(stream)
+        torch.cuda.synchronize()
+        msdf = d0.elapsed_time(d1) / args.steps
+        kdf, ldf, bdf = st.kernel_time()
+        st.set_timing(False)
+        st.set_double_float(False)
+        df_line = {"value": alg / (msdf / 1e3) / 1e9, "unit": "GB/s", "ms_per_step": msdf,
+                   "speedup_over_fp64_arithmetic": ms_step / msdf,
+                   "pass_kernel_gbs": bdf / (kdf / 1e3) / 1e9 if kdf > 0 else None,
+                   "pass_kernel_frac_of_hbm": (bdf / (kdf / 1e3) / 1e9 / peaks.get("hbm_gbs", 6800.0))
+                   if kdf > 0 else None,
+                   "vs_fp64_arithmetic": {"measured_bits": len(bits_df), "flipped_bits": flipped_df,
+                                          "amplitude_error": df_err},
+                   "arithmetic": "double-float (hi + lo FP32, 48 significand bits) on the FP32 pipe; amplitudes "
+                                 "stored as IEEE doubles; not the headline (FP64 arithmetic is)"}
+
     # secondary: the same circuit with FP32 amplitudes (FP64 reductions)
     fp32_line = None
     if args.precision == "f64" and rank == 0:
@@ -623,6 +673,51 @@ def main():
                                             "the oracle-pinned path)"},
                      "gates_per_s": len([g for g in gates if g[0] != "measure"]) / (ms32 / 1e3),
                      "pass_kernel_gbs": b32 / (k32 / 1e3) / 1e9 if k32 > 0 else None}
+        # dense blocks on the tensor cores: a QFT-heavy FP32 circuit (40 QFT /
+        # inverse-QFT pairs on random 5-qubit registers, 1200 gates) with automatic
+        # dense fusion off and on, from the same state
+        rng = np.random.default_rng(3)
+        regs = [sorted(int(q) for q in rng.choice(n, size=5, replace=False)) for _ in range(40)]
+
+        def qft_circuit(sx):
+            for r in regs:
+                sx.apply_qft(r)
+                sx.apply_qft_inverse(r[::-1])
+
+        dense = {}
+        outs = {}
+        for fusion in (0, 4):
+            st32.set_dense_fusion(fusion)
+            st32.upload(h32r.data_ptr(), h32i.data_ptr())
+            qft_circuit(st32)
+            st32.synchronize()
+            st32.reset_stats()
+            st32.set_timing(True)
+            st32.kernel_time()
+            q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            q0.record(stream)
+            for _ in range(args.steps):
+                qft_circuit(st32)
+            st32.flush()
+            q1.record(stream)
+            torch.cuda.synchronize()
+            kq, lq, bq = st32.kernel_time()
+            st32.set_timing(False)
+            sq = st32.stats()
+            dense[f"fusion_{fusion}"] = {"ms_per_step": q0.elapsed_time(q1) / args.steps,
+                                         "passes_per_step": sq["passes"] / args.steps,
+                                         "pass_kernel_gbs": bq / (kq / 1e3) / 1e9 if kq > 0 else None}
+            st32.upload(h32r.data_ptr(), h32i.data_ptr())
+            qft_circuit(st32)
+            outs[fusion] = st32.get_state()
+        st32.set_dense_fusion(0)
+        a0, a4 = outs[0], outs[4]
+        dense["speedup"] = dense["fusion_0"]["ms_per_step"] / dense["fusion_4"]["ms_per_step"]
+        dense["max_abs_diff_over_max_amplitude"] = float(np.max(np.abs(a4 - a0)) / np.max(np.abs(a0)))
+        dense["workload"] = (f"{n}-qubit FP32 state, 40 QFT + inverse-QFT pairs on random 5-qubit registers "
+                             f"(1200 gates); dense blocks by tcgen05 (TF32 three-term split)")
+        del outs, a0, a4
+        fp32_line["dense_blocks"] = dense
         st32.close()
         del h32r, h32i
         st = None
@@ -710,6 +805,7 @@ def main():
                 "roofline": roofline,
                 "cpu_baseline": cpu,
                 "fp32_same_circuit": fp32_line,
+                "fp64_double_float": df_line,
                 "fp64_30_qubits": n30_line,
                 "qms_batched": qms,
                 "qsa_walks": qsa}

@@ -126,6 +126,13 @@ int sq_apply_pauli_rotation(sq_state* s, uint32_t k, const uint32_t* qubits, con
  * least 5 qubits. */
 int sq_apply_unitary(sq_state* s, uint32_t k, const uint32_t* qubits, const double* u_re, const double* u_im,
                      uint64_t gc);
+/* FP64 states: run the arithmetic of multi-tile passes (gates without tables or
+ * dense blocks) in double-float on the FP32 pipe instead of the FP64 pipe (no
+ * counterpart in the reference).  Amplitudes stay IEEE doubles in memory; each
+ * pass converts them to hi + lo FP32 pairs (48 significand bits) and back with
+ * integer operations.  Rounding differs from FP64 arithmetic at the 1e-14 level
+ * per operation.  Default 0. */
+int sq_set_double_float(sq_state* s, int enabled);
 /* Automatic dense blocks (FP32 states): runs of consecutive gates on at most
  * five qubits with at least min_gates gates (uncontrolled X gates not counted)
  * are multiplied into one matrix on the host (FP64) and applied as one dense

@@ -103,6 +103,7 @@ _SIGS = {
     "sq_apply_unitary": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double), C.c_uint64]),
     "sq_set_dense_fusion": (C.c_int, [C.c_void_p, C.c_int]),
+    "sq_set_double_float": (C.c_int, [C.c_void_p, C.c_int]),
     "sq_set_dense_engine": (C.c_int, [C.c_void_p, C.c_int]),
     "sq_measure_qbit": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double, C.POINTER(C.c_uint32)]),
     "sq_prob_filter": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.POINTER(C.c_double)]),

@@ -7,10 +7,10 @@
 // D[c][n] = sum_k A[c][k] B[k][n] with k = (re/im, input index), n = (re/im,
 // output index), A = the tile's columns, B = [[Re U, Im U], [-Im U, Re U]]^T, by
 // tcgen05.mma kind::tf32 into a tensor-memory accumulator, M = 128 columns per
-// chunk, N = 64, K = 64.  TF32 keeps 10 mantissa bits, so each operand is split
-// into a high part (the FP32 value; the tensor core reads its top bits) and the
-// remainder, and D = A_hi B_hi + A_hi B_lo + A_lo B_hi (the three-term TF32
-// split; the dropped A_lo B_lo term is below 2^-21 of the result).  B_hi and B_lo
+// chunk, N = 64, K = 64.  TF32 keeps 10 fraction bits, so each operand is split
+// into a high part (rounded to TF32) and the remainder (rounded to TF32), and
+// D = A_hi B_hi + A_hi B_lo + A_lo B_hi + A_lo B_lo: what is lost is the rounding
+// of the remainders, about 2^-24 of each product.  B_hi and B_lo
 // are prepared on the host in the operand layout; A is gathered from the tile
 // per chunk.  Operand layout (no swizzle, K-major): per K-slice of 8 elements a
 // 128 x 8 (A) or 64 x 8 (B) block of 8-row x 16-byte core matrices, the two
@@ -69,8 +69,11 @@ __device__ __forceinline__ void tmem_ld_32x16(uint32_t taddr, float (&r)[16]) {
         : "r"(taddr)
         : "memory");
 }
-// the value with its low 13 mantissa bits cleared: what a TF32 operand keeps
-__device__ __forceinline__ float tf32_high(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+// the value rounded to TF32 (10 fraction bits, to nearest, ties away from zero):
+// exactly representable, so the tensor core's own conversion leaves it unchanged
+__device__ __forceinline__ float tf32_round(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
 
 // b-th set bit position of m, for b < popc(m)
 __device__ __forceinline__ uint32_t nth_bit(uint32_t m, int b) {
@@ -147,7 +150,7 @@ __device__ inline bool dense_tc_apply(float* tile, uint32_t TS, const Op& op, co
         // depend on how the tensor core converts FP32 inputs)
         for (int blk = warp; blk < 256; blk += nw) {
             const int sl = blk >> 5, g = (blk >> 1) & 15, kh = blk & 1;
-            A[blk * 32 + lane] = tf32_high(tile[ds.cdep[g * 8 + r8] + ds.kdep[sl * 8 + kh * 4 + kq]]);
+            A[blk * 32 + lane] = tf32_round(tile[ds.cdep[g * 8 + r8] + ds.kdep[sl * 8 + kh * 4 + kq]]);
         }
         fence_proxy_async_smem();
         __syncthreads();
@@ -172,20 +175,22 @@ __device__ inline bool dense_tc_apply(float* tile, uint32_t TS, const Op& op, co
         ok = mbar_wait_bounded(&ds.bar_mma, ph_mma, err, kErrMmaWait);
         ph_mma ^= 1u;
         if (__syncthreads_or(!ok)) return false;
-        // third term: A_lo B_hi, the TF32 remainders of the same elements (the tile
-        // is unchanged until the results are written back)
+        // A_lo B_hi + A_lo B_lo with the remainders of the same elements, rounded to
+        // TF32 (the tile is unchanged until the results are written back)
         for (int blk = warp; blk < 256; blk += nw) {
             const int sl = blk >> 5, g = (blk >> 1) & 15, kh = blk & 1;
             const float x = tile[ds.cdep[g * 8 + r8] + ds.kdep[sl * 8 + kh * 4 + kq]];
-            A[blk * 32 + lane] = x - tf32_high(x);
+            A[blk * 32 + lane] = tf32_round(x - tf32_round(x));
         }
         fence_proxy_async_smem();
         __syncthreads();
         if (tid == 0) {
             tc_fence_after();
-            for (int sl = 0; sl < 8; ++sl)
-                mma_tf32(ds.tmem, umma_desc(a0 + (uint32_t)sl * 4096u, 128u, 256u),
-                         umma_desc(b0 + (uint32_t)sl * 2048u, 128u, 256u), 1u);
+            for (int sl = 0; sl < 8; ++sl) {
+                const uint64_t ad = umma_desc(a0 + (uint32_t)sl * 4096u, 128u, 256u);
+                mma_tf32(ds.tmem, ad, umma_desc(b0 + (uint32_t)sl * 2048u, 128u, 256u), 1u);
+                mma_tf32(ds.tmem, ad, umma_desc(b0 + 16384u + (uint32_t)sl * 2048u, 128u, 256u), 1u);
+            }
             mma_commit(&ds.bar_mma);
         }
         ok = mbar_wait_bounded(&ds.bar_mma, ph_mma, err, kErrMmaWait);

@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 namespace {
@@ -79,6 +80,9 @@ struct sq_state {
     int staging = 1;                // multi-tile passes move tiles by bulk asynchronous copies
     // dense blocks: automatic fusion threshold (0 = off), engine (0 tensor cores
     // where possible, 1 CUDA cores), and the per-launch operand ring
+    // FP64 states: multi-tile passes of gates without tables or dense blocks run
+    // their arithmetic in double-float on the FP32 pipe (sq_set_double_float)
+    int dfloat = 0;
     int dense_fusion = 0;
     int dense_engine = 0;
     void* dense_dev = nullptr;      // kDenseSlots x kMaxDensePerPass x 32 KiB
@@ -122,6 +126,10 @@ size_t tile_smem(const sq_state* s, int K, int L) {
     return (size_t)2 * ((size_t)1 << K) * s->esz + (size_t)8 * ((size_t)1 << (K - L));
 }
 
+// The pass kernel for element type T: FP64, FP32, or double-float arithmetic on
+// an FP64 state (multi-tile passes only, 256 threads, so no 64-register cap).
+template <typename T> constexpr int kThreadsOf = std::is_same<T, sqk::df64>::value ? 256 : 1024;
+
 // Opts the pass kernel into the shared memory a tile needs (above the default 48 KiB).
 template <typename T>
 int configure_smem(sq_state* s, size_t smem) {
@@ -130,10 +138,10 @@ int configure_smem(sq_state* s, size_t smem) {
         int optin = 0;
         cudaFuncAttributes fa;
         SQ_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
-        SQ_CUDA(cudaFuncGetAttributes(&fa, sqk::k_pass<T>));
+        SQ_CUDA(cudaFuncGetAttributes(&fa, sqk::k_pass<T, kThreadsOf<T>>));
         const int dyn = optin - (int)fa.sharedSizeBytes;
         if ((int)smem > dyn) return fail(SQ_ERR_UNSUPPORTED, "tile does not fit in shared memory");
-        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T, kThreadsOf<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
         configured_smem = dyn;
     }
     return SQ_OK;
@@ -153,7 +161,7 @@ int resident_ctas(sq_state* s, int block, size_t smem, int* out) {
     int rc = configure_smem<T>(s, smem);
     if (rc) return rc;
     int occ = 0;
-    SQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sqk::k_pass<T>, block, smem));
+    SQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sqk::k_pass<T, kThreadsOf<T>>, block, smem));
     s->occ_cache.emplace_back(key, occ);
     *out = occ;
     return SQ_OK;
@@ -163,7 +171,7 @@ template <typename T>
 int launch_pass_t(sq_state* s, const sqk::PassArgs& a, const sqk::Prog& p, int grid, int block, size_t smem) {
     int rc = configure_smem<T>(s, smem);
     if (rc) return rc;
-    sqk::k_pass<T><<<grid, block, smem, s->stream>>>(a, p);
+    sqk::k_pass<T, kThreadsOf<T>><<<grid, block, smem, s->stream>>>(a, p);
     SQ_CUDA(cudaGetLastError());
     return SQ_OK;
 }
@@ -315,10 +323,11 @@ std::vector<HostOp> fuse_dense(std::vector<HostOp>&& ops, int min_weight) {
     return out;
 }
 
-float tf32_high_host(float x) {
+// x rounded to TF32 (10 fraction bits, to nearest), as the kernel rounds its operand
+float tf32_round_host(float x) {
     uint32_t b;
     std::memcpy(&b, &x, 4);
-    b &= 0xFFFFE000u;
+    b = (b + 0x1000u) & 0xFFFFE000u;
     float r;
     std::memcpy(&r, &b, 4);
     return r;
@@ -375,11 +384,10 @@ void write_dense_block(const HostOp& h, uint32_t opmask_local, uint32_t bm5, boo
             const int ro = (int)(n >> 5), ri = (int)(kk >> 5);
             // D[c][n] = sum_k A[c][k] B[k][n], A = (Re x, Im x), D = (Re y, Im y)
             const double val = (ro == 0) ? (ri == 0 ? u.real() : -u.imag()) : (ri == 0 ? u.imag() : u.real());
-            const float f = (float)val;
-            const float fh = tf32_high_host(f);
+            const float fh = tf32_round_host((float)val);
             const size_t off = (size_t)(kk >> 3) * 512 + (n >> 3) * 64 + ((kk & 7) >> 2) * 32 + (n & 7) * 4 + (kk & 3);
             hi[off] = fh;
-            lo[off] = (float)(val - (double)fh);
+            lo[off] = tf32_round_host((float)(val - (double)fh));
         }
 }
 
@@ -565,6 +573,11 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         o.fsn = (float)o.sn;
         o.fu = (float)o.u;
         o.fun = (float)o.un;
+        o.dc = sqk::df_const_host(o.c);
+        o.ds = sqk::df_const_host(o.s);
+        o.dsn = sqk::df_const_host(o.sn);
+        o.du = sqk::df_const_host(o.u);
+        o.dun = sqk::df_const_host(o.un);
         o.xpar = (uint8_t)(h.kind == sqk::OP_PAULI ? (popc(xm & o.lzy) & 1) : 0);
         if (!h.tab.empty()) {
             o.tab = tabpos;
@@ -591,6 +604,11 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     p.defer = p.defer >= 2 ? 1 : 0;  // deferring one factor costs as much as it saves
     const bool single = (K == n);
     const int block = single ? (K >= 10 ? 1024 : (K >= 8 ? 256 : 128)) : 256;
+    // double-float arithmetic: FP64 multi-tile passes without tables or dense blocks
+    bool use_df = s->prec == SQ_F64 && s->dfloat && !single && ndense == 0;
+    for (size_t i = i0; i < i1 && use_df; ++i)
+        if (ops[i].kind == sqk::OP_W || ops[i].kind == sqk::OP_PLIST) use_df = false;
+    if (use_df) a.stage = 0;  // the tile is converted on its way in and out
     size_t smem = tile_smem(s, K, L);
     if (dcount) {
         // the dense work area: tensor-core operands (A chunk + B), or the scratch tile
@@ -604,8 +622,9 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     }
     int occ = 0;
     {
-        const int orc = s->prec == SQ_F64 ? resident_ctas<double>(s, block, smem, &occ)
-                                          : resident_ctas<float>(s, block, smem, &occ);
+        const int orc = use_df ? resident_ctas<sqk::df64>(s, block, smem, &occ)
+                               : (s->prec == SQ_F64 ? resident_ctas<double>(s, block, smem, &occ)
+                                                    : resident_ctas<float>(s, block, smem, &occ));
         if (orc) return orc;
     }
     const uint64_t wave = occ > 0 ? (uint64_t)s->nsm * (uint64_t)occ : (uint64_t)s->max_grid;
@@ -624,8 +643,9 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         }
         SQ_CUDA(cudaEventRecord(e0, s->stream));
     }
-    int rc = (s->prec == SQ_F64) ? launch_pass_t<double>(s, a, p, grid, block, smem)
-                                 : launch_pass_t<float>(s, a, p, grid, block, smem);
+    int rc = use_df ? launch_pass_t<sqk::df64>(s, a, p, grid, block, smem)
+                    : ((s->prec == SQ_F64) ? launch_pass_t<double>(s, a, p, grid, block, smem)
+                                           : launch_pass_t<float>(s, a, p, grid, block, smem));
     if (rc) return rc;
     if (dcount) {
         SQ_CUDA(cudaEventRecord(s->dense_ev[dslot_i], s->stream));
@@ -743,7 +763,8 @@ int materialize(sq_state* s) {
 // has an 8-bit exponent) by materialising it when it leaves [2^-lim, 2^lim].
 int scale_by(sq_state* s, double f) {
     s->gscale *= f;
-    const double lim = s->prec == SQ_F64 ? 300.0 : 40.0;
+    // stored amplitudes stay within the FP32 exponent range in FP32 and double-float modes
+    const double lim = (s->prec == SQ_F64 && !s->dfloat) ? 300.0 : 40.0;
     const double e = std::fabs(std::log2(std::fabs(s->gscale)));
     if (e > lim) return materialize(s);
     return SQ_OK;
@@ -1286,6 +1307,15 @@ int sq_apply_unitary(sq_state* s, uint32_t k, const uint32_t* qubits, const doub
             h.dense[2 * o + 1] = u_im[(size_t)r * D + c];
         }
     return enqueue(s, std::move(h));
+}
+
+int sq_set_double_float(sq_state* s, int enabled) {
+    if (!s) return fail(SQ_ERR_ARG, "null state");
+    int rc = flush(s);
+    if (!rc && enabled && !s->dfloat && s->prec == SQ_F64 && std::fabs(std::log2(std::fabs(s->gscale))) > 40.0)
+        rc = materialize(s);
+    s->dfloat = (enabled && s->prec == SQ_F64) ? 1 : 0;
+    return rc;
 }
 
 int sq_set_dense_fusion(sq_state* s, int min_gates) {

@@ -16,7 +16,10 @@
 // include/suqa_cpu.hpp of SUQA); each case names its source below.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
+
+#include "sq_df64.cuh"
 
 namespace sqk {
 
@@ -61,6 +64,7 @@ struct Op {
     double c, s, sn;       // sn = -s
     double u, un;          // deferred rotation: u = s/c (cbig) or c/s, un = -u
     float fc, fs, fsn, fu, fun, fpad;  // the same in FP32 for the FP32 kernel
+    df64 dc, ds, dsn, du, dun;         // the same as double-float pairs for the df64 kernel
 };
 
 struct Prog {
@@ -165,6 +169,19 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 template <typename T> struct VecT;
 template <> struct VecT<double> { typedef double2 type; static constexpr int W = 2; };
 template <> struct VecT<float>  { typedef float4  type; static constexpr int W = 4; };
+template <> struct VecT<df64>   { typedef double2 type; static constexpr int W = 2; };  // stored as doubles
+
+template <typename T> constexpr bool kIsDf = std::is_same<T, df64>::value;
+
+// a double as the kernel's element type (the df64 split uses integer operations)
+template <typename T> __device__ __forceinline__ T tconv(double d) {
+    if constexpr (kIsDf<T>) return df_from_double(d);
+    else return (T)d;
+}
+template <typename T> __device__ __forceinline__ T tzero() {
+    if constexpr (kIsDf<T>) return df64{0.0f, 0.0f};
+    else return (T)0;
+}
 
 __device__ __forceinline__ uint32_t insert_zero(uint32_t p, uint32_t b) {
     const uint32_t lo = p & ((1u << b) - 1u);
@@ -205,6 +222,7 @@ __device__ __forceinline__ double neg_if(double x, bool f) {
 __device__ __forceinline__ float neg_if(float x, bool f) {
     return __uint_as_float(__float_as_uint(x) ^ ((unsigned)f << 31));
 }
+__device__ __forceinline__ df64 neg_if(df64 x, bool f) { return df_neg_if(x, f); }
 
 // Deferred-scale rotation: with cbig, out = a + u*(i^k b) (u = s/c, the factor c
 // deferred); otherwise out = u*a + i^k b (u = c/s, the factor s deferred).
@@ -227,6 +245,7 @@ __device__ __forceinline__ void rot_deferred(T ar, T ai, T br, T bi, int k, T up
 // part + |a|^2 (FP64 accumulation; FP32 amplitudes square in FP32)
 __device__ __forceinline__ double add_sq(double part, double r, double i) { return fma(r, r, fma(i, i, part)); }
 __device__ __forceinline__ double add_sq(double part, float r, float i) { return part + (double)fmaf(r, r, i * i); }
+__device__ __forceinline__ double add_sq(double part, df64 r, df64 i) { return part + df_to_double(fma(r, r, i * i)); }
 
 __device__ __forceinline__ void scale_vec(double2& v, double s) { v.x *= s; v.y *= s; }
 
@@ -277,8 +296,10 @@ __device__ __forceinline__ void block_reduce2(double& a, double& b, double (*sh)
 
 namespace sqk {
 
-template <typename T>
-__global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs a,
+// T = double (FP64 state), float (FP32 state), or df64 (FP64 state, arithmetic in
+// double-float on the FP32 pipe; multi-tile passes of 256 threads).
+template <typename T, int MAXT = 1024>
+__global__ void __launch_bounds__(MAXT) k_pass(const __grid_constant__ PassArgs a,
                                                const __grid_constant__ Prog p) {
     typedef typename VecT<T>::type V;
     constexpr int W = VecT<T>::W;
@@ -302,7 +323,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
     // bulk staging: warp 0 issues one asynchronous copy per run of 2^L elements
     // (re and im) against an mbarrier, and writes tiles back the same way; the
     // host enables it only when a run is a multiple of 16 bytes
-    const bool bulk = a.stage != 0;
+    const bool bulk = a.stage != 0 && !kIsDf<T>;
     const uint32_t run_bytes = (1u << L) * (uint32_t)sizeof(T);
     __shared__ __align__(8) uint64_t stage_bar;
     uint32_t stage_phase = 0u;
@@ -370,6 +391,19 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                 return;
             }
             stage_phase ^= 1u;
+        } else if (kIsDf<T>) {  // doubles in HBM, double-float pairs in the tile
+            const double* dre = reinterpret_cast<const double*>(a.re);
+            const double* dim = reinterpret_cast<const double*>(a.im);
+            for (uint32_t v = threadIdx.x; v < TS / 2; v += blockDim.x) {
+                const uint32_t t = v * 2;
+                const uint64_t g = base | offs[t >> L] | (t & lowmask);
+                const double2 r2 = __ldcs(reinterpret_cast<const double2*>(dre + g));
+                const double2 i2 = __ldcs(reinterpret_cast<const double2*>(dim + g));
+                const df64 r0 = df_from_double(r2.x), r1 = df_from_double(r2.y);
+                const df64 i0 = df_from_double(i2.x), i1 = df_from_double(i2.y);
+                *reinterpret_cast<float4*>(sre + t) = make_float4(r0.hi, r0.lo, r1.hi, r1.lo);
+                *reinterpret_cast<float4*>(sim + t) = make_float4(i0.hi, i0.lo, i1.hi, i1.lo);
+            }
         } else if ((1u << L) >= (uint32_t)W) {
             for (uint32_t v = threadIdx.x; v < TS / W; v += blockDim.x) {
                 const uint32_t t = v * W;
@@ -397,7 +431,9 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
             const Op& op = p.ops[k];
             if ((base & op.ocm) != op.ocv) continue;
             T c, s, sneg, up, un;
-            if constexpr (sizeof(T) == 8) {
+            if constexpr (kIsDf<T>) {
+                c = op.dc; s = op.ds; sneg = op.dsn; up = op.du; un = op.dun;
+            } else if constexpr (sizeof(T) == 8) {
                 c = op.c; s = op.s; sneg = op.sn; up = op.u; un = op.un;
             } else {
                 c = op.fc; s = op.fs; sneg = op.fsn; up = op.fu; un = op.fun;
@@ -406,7 +442,9 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
             const uint32_t lcm = op.lcm, lcv = op.lcv;
             if (kind == OP_DENSE) {
                 bool ok = true;
-                if constexpr (sizeof(T) == 4) {
+                if constexpr (kIsDf<T>) {
+                    // not reached: the host runs passes with dense blocks in FP64
+                } else if constexpr (sizeof(T) == 4) {
                     if (dense_tc)
                         ok = dense_tc_apply(sre, TS, op, reinterpret_cast<const float*>(a.dense), dbuf, dsm, ph_b,
                                             ph_mma, b_loaded, a.err);
@@ -460,7 +498,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                         }
                         if (!op.gdefer) sigma *= 0.7071067811865475;
                     } else {
-                        const T h = (T)0.7071067811865475;
+                        const T h = tconv<T>(0.7071067811865475);
                         const bool ori = op.orient != 0;
                         for (uint32_t u = threadIdx.x; u < npair; u += blockDim.x) {
                             const uint32_t t0 = deposit_zeros(u, sel) | lcv, t1 = t0 ^ lf;
@@ -509,7 +547,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                         const uint32_t t0 = insert_zero(pp, lp), t1 = t0 ^ lf;
                         const uint64_t g0 = base | offs[t0 >> L] | (t0 & lowmask);
                         const uint32_t e = (uint32_t)((g0 & op.zy) >> op.shift);
-                        const T f1 = (T)p.tab[2 * (op.tab + e)], f2 = (T)p.tab[2 * (op.tab + e) + 1];
+                        const T f1 = tconv<T>(p.tab[2 * (op.tab + e)]), f2 = tconv<T>(p.tab[2 * (op.tab + e) + 1]);
                         const T a0r = sre[t0], a0i = sim[t0], a1r = sre[t1], a1i = sim[t1];
                         sre[t0] = f2 * a0r + f1 * a1r; sim[t0] = f2 * a0i + f1 * a1i;
                         sre[t1] = f1 * a0r - f2 * a1r; sim[t1] = f1 * a0i - f2 * a1i;
@@ -556,7 +594,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                         // include/suqa_kernels.cuh:246-259 (guard: any gc bit set)
                         if ((g & op.cmask) == 0ull) continue;
                         const uint32_t e = (uint32_t)((g >> op.shift) & op.zy);
-                        const T cx = (T)p.tab[2 * (op.tab + e)], cy = (T)p.tab[2 * (op.tab + e) + 1];
+                        const T cx = tconv<T>(p.tab[2 * (op.tab + e)]), cy = tconv<T>(p.tab[2 * (op.tab + e) + 1]);
                         sre[t] = ar * cx - ai * cy;
                         sim[t] = ar * cy + ai * cx;
                     } else if (kind == OP_COLLAPSE) {
@@ -565,11 +603,11 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
                         // a scale of exactly 1 (kept by the host's global scale) is skipped
                         const bool keep = (g & op.cmask) == op.cval;
                         if (unit) {
-                            sre[t] = keep ? ar : (T)0;
-                            sim[t] = keep ? ai : (T)0;
+                            sre[t] = keep ? ar : tzero<T>();
+                            sim[t] = keep ? ai : tzero<T>();
                         } else {
-                            sre[t] = (keep ? ar : (T)0) * s;
-                            sim[t] = (keep ? ai : (T)0) * s;
+                            sre[t] = (keep ? ar : tzero<T>()) * s;
+                            sim[t] = (keep ? ai : tzero<T>()) * s;
                         }
                     } else {  // OP_SCALE
                         sre[t] = ar * s;
@@ -579,7 +617,7 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
             }
             __syncthreads();
         }
-        const T sg = (T)sigma;
+        const T sg = tconv<T>(sigma);
         const double sg2 = sigma * sigma;
 
         // ---- reduction contribution and store.  Each thread sums the squared
@@ -617,7 +655,21 @@ __global__ void __launch_bounds__(1024) k_pass(const __grid_constant__ PassArgs 
         if (a.store) {
             const bool scaled = sigma != 1.0;
             const uint32_t xm = p.xm;
-            if (bulk && !scaled && (xm & lowmask) == 0u) {
+            if constexpr (kIsDf<T>) {
+                double* dre = reinterpret_cast<double*>(a.re);
+                double* dim = reinterpret_cast<double*>(a.im);
+                for (uint32_t v = threadIdx.x; v < TS / 2; v += blockDim.x) {
+                    const uint32_t t = v * 2;
+                    const uint64_t g = base | offs[t >> L] | (t & lowmask);
+                    // logical element t is the physical element t ^ xm
+                    df64 r0 = sre[t ^ xm], r1 = sre[(t + 1) ^ xm], i0 = sim[t ^ xm], i1 = sim[(t + 1) ^ xm];
+                    if (scaled) {
+                        r0 = r0 * sg; r1 = r1 * sg; i0 = i0 * sg; i1 = i1 * sg;
+                    }
+                    __stcs(reinterpret_cast<double2*>(dre + g), make_double2(df_to_double(r0), df_to_double(r1)));
+                    __stcs(reinterpret_cast<double2*>(dim + g), make_double2(df_to_double(i0), df_to_double(i1)));
+                }
+            } else if (bulk && !scaled && (xm & lowmask) == 0u) {
                 // the frame only permutes whole runs: logical run h is physical run h ^ xh
                 fence_proxy_async_smem();
                 __syncthreads();

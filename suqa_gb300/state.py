@@ -109,6 +109,10 @@ class State:
         check(self.L.sq_apply_unitary(self.h, k, qs, re.ctypes.data_as(C.POINTER(C.c_double)),
                                       im.ctypes.data_as(C.POINTER(C.c_double)), self.gc_mask))
 
+    def set_double_float(self, enabled: bool):
+        """FP64 states: arithmetic of multi-tile passes in double-float on the FP32 pipe."""
+        check(self.L.sq_set_double_float(self.h, 1 if enabled else 0))
+
     def set_dense_fusion(self, min_gates: int):
         """FP32: fuse runs of >= min_gates gates on <= 5 qubits into dense blocks (0 off)."""
         check(self.L.sq_set_dense_fusion(self.h, min_gates))

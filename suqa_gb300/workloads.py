@@ -105,3 +105,53 @@ def fp64_instructions(gates, n: int) -> int:
     measurement 2 (the squared-magnitude reduction; the collapse is a select)."""
     cost = {"h": 2, "u1": 2, "ptp": 2, "measure": 2}
     return sum(cost.get(g[0], 0) for g in gates) * (1 << n)
+
+
+def qft_blocks(n: int, pairs: int = 40, seed: int = 3):
+    """QFT / inverse-QFT pairs on random 5-qubit registers (the dense-block
+    workload): a list of registers, each applied as QFT then inverse QFT."""
+    rng = np.random.default_rng(seed)
+    return [sorted(int(q) for q in rng.choice(n, size=5, replace=False)) for _ in range(pairs)]
+
+
+def _main(argv=None):
+    """Runs one workload through libsq on the current GPU (the commands the
+    committed profiles were captured with):
+
+        python -m suqa_gb300.workloads random --n 24 --gates 300 --precision f64 [--double-float]
+        python -m suqa_gb300.workloads qft-blocks --n 24 --pairs 40 --precision f32 --dense-fusion 4
+    """
+    import argparse
+    from . import State
+    ap = argparse.ArgumentParser(prog="python -m suqa_gb300.workloads")
+    ap.add_argument("kind", choices=["random", "qft-blocks"])
+    ap.add_argument("--n", type=int, default=24)
+    ap.add_argument("--gates", type=int, default=300)
+    ap.add_argument("--pairs", type=int, default=40)
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--repeat", type=int, default=2)
+    ap.add_argument("--dense-fusion", type=int, default=0)
+    ap.add_argument("--double-float", action="store_true")
+    ap.add_argument("--staging", type=int, default=None)
+    args = ap.parse_args(argv)
+    dt = np.float64 if args.precision == "f64" else np.float32
+    re, im = random_state(args.n, 7, dt)
+    with State(args.n, args.precision) as st:
+        st.upload(re.ctypes.data, im.ctypes.data)
+        st.set_dense_fusion(args.dense_fusion)
+        st.set_double_float(args.double_float)
+        if args.staging is not None:
+            st.set_staging(args.staging)
+        for _ in range(args.repeat):
+            if args.kind == "random":
+                apply_circuit(st, random_circuit(args.n, args.gates, seed=7))
+            else:
+                for r in qft_blocks(args.n, args.pairs):
+                    st.apply_qft(r)
+                    st.apply_qft_inverse(r[::-1])
+        st.synchronize()
+        print(st.stats())
+
+
+if __name__ == "__main__":
+    _main()

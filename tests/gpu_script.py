@@ -18,7 +18,7 @@ def _ph(x):
     return float.fromhex(x) if ("0x" in x or "0X" in x) else float(x)
 
 
-def run_script(lines, precision="f64", fusion=True, dense_fusion=0):
+def run_script(lines, precision="f64", fusion=True, dense_fusion=0, dfloat=False):
     st = None
     out = []
     it = iter(lines)
@@ -35,6 +35,8 @@ def run_script(lines, precision="f64", fusion=True, dense_fusion=0):
             st.set_fusion(fusion)
             if dense_fusion:
                 st.set_dense_fusion(dense_fusion)
+            if dfloat:
+                st.set_double_float(True)
             continue
         if cmd == "setstate":
             vals = np.array([float.fromhex(v) for v in next(it).split()])

@@ -1,6 +1,6 @@
 """Dense k-qubit blocks (OP_DENSE): sq_apply_unitary against a numpy
 application of the same matrix, on the tensor-core path (FP32 states with tiles
-of 2^12 amplitudes or more: tcgen05 TF32 three-term split) and the CUDA-core
+of 2^12 amplitudes or more: tcgen05, TF32 high/remainder split, four products) and the CUDA-core
 path (FP64 states, small FP32 states), with global controls inside and outside
 the tile; and automatic fusion of gate runs on at most five qubits against the
 CPU oracle, which applies the same gates one by one.  FP32 tolerance 2e-5 of
@@ -76,7 +76,8 @@ def test_apply_unitary_matches_numpy(precision, n, engine):
 
 def test_tensor_and_cuda_core_engines_agree():
     """The same dense blocks on both engines of an FP32 state: the TF32
-    three-term split against FP64 arithmetic rounded to FP32."""
+    high/remainder split on the tensor cores against FP64 arithmetic rounded to
+    FP32 (12 blocks; the FP32 bar of the other tests)."""
     from suqa_gb300 import State
     rng = np.random.default_rng(5)
     n = 16
@@ -90,7 +91,9 @@ def test_tensor_and_cuda_core_engines_agree():
             for qs, U in blocks:
                 st.apply_unitary(qs, U)
             out.append(st.get_state())
-    assert float(np.max(np.abs(out[0] - out[1])) / np.max(np.abs(out[1]))) <= 1e-5
+    err = float(np.max(np.abs(out[0] - out[1])) / np.max(np.abs(out[1])))
+    print(f"\ntensor vs CUDA cores after 12 blocks: {err:.2e} of the largest amplitude")
+    assert err <= 2e-5
 
 
 @pytest.mark.parametrize("n", [13, 16, 20])

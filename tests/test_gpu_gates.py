@@ -39,6 +39,18 @@ def test_random_scripts_vs_oracle_fp64(seed):
     golden_io.compare_results(got, want, rtol=RTOL64)
 
 
+@pytest.mark.parametrize("seed", range(10))
+def test_random_scripts_vs_oracle_double_float(seed):
+    """FP64 states with the double-float arithmetic option: multi-tile passes
+    compute in hi + lo FP32 pairs (48 significand bits); the FP64 bar holds."""
+    n = [13, 14, 15, 16, 17][seed % 5]
+    lines = circuits.random_script(1300 + seed, n, 70, reference_only=False, random_init=False,
+                                   dump_every=35)
+    want = oracle.run_script(lines)
+    got = gpu_script.run_script(lines, "f64", dfloat=True)
+    golden_io.compare_results(got, want, rtol=RTOL64)
+
+
 @pytest.mark.parametrize("n", [18, 20, 22])
 def test_large_random_vs_oracle_fp64(n):
     lines = circuits.random_script(77 + n, n, 40, reference_only=False, random_init=False,

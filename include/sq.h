@@ -81,11 +81,13 @@ int sq_set_fusion(sq_state* s, int enabled);
 int sq_set_tile_qubits(sq_state* s, int k);
 /* How multi-tile passes move tiles between HBM and shared memory (no
  * counterpart in the reference; a tuning knob, results are identical):
- * 1 (default) = bulk asynchronous copies (cp.async.bulk on the TMA engine), one
- * per run of contiguous amplitudes, completion on an mbarrier whose waits are
- * bounded (a pass that gives up sets an error word that the next synchronising
- * call reports as SQ_ERR_CUDA); 0 = 16-byte vector loads and stores through
- * registers. */
+ * 0 = 16-byte vector loads and stores through registers; 1 = bulk asynchronous
+ * copies (cp.async.bulk on the TMA engine), one per run of contiguous
+ * amplitudes, completion on an mbarrier whose waits are bounded (a pass that
+ * gives up sets an error word that the next synchronising call reports as
+ * SQ_ERR_CUDA); 2 = the same with two tile buffers, the next tile's copies in
+ * flight while the current tile is worked on (tiles of 2^12 FP32 / 2^11 FP64
+ * amplitudes). */
 int sq_set_staging(sq_state* s, int mode);
 
 /* --- state utilities: src/suqa.cu:70-111 --- */

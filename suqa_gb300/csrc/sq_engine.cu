@@ -126,22 +126,25 @@ size_t tile_smem(const sq_state* s, int K, int L) {
     return (size_t)2 * ((size_t)1 << K) * s->esz + (size_t)8 * ((size_t)1 << (K - L));
 }
 
-// The pass kernel for element type T: FP64, FP32, or double-float arithmetic on
-// an FP64 state (multi-tile passes only, 256 threads, so no 64-register cap).
-template <typename T> constexpr int kThreadsOf = std::is_same<T, sqk::df64>::value ? 256 : 1024;
+// The pass kernel for element type T (FP64, FP32, or double-float arithmetic on
+// an FP64 state) and CTA size bound MAXT: multi-tile passes run 256 threads (no
+// 64-register cap), single-tile passes of small states up to 1024.
 
 // Opts the pass kernel into the shared memory a tile needs (above the default 48 KiB).
-template <typename T>
+template <typename T, int MAXT>
 int configure_smem(sq_state* s, size_t smem) {
     static std::atomic<int> configured_smem{-1};  // states may run in several host threads
     if ((int)smem > 48 * 1024 && configured_smem.load() < (int)smem) {
         int optin = 0;
         cudaFuncAttributes fa;
         SQ_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
-        SQ_CUDA(cudaFuncGetAttributes(&fa, sqk::k_pass<T, kThreadsOf<T>>));
+        SQ_CUDA(cudaFuncGetAttributes(&fa, sqk::k_pass<T, MAXT>));
         const int dyn = optin - (int)fa.sharedSizeBytes;
         if ((int)smem > dyn) return fail(SQ_ERR_UNSUPPORTED, "tile does not fit in shared memory");
-        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T, kThreadsOf<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+        // the whole unified L1 / shared array as shared memory: tiles are staged
+        // explicitly, and several CTAs per SM hide each other's waits
+        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T, MAXT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         configured_smem = dyn;
     }
     return SQ_OK;
@@ -150,28 +153,30 @@ int configure_smem(sq_state* s, size_t smem) {
 // CTAs of the pass kernel resident per SM at this block and tile size (cached per
 // state): a pass launches one full wave, every CTA looping over an equal share of
 // the tiles, so no partial last wave leaves SMs idle.
-template <typename T>
+template <typename T, int MAXT>
 int resident_ctas(sq_state* s, int block, size_t smem, int* out) {
-    const uint64_t key = ((uint64_t)block << 32) | (uint64_t)smem;
+    // kernels differ by element type: FP64 and double-float passes of one state share the cache
+    const uint64_t key = ((uint64_t)(std::is_same<T, sqk::df64>::value ? 1 : 0) << 63) | ((uint64_t)block << 32) |
+                         (uint64_t)smem;
     for (const auto& kv : s->occ_cache)
         if (kv.first == key) {
             *out = kv.second;
             return SQ_OK;
         }
-    int rc = configure_smem<T>(s, smem);
+    int rc = configure_smem<T, MAXT>(s, smem);
     if (rc) return rc;
     int occ = 0;
-    SQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sqk::k_pass<T, kThreadsOf<T>>, block, smem));
+    SQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sqk::k_pass<T, MAXT>, block, smem));
     s->occ_cache.emplace_back(key, occ);
     *out = occ;
     return SQ_OK;
 }
 
-template <typename T>
+template <typename T, int MAXT>
 int launch_pass_t(sq_state* s, const sqk::PassArgs& a, const sqk::Prog& p, int grid, int block, size_t smem) {
-    int rc = configure_smem<T>(s, smem);
+    int rc = configure_smem<T, MAXT>(s, smem);
     if (rc) return rc;
-    sqk::k_pass<T, kThreadsOf<T>><<<grid, block, smem, s->stream>>>(a, p);
+    sqk::k_pass<T, MAXT><<<grid, block, smem, s->stream>>>(a, p);
     SQ_CUDA(cudaGetLastError());
     return SQ_OK;
 }
@@ -419,6 +424,10 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     // tensor-core operands); FP64 (CUDA-core path, with a scratch copy of the
     // tile) at most 2^12
     if (ndense && (int)s->n > small_max(s)) K = std::max(needbits, 12);
+    // double-buffered staging holds two tiles: 2^12 amplitudes (FP32) or 2^11 (FP64)
+    // keep three CTAs per SM
+    const bool dbuf = s->staging == 2 && !ndense && (int)s->n > small_max(s);
+    if (dbuf) K = std::max(needbits, s->prec == SQ_F64 ? 11 : 12);
     if (K > n) K = n;
     if (K > tile_cap(s)) return fail(SQ_ERR_UNSUPPORTED, "gate touches too many qubits for one tile");
     if (ndense && s->prec == SQ_F64 && K > 12)
@@ -451,7 +460,8 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     // least 128 bytes (shorter runs cost more per copy than they save)
     {
         const uint64_t rb = ((uint64_t)1 << L) * s->esz;
-        a.stage = (s->staging && K < n && rb % 16 == 0 && rb >= 128) ? 1 : 0;
+        const bool ok = K < n && rb % 16 == 0 && rb >= 128;
+        a.stage = !ok ? 0 : (dbuf ? 2 : (s->staging ? 1 : 0));
     }
     int nhb = 0;
     for (int b = L; b < n; ++b)
@@ -609,7 +619,8 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     for (size_t i = i0; i < i1 && use_df; ++i)
         if (ops[i].kind == sqk::OP_W || ops[i].kind == sqk::OP_PLIST) use_df = false;
     if (use_df) a.stage = 0;  // the tile is converted on its way in and out
-    size_t smem = tile_smem(s, K, L);
+    if (ndense && a.stage == 2) a.stage = 1;
+    size_t smem = tile_smem(s, K, L) + (a.stage == 2 ? (size_t)2 * ((size_t)1 << K) * s->esz : 0);
     if (dcount) {
         // the dense work area: tensor-core operands (A chunk + B), or the scratch tile
         a.dense_off = (uint32_t)((smem + 127) & ~(size_t)127);
@@ -621,10 +632,13 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         a.dense = dev;
     }
     int occ = 0;
+    const bool big = block > 256;
     {
-        const int orc = use_df ? resident_ctas<sqk::df64>(s, block, smem, &occ)
-                               : (s->prec == SQ_F64 ? resident_ctas<double>(s, block, smem, &occ)
-                                                    : resident_ctas<float>(s, block, smem, &occ));
+        const int orc = use_df ? resident_ctas<sqk::df64, 256>(s, block, smem, &occ)
+                        : s->prec == SQ_F64 ? (big ? resident_ctas<double, 1024>(s, block, smem, &occ)
+                                                   : resident_ctas<double, 256>(s, block, smem, &occ))
+                                            : (big ? resident_ctas<float, 1024>(s, block, smem, &occ)
+                                                   : resident_ctas<float, 256>(s, block, smem, &occ));
         if (orc) return orc;
     }
     const uint64_t wave = occ > 0 ? (uint64_t)s->nsm * (uint64_t)occ : (uint64_t)s->max_grid;
@@ -643,9 +657,11 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         }
         SQ_CUDA(cudaEventRecord(e0, s->stream));
     }
-    int rc = use_df ? launch_pass_t<sqk::df64>(s, a, p, grid, block, smem)
-                    : ((s->prec == SQ_F64) ? launch_pass_t<double>(s, a, p, grid, block, smem)
-                                           : launch_pass_t<float>(s, a, p, grid, block, smem));
+    int rc = use_df ? launch_pass_t<sqk::df64, 256>(s, a, p, grid, block, smem)
+             : s->prec == SQ_F64 ? (big ? launch_pass_t<double, 1024>(s, a, p, grid, block, smem)
+                                        : launch_pass_t<double, 256>(s, a, p, grid, block, smem))
+                                 : (big ? launch_pass_t<float, 1024>(s, a, p, grid, block, smem)
+                                        : launch_pass_t<float, 256>(s, a, p, grid, block, smem));
     if (rc) return rc;
     if (dcount) {
         SQ_CUDA(cudaEventRecord(s->dense_ev[dslot_i], s->stream));
@@ -911,7 +927,8 @@ int sq_set_fusion(sq_state* s, int enabled) {
 
 int sq_set_staging(sq_state* s, int mode) {
     if (!s) return fail(SQ_ERR_ARG, "null state");
-    if (mode != 0 && mode != 1) return fail(SQ_ERR_ARG, "staging mode must be 0 (registers) or 1 (bulk copies)");
+    if (mode < 0 || mode > 2)
+        return fail(SQ_ERR_ARG, "staging mode must be 0 (registers), 1 (bulk copies) or 2 (bulk, double-buffered)");
     int rc = flush(s);
     s->staging = mode;
     return rc;

@@ -297,10 +297,11 @@ __device__ __forceinline__ void block_reduce2(double& a, double& b, double (*sh)
 namespace sqk {
 
 // T = double (FP64 state), float (FP32 state), or df64 (FP64 state, arithmetic in
-// double-float on the FP32 pipe; multi-tile passes of 256 threads).
+// double-float on the FP32 pipe; multi-tile passes only).  MAXT = 256 for
+// multi-tile passes (three CTAs per SM), 1024 for single-tile passes.
 template <typename T, int MAXT = 1024>
-__global__ void __launch_bounds__(MAXT) k_pass(const __grid_constant__ PassArgs a,
-                                               const __grid_constant__ Prog p) {
+__global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid_constant__ PassArgs a,
+                                                                   const __grid_constant__ Prog p) {
     typedef typename VecT<T>::type V;
     constexpr int W = VecT<T>::W;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -310,9 +311,13 @@ __global__ void __launch_bounds__(MAXT) k_pass(const __grid_constant__ PassArgs 
     const int K = a.K, L = a.L;
     const uint32_t TS = 1u << K;
     const uint32_t lowmask = (1u << L) - 1u;
-    T* sre = reinterpret_cast<T*>(smem_raw);
+    // one tile buffer (re block then im block), or two when the next tile is
+    // prefetched (staging mode 2); the run offsets follow the buffers
+    const int nbuf = (MAXT == 256 && a.stage == 2 && !kIsDf<T>) ? 2 : 1;
+    T* tiles = reinterpret_cast<T*>(smem_raw);
+    T* sre = tiles;
     T* sim = sre + TS;
-    uint64_t* offs = reinterpret_cast<uint64_t*>(sim + TS);
+    uint64_t* offs = reinterpret_cast<uint64_t*>(tiles + (size_t)nbuf * 2 * TS);
     const uint32_t nh = 1u << (K - L);
     for (uint32_t h = threadIdx.x; h < nh; h += blockDim.x) {
         uint64_t o = 0;
@@ -323,10 +328,12 @@ __global__ void __launch_bounds__(MAXT) k_pass(const __grid_constant__ PassArgs 
     // bulk staging: warp 0 issues one asynchronous copy per run of 2^L elements
     // (re and im) against an mbarrier, and writes tiles back the same way; the
     // host enables it only when a run is a multiple of 16 bytes
-    const bool bulk = a.stage != 0 && !kIsDf<T>;
+    // (single-tile passes, the 1024-thread instantiation, never stage in bulk)
+    const bool bulk = MAXT == 256 && a.stage != 0 && !kIsDf<T>;
     const uint32_t run_bytes = (1u << L) * (uint32_t)sizeof(T);
-    __shared__ __align__(8) uint64_t stage_bar;
-    uint32_t stage_phase = 0u;
+    __shared__ __align__(8) uint64_t stage_bar[2];
+    uint32_t stage_phase = 0u;  // bit b: parity of the next completion of stage_bar[b]
+    uint32_t stage_pend = 0u;   // bit b: a load into buffer b is in flight
     // dense ops: mbarriers, and on the tensor-core path a 64-column TMEM accumulator
     // held by warp 0 for the whole launch
     __shared__ __align__(16) DenseSmem dsm;
@@ -335,7 +342,10 @@ __global__ void __launch_bounds__(MAXT) k_pass(const __grid_constant__ PassArgs 
     int b_loaded = -1;
     unsigned char* dbuf = smem_raw + a.dense_off;
     if (threadIdx.x == 0) {
-        if (bulk) mbar_init(&stage_bar, 1u);
+        if (bulk) {
+            mbar_init(&stage_bar[0], 1u);
+            mbar_init(&stage_bar[1], 1u);
+        }
         if (dense_tc) {
             mbar_init(&dsm.bar_b, 1u);
             mbar_init(&dsm.bar_mma, 1u);
@@ -351,46 +361,68 @@ __global__ void __launch_bounds__(MAXT) k_pass(const __grid_constant__ PassArgs 
     T* gim = reinterpret_cast<T*>(a.im);
     double acc0 = 0.0, acc1 = 0.0;
 
-    for (uint64_t tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
-        uint64_t base = a.ofix;
-        {
-            uint64_t f = a.ofree, t = tile;
-            while (f) {
-                const uint64_t b = f & (~f + 1ull);
-                if (t & 1ull) base |= b;
-                t >>= 1;
-                f ^= b;
+    // tile index -> global index of its element 0, and whether any op of the
+    // pass touches it (uniform over the CTA)
+    auto tile_base = [&](uint64_t tile) {
+        uint64_t b = a.ofix, f = a.ofree, t = tile;
+        while (f) {
+            const uint64_t low = f & (~f + 1ull);
+            if (t & 1ull) b |= low;
+            t >>= 1;
+            f ^= low;
+        }
+        return b;
+    };
+    auto tile_active = [&](uint64_t b) {
+        bool any = p.red != 0 || p.xm != 0u;  // a frame permutes every tile
+        for (int k = 0; k < p.nops && !any; ++k) any = (b & p.ops[k].ocm) == p.ops[k].ocv;
+        return any;
+    };
+    // warp 0 issues the bulk copies of one tile into buffer bi; the buffer's
+    // previous bulk stores must have read it first
+    auto issue_load = [&](uint64_t b, int bi) {
+        if (threadIdx.x < 32) {
+            bulk_wait_read_all();
+            __syncwarp();
+            T* dre = tiles + (size_t)bi * 2 * TS;
+            T* dim = dre + TS;
+            if (threadIdx.x == 0) mbar_arrive_expect_tx(&stage_bar[bi], 2u * TS * (uint32_t)sizeof(T));
+            __syncwarp();
+            for (uint32_t h = threadIdx.x; h < nh; h += 32) {
+                const uint64_t g = b | offs[h];
+                bulk_load(dre + (h << L), gre + g, run_bytes, &stage_bar[bi]);
+                bulk_load(dim + (h << L), gim + g, run_bytes, &stage_bar[bi]);
             }
         }
-        bool any = p.red != 0 || p.xm != 0u;  // a frame permutes every tile
-        for (int k = 0; k < p.nops && !any; ++k)
-            any = (base & p.ops[k].ocm) == p.ops[k].ocv;
-        if (!any) continue;  // uniform over the CTA
+        stage_pend |= 1u << bi;
+    };
+
+    uint64_t tile = blockIdx.x, base = 0;
+    while (tile < a.ntiles && !tile_active(base = tile_base(tile))) tile += gridDim.x;
+    int buf = 0;
+    if (bulk && tile < a.ntiles) issue_load(base, 0);
+    while (tile < a.ntiles) {
+        uint64_t nxt = tile + gridDim.x, nbase = 0;
+        while (nxt < a.ntiles && !tile_active(nbase = tile_base(nxt))) nxt += gridDim.x;
+        sre = tiles + (size_t)buf * 2 * TS;
+        sim = sre + TS;
 
         // ---- load the tile (16-byte vectors, runs of 2^L contiguous elements)
         if (bulk) {
-            if (threadIdx.x < 32) {
-                bulk_wait_read_all();  // this lane's stores of the previous tile have read the buffer
-                __syncwarp();
-                if (threadIdx.x == 0) mbar_arrive_expect_tx(&stage_bar, 2u * TS * (uint32_t)sizeof(T));
-                __syncwarp();
-                for (uint32_t h = threadIdx.x; h < nh; h += 32) {
-                    const uint64_t g = base | offs[h];
-                    bulk_load(sre + (h << L), gre + g, run_bytes, &stage_bar);
-                    bulk_load(sim + (h << L), gim + g, run_bytes, &stage_bar);
-                }
-            }
-            const bool ok = mbar_wait_bounded(&stage_bar, stage_phase, a.err, kErrStageWait);
+            if (nbuf == 2 && nxt < a.ntiles) issue_load(nbase, buf ^ 1);  // prefetch the next tile
+            const bool ok = mbar_wait_bounded(&stage_bar[buf], (stage_phase >> buf) & 1u, a.err, kErrStageWait);
             if (__syncthreads_or(!ok)) {
-                // give the copies in flight a second bounded wait, then leave
-                mbar_wait_bounded(&stage_bar, stage_phase, nullptr, 0u);
+                // give every load in flight a second bounded wait, then leave
+                for (int bi = 0; bi < 2; ++bi)
+                    if ((stage_pend >> bi) & 1u) mbar_wait_bounded(&stage_bar[bi], (stage_phase >> bi) & 1u, nullptr, 0u);
                 if (threadIdx.x < 32) {
                     bulk_wait_all();
                     if (dense_tc) tmem_dealloc(dsm.tmem, kDenseTmemCols);
                 }
                 return;
             }
-            stage_phase ^= 1u;
+            stage_phase ^= 1u << buf;
+            stage_pend &= ~(1u << buf);
         } else if (kIsDf<T>) {  // doubles in HBM, double-float pairs in the tile
             const double* dre = reinterpret_cast<const double*>(a.re);
             const double* dim = reinterpret_cast<const double*>(a.im);
@@ -709,8 +741,12 @@ __global__ void __launch_bounds__(MAXT) k_pass(const __grid_constant__ PassArgs 
                 }
             }
         }
-        if (bulk) fence_proxy_async_smem();  // before the next tile's copies overwrite the buffer
+        if (bulk) fence_proxy_async_smem();  // before later copies overwrite the buffer
         __syncthreads();
+        if (bulk && nbuf == 1 && nxt < a.ntiles) issue_load(nbase, 0);
+        tile = nxt;
+        base = nbase;
+        if (nbuf == 2) buf ^= 1;
     }
     if (bulk && threadIdx.x < 32) bulk_wait_all();  // stores complete before the CTA leaves
     if (dense_tc) {

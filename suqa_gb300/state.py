@@ -122,8 +122,8 @@ class State:
         check(self.L.sq_set_dense_engine(self.h, engine))
 
     def set_staging(self, mode: int):
-        """Tile staging of multi-tile passes: 1 bulk asynchronous copies (default),
-        0 vector loads and stores through registers."""
+        """Tile staging of multi-tile passes: 0 vector loads and stores through
+        registers, 1 bulk asynchronous copies, 2 bulk copies double-buffered."""
         check(self.L.sq_set_staging(self.h, mode))
 
     def get_state(self) -> np.ndarray:

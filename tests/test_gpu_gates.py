@@ -189,14 +189,15 @@ def test_tile_size_does_not_change_results(precision):
 def test_bulk_staging_is_bit_identical_to_register_staging(precision, n, k):
     """Multi-tile passes move tiles by bulk asynchronous copies (runs of 2^L
     amplitudes, completion on an mbarrier) or through registers; the arithmetic
-    is the same, so the measured bits and every amplitude must be identical.
+    is the same, so the measured bits and every amplitude must be identical
+    (modes 0 and 1).
     The circuits hold X gates on low and high qubits (index frames with and
     without a part below L), controlled gates and measurements."""
     from suqa_gb300 import State
     from suqa_gb300.workloads import apply_circuit, random_circuit
     gates = random_circuit(n, 160, seed=40 + n, measure_every=40)
     results = []
-    for mode in (0, 1):
+    for mode in (0, 1, 2):
         with State(n, precision) as st:
             st.set_tile_qubits(k)
             st.set_staging(mode)
@@ -206,6 +207,11 @@ def test_bulk_staging_is_bit_identical_to_register_staging(precision, n, k):
             results.append((bits, st.get_state()))
     assert results[0][0] == results[1][0]
     assert np.array_equal(results[0][1], results[1][1])
+    # double-buffered staging uses its own tile size (2^12 FP32, 2^11 FP64): the same
+    # results to rounding
+    tol = 1e-12 if precision == "f64" else 2e-5
+    assert results[2][0] == results[0][0]
+    assert np.max(np.abs(results[2][1] - results[0][1])) <= tol * np.max(np.abs(results[0][1]))
 
 
 def test_fp64_fma_rate_probe_reports_a_rate():

@@ -81,7 +81,7 @@ int sq_set_fusion(sq_state* s, int enabled);
 int sq_set_tile_qubits(sq_state* s, int k);
 /* How multi-tile passes move tiles between HBM and shared memory (no
  * counterpart in the reference; a tuning knob, results are identical):
- * 0 = 16-byte vector loads and stores through registers; 1 = bulk asynchronous
+ * 0 (default) = 16-byte vector loads and stores through registers; 1 = bulk asynchronous
  * copies (cp.async.bulk on the TMA engine), one per run of contiguous
  * amplitudes, completion on an mbarrier whose waits are bounded (a pass that
  * gives up sets an error word that the next synchronising call reports as

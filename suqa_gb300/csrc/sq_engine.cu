@@ -77,7 +77,7 @@ struct sq_state {
     // renormalisations of measurement and vnormalize; it is applied to memory
     // (one fused scale) before any read-out and when it drifts far from 1.
     double gscale = 1.0;
-    int staging = 1;                // multi-tile passes move tiles by bulk asynchronous copies
+    int staging = 0;                // multi-tile passes: 0 registers, 1 bulk copies, 2 double-buffered bulk
     // dense blocks: automatic fusion threshold (0 = off), engine (0 tensor cores
     // where possible, 1 CUDA cores), and the per-launch operand ring
     // FP64 states: multi-tile passes of gates without tables or dense blocks run
@@ -728,7 +728,10 @@ int flush(sq_state* s, int red = 0, uint64_t rmask = 0, uint64_t rval = 0) {
             if (h.kind == sqk::OP_DENSE && nd == kMaxDensePerPass) break;
             const uint64_t nn = need | h.flip;
             const int bits = popc(nn | 3ull);
-            const bool fits_tile = ((int)s->n <= small_max(s)) ? true : (bits <= s->kp || (j == i && bits <= kcap));
+            // passes with dense blocks keep to tiles of 2^12 amplitudes (two CTAs per SM
+            // with the tensor-core operands)
+            const int cap = (nd > 0 || h.kind == sqk::OP_DENSE) ? std::min(s->kp, 12) : s->kp;
+            const bool fits_tile = ((int)s->n <= small_max(s)) ? true : (bits <= cap || (j == i && bits <= kcap));
             if (j > i && (!s->fusion || !fits_tile)) break;
             if (j == i && !fits_tile) return fail(SQ_ERR_UNSUPPORTED, "gate touches too many qubits for one tile");
             if ((int)(j - i) >= sqk::kMaxOps) break;

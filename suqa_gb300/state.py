@@ -123,7 +123,8 @@ class State:
 
     def set_staging(self, mode: int):
         """Tile staging of multi-tile passes: 0 vector loads and stores through
-        registers, 1 bulk asynchronous copies, 2 bulk copies double-buffered."""
+        registers (default), 1 bulk asynchronous copies, 2 bulk copies
+        double-buffered."""
         check(self.L.sq_set_staging(self.h, mode))
 
     def get_state(self) -> np.ndarray:

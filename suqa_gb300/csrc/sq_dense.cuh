@@ -241,8 +241,8 @@ __device__ void dense_cc(T* tile, uint32_t TS, const Op& op, const double* U, T*
             const uint32_t ti = cb | ds.kdep[i];
             const double xr = (double)tile[ti], xi = (double)tile[TS + ti];
             const double ur = row[2 * i], ui = row[2 * i + 1];
-            yr = fma(ur, xr, fma(-ui, xi, yr));
-            yi = fma(ur, xi, fma(ui, xr, yi));
+            yr = __fma_rn(ur, xr, __fma_rn(-ui, xi, yr));
+            yi = __fma_rn(ur, xi, __fma_rn(ui, xr, yi));
         }
         scratch[t] = (T)yr;
         scratch[TS + t] = (T)yi;

@@ -205,8 +205,7 @@ SQ_HD df64 operator+(df64 a, df64 b) { return df_add(a, b); }
 SQ_HD df64 operator-(df64 a, df64 b) { return df_sub(a, b); }
 SQ_HD df64 operator-(df64 a) { return df_neg(a); }
 SQ_HD df64 operator*(df64 a, df64 b) { return df_mul(a, b); }
-SQ_HD df64 fma(df64 a, df64 b, df64 c) { return df_fmadd(a, b, c); }
-using ::fma;  // keep the double and float overloads visible beside the df64 one in this namespace
+
 
 // a df64 constant from a double computed on the host (exact split, no flush)
 inline df64 df_const_host(double d) {

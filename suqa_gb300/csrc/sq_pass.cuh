@@ -173,6 +173,14 @@ template <> struct VecT<df64>   { typedef double2 type; static constexpr int W =
 
 template <typename T> constexpr bool kIsDf = std::is_same<T, df64>::value;
 
+// a * b + c in the kernel's element type, with the precision spelled out: a
+// float fused multiply-add stays on the FP32 pipe
+template <typename T> __device__ __forceinline__ T tfma(T a, T b, T c) {
+    if constexpr (kIsDf<T>) return df_fmadd(a, b, c);
+    else if constexpr (sizeof(T) == 4) return __fmaf_rn(a, b, c);
+    else return __fma_rn(a, b, c);
+}
+
 // a double as the kernel's element type (the df64 split uses integer operations)
 template <typename T> __device__ __forceinline__ T tconv(double d) {
     if constexpr (kIsDf<T>) return df_from_double(d);
@@ -234,18 +242,18 @@ __device__ __forceinline__ void rot_deferred(T ar, T ai, T br, T bi, int k, T up
     const T xi = (k & 1) ? br : bi;
     const bool nr = (k == 1 || k == 2), ni = (k >= 2);
     if (cbig) {
-        outr = fma(xr, nr ? un : up, ar);
-        outi = fma(xi, ni ? un : up, ai);
+        outr = tfma<T>(xr, nr ? un : up, ar);
+        outi = tfma<T>(xi, ni ? un : up, ai);
     } else {
-        outr = fma(ar, up, neg_if(xr, nr));
-        outi = fma(ai, up, neg_if(xi, ni));
+        outr = tfma<T>(ar, up, neg_if(xr, nr));
+        outi = tfma<T>(ai, up, neg_if(xi, ni));
     }
 }
 
 // part + |a|^2 (FP64 accumulation; FP32 amplitudes square in FP32)
-__device__ __forceinline__ double add_sq(double part, double r, double i) { return fma(r, r, fma(i, i, part)); }
+__device__ __forceinline__ double add_sq(double part, double r, double i) { return __fma_rn(r, r, __fma_rn(i, i, part)); }
 __device__ __forceinline__ double add_sq(double part, float r, float i) { return part + (double)fmaf(r, r, i * i); }
-__device__ __forceinline__ double add_sq(double part, df64 r, df64 i) { return part + df_to_double(fma(r, r, i * i)); }
+__device__ __forceinline__ double add_sq(double part, df64 r, df64 i) { return part + df_to_double(df_fmadd(r, r, i * i)); }
 
 __device__ __forceinline__ void scale_vec(double2& v, double s) { v.x *= s; v.y *= s; }
 

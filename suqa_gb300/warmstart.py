@@ -140,35 +140,105 @@ def training_set(chains, runs, burn_in):
     return np.array(xs), np.array(ts), np.array(ms)
 
 
+def scan_targets(points, ene_qbits, thetas, warm_chains, warm_steps, cold_chains, cold_steps, precision="f32",
+                 seed=7):
+    """Warm-start targets from plain chains by an angle scan.  For every
+    parameter point (spins, J, h, beta): cold-started chains give the long-run
+    mean energy (the mean over the second half of cold_steps), and chains started
+    from RY(theta) on every spin, for each theta of the grid, give their mean
+    energy over their first warm_steps steps; the target angle is where that
+    early mean meets the cold long-run mean (linear interpolation between grid
+    angles where the difference changes sign, else the closest grid angle).
+    Every chain is a plain QMS chain (the Metropolis steps are untouched), so the
+    targets come from chains the plain method generates.  Returns (x, t, mask,
+    details)."""
+    from .batch import TfimChain, run_tfim_batch
+    chains = []
+    for pi, (sp, J, h, beta) in enumerate(points):
+        base = dict(spins=sp, ene_qbits=ene_qbits, beta=beta, h=h, J=J, thermalization=0)
+        chains += [TfimChain(steps=cold_steps, seed=seed * 1_000_000 + 10_000 * pi + k, **base)
+                   for k in range(cold_chains)]
+        for ti, th in enumerate(thetas):
+            chains += [TfimChain(steps=warm_steps, seed=seed * 1_000_000 + 10_000 * pi + 1000 * (ti + 1) + k,
+                                 warm_angles=[float(th)] * sp, **base) for k in range(warm_chains)]
+    runs, ms = run_tfim_batch(chains, precision)
+    xs, ts, mk, det = [], [], [], []
+    o = 0
+    for sp, J, h, beta in points:
+        cold = runs[o:o + cold_chains]
+        o += cold_chains
+        late = np.concatenate([r.E[r.step >= cold_steps // 2] for r in cold])
+        target_E = float(np.mean(late))
+        early = []
+        for _ in thetas:
+            rr = runs[o:o + warm_chains]
+            o += warm_chains
+            early.append(float(np.mean(np.concatenate([r.E[r.step >= 1] for r in rr]))))
+        d = np.array(early) - target_E
+        th = float(thetas[int(np.argmin(np.abs(d)))])
+        for i in range(len(thetas) - 1):  # first sign change along the grid
+            if d[i] == 0.0 or d[i] * d[i + 1] < 0.0:
+                f = d[i] / (d[i] - d[i + 1]) if d[i] != d[i + 1] else 0.0
+                th = float(thetas[i] + f * (thetas[i + 1] - thetas[i]))
+                break
+        xs.append(features(sp, J, h, beta))
+        t = np.zeros(MAX_SPINS, np.float32)
+        m = np.zeros(MAX_SPINS, np.float32)
+        t[:sp] = th
+        m[:sp] = 1.0
+        ts.append(t)
+        mk.append(m)
+        det.append({"spins": sp, "J": J, "h": h, "beta": beta, "cold_long_run_E": target_E,
+                    "warm_early_E": [round(v, 3) for v in early], "target_angle": th,
+                    "cold_samples": int(late.size)})
+    info = {"chains": len(chains), "chain_steps": cold_chains * cold_steps * len(points) +
+            warm_chains * warm_steps * len(points) * len(thetas), "device_ms": ms, "points": det}
+    return np.array(xs), np.array(ts), np.array(mk), info
+
+
 def burn_in_experiment(spins=(4, 5, 6), ene_qbits=4, train_chains=512, train_steps=12, train_burn=6,
                        eval_groups=((6, 1.0, 0.3), (6, 1.0, 1.0), (6, 0.7, 1.8)), eval_chains=96, eval_steps=8,
-                       precision="f32", iters=1500, seed=7, eval_ene_qbits=None):
-    """Trains the network on plain cold-start chains and compares warm- and
-    cold-started chains of held-out parameter sets.  Returns a dict with, per
-    group, the equilibrium energy (cold chains after burn-in), the mean energy
-    error of the first samples for cold and warm starts, and the number of steps
-    each start needs before its step-averaged energy stays within two standard
-    errors of equilibrium.  The training chains use ene_qbits energy qubits, the
-    evaluation chains eval_ene_qbits (default: the same)."""
+                       precision="f32", iters=1500, seed=7, eval_ene_qbits=None, target="energy", scan=None):
+    """Trains the network on plain chains and compares warm- and cold-started
+    chains of held-out parameter sets.  Returns a dict with, per group, the
+    equilibrium energy (cold chains after burn-in), the mean energy error of the
+    first samples for cold and warm starts, and the number of steps each start
+    needs before its step-averaged energy stays within two standard errors of
+    equilibrium.
+
+    target = "energy": the training angle of a parameter set is the product
+    state with the cold chains' mean energy (training_set); the chains use
+    ene_qbits energy qubits, the evaluation chains eval_ene_qbits (default: the
+    same).  target = "scan": the angles come from scan_targets(**scan) (chains of
+    the evaluation width started at a grid of angles), the angle whose plain
+    chains reach the cold chains' long-run energy first."""
     from .batch import TfimChain, run_tfim_batch
     ee = ene_qbits if eval_ene_qbits is None else eval_ene_qbits
     rng = np.random.default_rng(seed)
-    chains = [TfimChain(spins=int(rng.choice(spins)), ene_qbits=ene_qbits, steps=train_steps,
-                        beta=float(rng.uniform(0.2, 2.0)), h=float(rng.uniform(0.5, 1.5)), thermalization=0,
-                        seed=10_000 + i) for i in range(train_chains)]
-    runs, ms_data = run_tfim_batch(chains, precision)
-    x, t, m = training_set(chains, runs, train_burn)
+    if target == "scan":
+        t0 = time.perf_counter()
+        x, t, m, sinfo = scan_targets(precision=precision, seed=seed, **scan)
+        data = {"target": "angle scan", "scan": sinfo, "scan_s": time.perf_counter() - t0,
+                "train_rows": int(x.shape[0]), "train_qubits": [scan["points"][0][0] + scan["ene_qbits"] + 1]}
+    else:
+        chains = [TfimChain(spins=int(rng.choice(spins)), ene_qbits=ene_qbits, steps=train_steps,
+                            beta=float(rng.uniform(0.2, 2.0)), h=float(rng.uniform(0.5, 1.5)), thermalization=0,
+                            seed=10_000 + i) for i in range(train_chains)]
+        runs, ms_data = run_tfim_batch(chains, precision)
+        x, t, m = training_set(chains, runs, train_burn)
+        data = {"target": "product-state energy", "train_chains": train_chains,
+                "train_qubits": sorted({c.nqubits for c in chains}),
+                "train_samples": int(sum(int(np.sum(r.step >= train_burn)) for r in runs)),
+                "train_rows": int(x.shape[0]), "data_device_ms": ms_data,
+                "data_chain_steps_per_s": train_chains * train_steps / (ms_data / 1e3)}
     net = WarmStartNet(seed=seed)
     t0 = time.perf_counter()
     losses = net.fit(x, t, m, iters=iters, batch=256, lr=2e-3, seed=seed)
     fit_s = time.perf_counter() - t0
-    out = {"train_chains": train_chains, "train_qubits": sorted({c.nqubits for c in chains}),
-           "train_samples": int(sum(int(np.sum(r.step >= train_burn)) for r in runs)),
-           "train_rows": int(x.shape[0]), "data_device_ms": ms_data,
-           "data_chain_steps_per_s": train_chains * train_steps / (ms_data / 1e3),
-           "fit_iters": iters, "fit_s": fit_s,
-           "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-20:])),
-           "eval_chains_per_group": eval_chains, "eval_qubits": None, "groups": []}
+    out = dict(data)
+    out.update({"fit_iters": iters, "fit_s": fit_s,
+                "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-20:])),
+                "eval_chains_per_group": eval_chains, "eval_qubits": None, "groups": []})
     # every group's cold and warm chains run as one batch (better load balance)
     allc, angs = [], []
     for gi, (s, h, beta) in enumerate(eval_groups):
@@ -248,12 +318,35 @@ FULL_STUDY = dict(spins=(12,), ene_qbits=4, train_chains=1024, train_steps=60, t
                   eval_groups=((12, 1.0, 1.0), (12, 0.8, 1.9)),
                   eval_chains=48, eval_steps=100, eval_ene_qbits=6, iters=2000)
 
+# A small angle-scan study (6-spin rings, 4 energy qubits: 11 qubits), seconds
+# on one GPU: the configuration of the test suite.
+SMALL_SCAN_STUDY = dict(ene_qbits=4, eval_groups=((6, 0.8, 0.9), (6, 1.2, 1.6)), eval_chains=64, eval_steps=30,
+                        iters=1500, target="scan",
+                        scan=dict(points=[(6, 1.0, h, b) for h in (0.6, 1.0, 1.4) for b in (0.5, 1.2, 1.9)],
+                                  ene_qbits=4, thetas=tuple(float(v) for v in np.linspace(-1.2, 0.0, 7)),
+                                  warm_chains=16, warm_steps=8, cold_chains=32, cold_steps=30))
+
+# The same evaluation with angle-scan targets: 12 parameter points of 12-spin
+# rings (h in {0.6, 1.0, 1.4} x beta in {0.4, 0.9, 1.4, 1.9}) with the evaluation
+# width (6 energy qubits, 19 qubits): 32 cold chains x 60 steps per point and 8
+# chains x 12 steps per grid angle; the evaluation groups are off the grid.
+SCAN_ANGLES = tuple(float(v) for v in np.linspace(-1.2, 0.0, 9))
+FULL_SCAN_STUDY = dict(ene_qbits=6, eval_groups=((12, 0.8, 1.15), (12, 1.2, 1.65)), eval_chains=48,
+                       eval_steps=100, eval_ene_qbits=6, iters=2000, target="scan",
+                       scan=dict(points=[(12, 1.0, h, b) for h in (0.6, 1.0, 1.4) for b in (0.4, 0.9, 1.4, 1.9)],
+                                 ene_qbits=6, thetas=SCAN_ANGLES, warm_chains=8, warm_steps=12, cold_chains=32,
+                                 cold_steps=60))
+
 
 if __name__ == "__main__":
     import argparse
     import json
     ap = argparse.ArgumentParser(description="learned warm-start burn-in study")
     ap.add_argument("--full", action="store_true", help="the full-size study (several GPU minutes)")
+    ap.add_argument("--scan", action="store_true", help="angle-scan targets (with --full: FULL_SCAN_STUDY)")
     a = ap.parse_args()
-    res = burn_in_experiment(**FULL_STUDY) if a.full else burn_in_experiment()
+    if a.scan:
+        res = burn_in_experiment(**FULL_SCAN_STUDY) if a.full else burn_in_experiment(**SMALL_SCAN_STUDY)
+    else:
+        res = burn_in_experiment(**FULL_STUDY) if a.full else burn_in_experiment()
     print(json.dumps(res))

@@ -40,9 +40,11 @@ def test_training_reduces_loss():
     assert np.mean(losses[-20:]) < 0.1 * np.mean(losses[:20])
 
 
-def test_warm_start_shortens_burn_in():
-    """Chains started from the trained network's product state are closer to the
-    equilibrium energy in their first steps than cold-started chains."""
+def test_energy_target_warm_start_lowers_first_sample_error():
+    """With product-state energy targets, chains started from the trained
+    network's product state are closer to the equilibrium energy in their first
+    steps than cold-started chains (their later burn-in is not shorter: these
+    chains keep memory of their start)."""
     from suqa_gb300.warmstart import burn_in_experiment
     res = burn_in_experiment()
     print(res)
@@ -50,3 +52,19 @@ def test_warm_start_shortens_burn_in():
     cold = np.mean([g["cold_first_err"] for g in res["groups"]])
     warm = np.mean([g["warm_first_err"] for g in res["groups"]])
     assert warm < cold, (warm, cold)
+
+
+def test_scan_target_warm_start_shortens_burn_in():
+    """With angle-scan targets (the angle whose plain chains reach the cold
+    chains' long-run energy first, learned over a grid of (h, beta)), warm chains
+    of held-out parameter sets reach the cold chains' long-run band in fewer
+    steps than cold chains, and their energy excess over the first steps is
+    smaller."""
+    from suqa_gb300.warmstart import SMALL_SCAN_STUDY, burn_in_experiment
+    res = burn_in_experiment(**SMALL_SCAN_STUDY)
+    print({k: v for k, v in res.items() if k != "scan"})
+    assert res["loss_last"] < res["loss_first"]
+    for g in res["groups"]:
+        assert g["warm_burn_in_steps"] <= g["cold_burn_in_steps"], g
+    assert sum(g["warm_burn_in_steps"] for g in res["groups"]) < sum(g["cold_burn_in_steps"] for g in res["groups"])
+    assert sum(g["warm_excess_first10"] for g in res["groups"]) < sum(g["cold_excess_first10"] for g in res["groups"])

@@ -324,6 +324,11 @@ typedef struct sq_qsa_walk_result {
     double E, absM;    /* energy and |magnetisation| of the readout */
     double last_p0;    /* probability of the zero walk phase at the last step */
 } sq_qsa_walk_result;
+/* FP32 walks by orbit classes: the class-sorted orbit pass with 16 warps per
+ * CTA (default, where the batch's classes fit its shared memory) or the 8-warp
+ * pass (per-warp class sums).  Process-wide; results agree to FP32 rounding (the
+ * class sums are added in different orders).  No counterpart in the reference. */
+int sq_set_walk_orbit_warps(int warps);
 int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int precision, sq_qsa_walk_result* results,
                       double* p0_trace, float* kernel_ms);
 

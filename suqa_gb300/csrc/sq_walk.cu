@@ -33,6 +33,7 @@
 // k_walk_step_sorted (FP32) or k_walk_step_cls and k_walk_measure per step.
 // k_walk_readout reads the spins of every completed walk.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -1272,6 +1273,242 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
     }
 }
 
+// The same orbit pass with 16 warps per CTA (one CTA per SM, twice the warps of
+// k_walk_step_sorted): chunks of 512 orbits, the class sums in one CTA-level slot
+// array instead of one per warp, and the sorted amplitudes overwritten in place by
+// S.  A warp's sorted range holds whole runs of the classes strictly inside it, so
+// it adds those classes' sums directly; the classes at the two ends of its range
+// may continue in the neighbouring warps, so their partial sums go to a per-warp
+// edge buffer that is added in warp order after the chunk (the sums stay
+// deterministic).  Rows of 16 floats (the in-place S needs the row's 16 slots).
+// process-wide choice of the FP32 class-sorted orbit pass (sq_set_walk_orbit_warps)
+std::atomic<int> g_orbit_warps{16};
+
+constexpr int kS2Threads = 512;
+constexpr int kS2Warps = kS2Threads / 32;
+constexpr int kS2Chunk = kS2Threads;
+constexpr int kS2Row = 16;
+
+__global__ void __launch_bounds__(kS2Threads, 1) k_walk_step_sorted2(
+    const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk, const WalkRec* __restrict__ recs,
+    const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ ncls, const float* __restrict__ cls,
+    const uint32_t* __restrict__ gid, float* __restrict__ states, double* __restrict__ npart, int nslot) {
+    const int w = cta_walk[blockIdx.x];
+    const WalkDev& W = walks[w];
+    const WalkRec& R = recs[w];
+    if (R.status != 0) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nk = 2 * nslot;
+    float* cls_s = reinterpret_cast<float*>(smem_raw);               // [nslot][512]: V^T rows, then Q rows
+    float* slots = cls_s + nslot * 512;                               // [nslot][16] class sums of the CTA
+    float* edge = slots + nslot * 16;                                 // [warps][2][16] end-of-range partial sums
+    float* vbuf = edge + kS2Warps * 2 * 16;                           // [kS2Chunk][16] amplitudes, then S
+    unsigned long long* htab = reinterpret_cast<unsigned long long*>(vbuf + kS2Chunk * kS2Row);  // [kHash]
+    unsigned long long* sent = htab + kHash;                          // [kMaxCls] class data entries
+    int* wcnt = reinterpret_cast<int*>(sent + kMaxCls);               // [warps][nk]
+    int* kstart = wcnt + kS2Warps * nk;                               // [nk]
+    int* kend = kstart + nk;                                          // [nk]
+    int* wsum = kend + nk;                                            // [warps]
+    int* ecls = wsum + kS2Warps;                                      // [warps][2] class of each edge sum (-1: none)
+    int* nact_s = ecls + 2 * kS2Warps;
+    unsigned char* csort = reinterpret_cast<unsigned char*>(nact_s + 4);  // [kS2Chunk]
+    const int s = W.s, C = (int)R.C;
+    const uint32_t nc = ncls[(uint64_t)w * kMaxMoves + C];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < nslot * 16; i += kS2Threads) slots[i] = 0.f;
+    for (int i = threadIdx.x; i < kHash; i += kS2Threads) htab[i] = 0ull;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < nc; i += kS2Threads) {
+        const unsigned long long key = keys[((uint64_t)w * kMaxMoves + C) * kMaxCls + i];
+        uint32_t h = cls_hash(key);
+        for (int probe = 0; probe < kHash; ++probe) {  // distinct keys, nc <= 96 < kHash: always placed
+            if (atomicCAS(&htab[h], 0ull, (key << 8) | (unsigned long long)i) == 0ull) break;
+            h = (h + 1u) & (kHash - 1);
+        }
+    }
+    for (uint32_t i = threadIdx.x; i < max(nc, 1u); i += kS2Threads) sent[i] = cls_entry(W, R, gid, w, i);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < nc * 128u; i += kS2Threads) {
+        const uint32_t c = i >> 7, e = (i & 127u) * 4u;
+        *reinterpret_cast<float4*>(cls_s + c * 512 + e) = __ldg(reinterpret_cast<const float4*>(cls + sent[c] * kClsStride + e));
+    }
+    const uint32_t norb = norbits(s), eC = 1u << C;
+    const uint32_t mc = eC << s, macc = 1u << (2 * s);
+    RingBonds bonds;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) bonds.plane[k] = W.jplane[k];
+    bonds.np = W.jnp;
+    bonds.off = W.joff;
+    bonds.s = s;
+    bonds.smask = (1u << s) - 1u;
+    const int kslot = threadIdx.x;
+    float* st = states + W.state_off;
+    const bool fresh = R.fresh != 0;
+    const float scale = (float)R.scale;
+    const float init = (float)(1.0 / sqrt((double)(1u << s)));
+    const uint32_t first = (blockIdx.x - W.cta0) * (uint32_t)kClsOrbitsPerCta;
+    constexpr int kChunks = kClsOrbitsPerCta / kS2Chunk;
+    const int row = lane & 15, part = lane >> 4;
+
+    SortedLoad ld;
+    sorted_issue(first + threadIdx.x, norb, s, C, eC, bonds, st, ld);
+    for (int k = 0; k < kChunks; ++k) {
+        const uint32_t cbase = first + (uint32_t)(k * kS2Chunk);
+        if (cbase >= norb) break;  // uniform over the CTA
+        float vn[16];
+        const int ci = sorted_finish(ld, htab, fresh, scale, init, vn);
+        const bool single = ld.single;
+        const uint32_t b0 = ld.b0, dp = ld.dp;
+        const int q = ci >= 0 ? 2 * ci + (single ? 1 : 0) : -1;
+        for (int c = lane; c < nk; c += 32) wcnt[warp * nk + c] = 0;
+        __syncwarp();
+        const unsigned grp = __match_any_sync(0xffffffffu, q);
+        const int rank = __popc(grp & ((1u << lane) - 1u));
+        if (q >= 0 && rank == 0) wcnt[warp * nk + q] = __popc(grp);
+        __syncthreads();
+        int tot = 0;
+        if (kslot < nk) {
+            for (int wp = 0; wp < kS2Warps; ++wp) {
+                const int t = wcnt[wp * nk + kslot];
+                wcnt[wp * nk + kslot] = tot;
+                tot += t;
+            }
+        }
+        int incl = tot;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += y;
+        }
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        if (kslot < nk) {
+            int base = incl - tot;
+            for (int wp = 0; wp < warp; ++wp) base += wsum[wp];
+            kstart[kslot] = base;
+            kend[kslot] = base + tot;
+        }
+        if (threadIdx.x == 0) {
+            int n = 0;
+            for (int wp = 0; wp < kS2Warps; ++wp) n += wsum[wp];
+            *nact_s = n;
+        }
+        __syncthreads();
+        int pos = -1;
+        if (q >= 0) {
+            pos = kstart[q] + wcnt[warp * nk + q] + rank;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                *reinterpret_cast<float4*>(vbuf + pos * kS2Row + 4 * u) =
+                    make_float4(vn[4 * u], vn[4 * u + 1], vn[4 * u + 2], vn[4 * u + 3]);
+            csort[pos] = (unsigned char)q;
+        }
+        __syncthreads();
+        if (k + 1 < kChunks)  // the next chunk's loads overlap this chunk's products
+            sorted_issue(cbase + kS2Chunk + threadIdx.x, norb, s, C, eC, bonds, st, ld);
+        {
+            const int nact = *nact_s;
+            const int p1 = nact * (warp + 1) / kS2Warps;
+            int p = nact * warp / kS2Warps;
+            // the classes at the two ends of this warp's range
+            const int cfirst = p < p1 ? (int)(csort[p] >> 1) : -1;
+            const int clast = p < p1 ? (int)(csort[p1 - 1] >> 1) : -1;
+            if (lane < 2) ecls[warp * 2 + lane] = lane == 0 ? cfirst : (clast != cfirst ? clast : -1);
+            int cur = -1;
+            float nacc = 0.f;
+            f2 r[8];
+#pragma unroll
+            for (int m = 0; m < 8; ++m) r[m] = 0ull;
+            auto close_class = [&](int c) {
+                if (c < 0 || part != 0) return;
+                if (c == cfirst) edge[(warp * 2) * 16 + row] = nacc;
+                else if (c == clast) edge[(warp * 2 + 1) * 16 + row] = nacc;
+                else slots[c * 16 + row] += nacc;  // only this warp holds class c in this chunk
+            };
+            while (p < p1) {  // one run (one key) per iteration; uniform over the warp
+                const int qq = csort[p];
+                const int e = max(min(kend[qq], p1), p + 1);
+                const float wt = (qq & 1) ? 0.5f : 1.f;
+                if ((qq >> 1) != cur) {
+                    close_class(cur);
+                    nacc = 0.f;
+                    cur = qq >> 1;
+                    const ulonglong2* rp = reinterpret_cast<const ulonglong2*>(cls_s + cur * 512 + lane * 16);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const ulonglong2 t = rp[u];
+                        r[2 * u] = t.x;
+                        r[2 * u + 1] = t.y;
+                    }
+                }
+                for (; p + 4 <= e; p += 4) {
+                    f2 v0[8], v1[8], v2[8], v3[8];
+                    sorted_row(vbuf + p * kS2Row, v0);
+                    sorted_row(vbuf + (p + 1) * kS2Row, v1);
+                    sorted_row(vbuf + (p + 2) * kS2Row, v2);
+                    sorted_row(vbuf + (p + 3) * kS2Row, v3);
+                    const float y0 = sorted_dot(r, v0), y1 = sorted_dot(r, v1);
+                    const float y2 = sorted_dot(r, v2), y3 = sorted_dot(r, v3);
+                    __syncwarp();  // every lane has read these rows before S overwrites them
+                    if (part == 0) {
+                        nacc += wt * y0 * y0;
+                        nacc += wt * y1 * y1;
+                        nacc += wt * y2 * y2;
+                        nacc += wt * y3 * y3;
+                    } else {
+                        vbuf[p * kS2Row + row] = y0;
+                        vbuf[(p + 1) * kS2Row + row] = y1;
+                        vbuf[(p + 2) * kS2Row + row] = y2;
+                        vbuf[(p + 3) * kS2Row + row] = y3;
+                    }
+                    __syncwarp();
+                }
+                for (; p < e; ++p) {
+                    f2 v0[8];
+                    sorted_row(vbuf + p * kS2Row, v0);
+                    const float y0 = sorted_dot(r, v0);
+                    __syncwarp();
+                    if (part == 0) nacc += wt * y0 * y0;
+                    else vbuf[p * kS2Row + row] = y0;
+                    __syncwarp();
+                }
+            }
+            close_class(cur);
+        }
+        __syncthreads();
+        // the end-of-range sums, warp by warp (a fixed order)
+        if (threadIdx.x < 16) {
+            for (int wp = 0; wp < kS2Warps; ++wp)
+                for (int e2 = 0; e2 < 2; ++e2) {
+                    const int c = ecls[wp * 2 + e2];
+                    if (c >= 0) slots[c * 16 + threadIdx.x] += edge[(wp * 2 + e2) * 16 + threadIdx.x];
+                }
+        }
+        if (q >= 0) {
+            float S[16];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float4 t = *reinterpret_cast<const float4*>(vbuf + pos * kS2Row + 4 * u);
+                S[4 * u] = t.x;
+                S[4 * u + 1] = t.y;
+                S[4 * u + 2] = t.z;
+                S[4 * u + 3] = t.w;
+            }
+#pragma unroll
+            for (int pp = 0; pp < 8; ++pp) {
+                const int a = pp >> 2, b = (pp >> 1) & 1, c = pp & 1;
+                if (single && a == 1) continue;
+                const uint32_t i0 = b0 ^ (a ? dp : 0u) ^ (b ? eC : 0u) ^ (c ? mc : 0u);
+                st[i0] = S[SLOT(a, b, c, 0)];
+                st[i0 ^ macc] = S[SLOT(a, b, c, 1)];
+            }
+        }
+        __syncthreads();  // S read back and edges added before the next chunk reuses the buffers
+    }
+    __syncthreads();
+    for (uint32_t e = threadIdx.x; e < nc * 16u; e += blockDim.x) npart[(uint64_t)blockIdx.x * kMaxCls * 16 + e] = (double)slots[e];
+}
+
 // g_k of a walk from its class sums (algo 1): g_k = sum_{c,i} N_{c,i} d_{c,k,i}.
 template <typename T>
 __device__ void cls_overlaps(const WalkDev& W, const WalkRec& R, uint32_t nc, const double* __restrict__ npart,
@@ -1461,6 +1698,12 @@ int wfail(int code, const std::string& m) {
 }
 }  // namespace
 
+extern "C" int sq_set_walk_orbit_warps(int warps) {
+    if (warps != 8 && warps != 16) return wfail(SQ_ERR_ARG, "orbit-pass warps must be 8 or 16");
+    sqw::g_orbit_warps.store(warps);
+    return SQ_OK;
+}
+
 extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int precision,
                                  sq_qsa_walk_result* results, double* p0_trace, float* kernel_ms) {
     using namespace sqw;
@@ -1615,7 +1858,7 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
     }
     size_t prep_smem = 0, cls_smem = 0;
     int nslot = 1;
-    bool staged = false, sorted = false;
+    bool staged = false, sorted = false, sorted2 = false;
     bool tabled = false;
     uint32_t tab_entries = 0, tab_slots = 0;
     if (err == cudaSuccess && classes) {
@@ -1735,9 +1978,15 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
             if (err == cudaSuccess) err = cudaGetDevice(&cur_dev);  // the device the walks run on
             if (err == cudaSuccess)
                 err = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cur_dev);
-            sorted = precision == SQ_F32 && sorted_smem <= (size_t)optin;
-            staged = !sorted && precision == SQ_F32 && staged_smem <= (size_t)optin;
-            cls_smem = sorted ? sorted_smem : staged ? staged_smem : base_smem;
+            const size_t sorted2_smem =
+                sizeof(float) * ((size_t)nslot * 512 + (size_t)nslot * 16 + (size_t)kS2Warps * 2 * 16 +
+                                 (size_t)kS2Chunk * kS2Row) +
+                sizeof(unsigned long long) * (kHash + kMaxCls) +
+                sizeof(int) * ((size_t)(kS2Warps + 2) * 2 * nslot + kS2Warps + 2 * kS2Warps + 4) + kS2Chunk;
+            sorted2 = precision == SQ_F32 && g_orbit_warps.load() == 16 && sorted2_smem <= (size_t)optin;
+            sorted = !sorted2 && precision == SQ_F32 && sorted_smem <= (size_t)optin;
+            staged = !sorted2 && !sorted && precision == SQ_F32 && staged_smem <= (size_t)optin;
+            cls_smem = sorted2 ? sorted2_smem : sorted ? sorted_smem : staged ? staged_smem : base_smem;
             if (err == cudaSuccess && precision == SQ_F64) {
                 err = tabled ? cudaFuncSetAttribute(k_cls_table<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     (int)prep_smem)
@@ -1752,7 +2001,9 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
                              : cudaFuncSetAttribute(k_cls_prep<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     (int)prep_smem);
                 if (err == cudaSuccess)
-                    err = sorted   ? cudaFuncSetAttribute(k_walk_step_sorted, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                    err = sorted2  ? cudaFuncSetAttribute(k_walk_step_sorted2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                          (int)cls_smem)
+                          : sorted ? cudaFuncSetAttribute(k_walk_step_sorted, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                           (int)cls_smem)
                           : staged ? cudaFuncSetAttribute(k_walk_step_cls<float, true>,
                                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cls_smem)
@@ -1791,7 +2042,11 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
                     if (!tabled)
                         k_cls_prep<float><<<nwalks, kPrepThreads, prep_smem, st>>>(d_walks, d_recs, d_keys, d_ncls,
                                                                                    (float*)d_cls);
-                    if (sorted)
+                    if (sorted2)
+                        k_walk_step_sorted2<<<(unsigned)nct, kS2Threads, cls_smem, st>>>(
+                            d_walks, d_cta, d_recs, d_keys, d_ncls, (const float*)d_cls, d_gid, (float*)d_states,
+                            d_partial, nslot);
+                    else if (sorted)
                         k_walk_step_sorted<<<(unsigned)nct, kThreads, cls_smem, st>>>(
                             d_walks, d_cta, d_recs, d_keys, d_ncls, (const float*)d_cls, d_gid, (float*)d_states,
                             d_partial, nslot);

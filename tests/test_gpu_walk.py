@@ -170,14 +170,22 @@ def test_class_table_matches_per_step_preparation(precision):
 
 @pytest.mark.parametrize("precision,tol", [("f64", 1e-9), ("f32", 5e-5)])
 def test_orbit_class_algorithm_with_many_classes(precision, tol):
-    """5-spin rings with couplings +-1, +-2 have 76-78 classes per move: FP32
-    then takes the orbit pass that reads every class through its own lane
-    (the class-sorted pass holds at most 71 classes in shared memory)."""
+    """5-spin rings with couplings +-1, +-2 have 76-78 classes per move: the
+    16-warp class-sorted FP32 pass holds them (up to 85 classes in shared
+    memory); with the 8-warp setting (at most 71 classes) FP32 takes the orbit
+    pass that reads every class through its own lane.  Both against the oracle."""
+    from suqa_gb300 import _lib
     from suqa_gb300.walk import QsaWalk, run_qsa_walks
     rings = [[-2, 1, 1, -2, -2], [-1, -2, -1, -2, 2], [1, 1, -2, -1, -2], [2, -1, -2, -1, 1], [2, 2, -1, 2, -1]]
     walks = [QsaWalk(5, J, 0.5 + 0.3 * k, 3, 3, 1 + k, 700 + k, algo=1) for k, J in enumerate(rings)]
-    runs, _ = run_qsa_walks(walks, precision, trace=True)
-    _check(runs, walks, tol)
+    L = _lib.load()
+    try:
+        for warps in (16, 8):
+            assert L.sq_set_walk_orbit_warps(warps) == 0
+            runs, _ = run_qsa_walks(walks, precision, trace=True)
+            _check(runs, walks, tol)
+    finally:
+        L.sq_set_walk_orbit_warps(16)
 
 
 @pytest.mark.parametrize("precision,tol", [("f64", 1e-9), ("f32", 5e-5)])
@@ -204,3 +212,28 @@ def test_orbit_class_algorithm_refuses_rings_with_too_many_classes():
     w.algo = 0
     runs, _ = run_qsa_walks([w], "f64", trace=True)
     _check(runs, [w], 1e-10)
+
+
+def test_sixteen_and_eight_warp_orbit_passes_agree():
+    """The class-sorted FP32 orbit pass with 16 warps per CTA (CTA-level class
+    sums, end-of-range sums added in warp order) and with 8 warps (per-warp class
+    sums): the same walks (restarts, steps, read-outs) and probabilities to FP32
+    rounding; each against the oracle."""
+    from suqa_gb300 import _lib
+    from suqa_gb300.walk import ising_ring_walks, run_qsa_walks
+    L = _lib.load()
+    walks = ising_ring_walks(24, 10, 1.0, 3, 2, 6, seed=21, algo=1)
+    out = {}
+    try:
+        for warps in (8, 16):
+            assert L.sq_set_walk_orbit_warps(warps) == 0
+            out[warps], _ = run_qsa_walks(walks, "f32", trace=True)
+    finally:
+        L.sq_set_walk_orbit_warps(16)
+    same = 0
+    for a, b in zip(out[8], out[16]):
+        if (a.done, a.restarts, a.steps, a.readout) == (b.done, b.restarts, b.steps, b.readout):
+            same += 1
+            assert np.max(np.abs(a.p0 - b.p0)) < 2e-5
+    assert same >= 23
+    _check(out[16][:6], walks[:6], 5e-5)

@@ -131,20 +131,20 @@ size_t tile_smem(const sq_state* s, int K, int L) {
 // 64-register cap), single-tile passes of small states up to 1024.
 
 // Opts the pass kernel into the shared memory a tile needs (above the default 48 KiB).
-template <typename T, int MAXT>
+template <typename T, int MAXT, bool TC>
 int configure_smem(sq_state* s, size_t smem) {
     static std::atomic<int> configured_smem{-1};  // states may run in several host threads
     if ((int)smem > 48 * 1024 && configured_smem.load() < (int)smem) {
         int optin = 0;
         cudaFuncAttributes fa;
         SQ_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
-        SQ_CUDA(cudaFuncGetAttributes(&fa, sqk::k_pass<T, MAXT>));
+        SQ_CUDA(cudaFuncGetAttributes(&fa, sqk::k_pass<T, MAXT, TC>));
         const int dyn = optin - (int)fa.sharedSizeBytes;
         if ((int)smem > dyn) return fail(SQ_ERR_UNSUPPORTED, "tile does not fit in shared memory");
-        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T, MAXT, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
         // the whole unified L1 / shared array as shared memory: tiles are staged
         // explicitly, and several CTAs per SM hide each other's waits
-        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T, MAXT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T, MAXT, TC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         configured_smem = dyn;
     }
     return SQ_OK;
@@ -153,30 +153,30 @@ int configure_smem(sq_state* s, size_t smem) {
 // CTAs of the pass kernel resident per SM at this block and tile size (cached per
 // state): a pass launches one full wave, every CTA looping over an equal share of
 // the tiles, so no partial last wave leaves SMs idle.
-template <typename T, int MAXT>
+template <typename T, int MAXT, bool TC>
 int resident_ctas(sq_state* s, int block, size_t smem, int* out) {
     // kernels differ by element type: FP64 and double-float passes of one state share the cache
-    const uint64_t key = ((uint64_t)(std::is_same<T, sqk::df64>::value ? 1 : 0) << 63) | ((uint64_t)block << 32) |
-                         (uint64_t)smem;
+    const uint64_t key = ((uint64_t)(std::is_same<T, sqk::df64>::value ? 1 : 0) << 63) |
+                         ((uint64_t)(TC ? 1 : 0) << 62) | ((uint64_t)block << 32) | (uint64_t)smem;
     for (const auto& kv : s->occ_cache)
         if (kv.first == key) {
             *out = kv.second;
             return SQ_OK;
         }
-    int rc = configure_smem<T, MAXT>(s, smem);
+    int rc = configure_smem<T, MAXT, TC>(s, smem);
     if (rc) return rc;
     int occ = 0;
-    SQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sqk::k_pass<T, MAXT>, block, smem));
+    SQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sqk::k_pass<T, MAXT, TC>, block, smem));
     s->occ_cache.emplace_back(key, occ);
     *out = occ;
     return SQ_OK;
 }
 
-template <typename T, int MAXT>
+template <typename T, int MAXT, bool TC>
 int launch_pass_t(sq_state* s, const sqk::PassArgs& a, const sqk::Prog& p, int grid, int block, size_t smem) {
-    int rc = configure_smem<T, MAXT>(s, smem);
+    int rc = configure_smem<T, MAXT, TC>(s, smem);
     if (rc) return rc;
-    sqk::k_pass<T, MAXT><<<grid, block, smem, s->stream>>>(a, p);
+    sqk::k_pass<T, MAXT, TC><<<grid, block, smem, s->stream>>>(a, p);
     SQ_CUDA(cudaGetLastError());
     return SQ_OK;
 }
@@ -633,12 +633,19 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     }
     int occ = 0;
     const bool big = block > 256;
+    const bool tcp = dcount > 0 && dense_tc;  // the tensor-core instantiation (FP32)
     {
-        const int orc = use_df ? resident_ctas<sqk::df64, 256>(s, block, smem, &occ)
-                        : s->prec == SQ_F64 ? (big ? resident_ctas<double, 1024>(s, block, smem, &occ)
-                                                   : resident_ctas<double, 256>(s, block, smem, &occ))
-                                            : (big ? resident_ctas<float, 1024>(s, block, smem, &occ)
-                                                   : resident_ctas<float, 256>(s, block, smem, &occ));
+        int orc;
+        if (use_df) orc = resident_ctas<sqk::df64, 256, false>(s, block, smem, &occ);
+        else if (s->prec == SQ_F64)
+            orc = big ? resident_ctas<double, 1024, false>(s, block, smem, &occ)
+                      : resident_ctas<double, 256, false>(s, block, smem, &occ);
+        else if (tcp)
+            orc = big ? resident_ctas<float, 1024, true>(s, block, smem, &occ)
+                      : resident_ctas<float, 256, true>(s, block, smem, &occ);
+        else
+            orc = big ? resident_ctas<float, 1024, false>(s, block, smem, &occ)
+                      : resident_ctas<float, 256, false>(s, block, smem, &occ);
         if (orc) return orc;
     }
     const uint64_t wave = occ > 0 ? (uint64_t)s->nsm * (uint64_t)occ : (uint64_t)s->max_grid;
@@ -657,11 +664,17 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         }
         SQ_CUDA(cudaEventRecord(e0, s->stream));
     }
-    int rc = use_df ? launch_pass_t<sqk::df64, 256>(s, a, p, grid, block, smem)
-             : s->prec == SQ_F64 ? (big ? launch_pass_t<double, 1024>(s, a, p, grid, block, smem)
-                                        : launch_pass_t<double, 256>(s, a, p, grid, block, smem))
-                                 : (big ? launch_pass_t<float, 1024>(s, a, p, grid, block, smem)
-                                        : launch_pass_t<float, 256>(s, a, p, grid, block, smem));
+    int rc;
+    if (use_df) rc = launch_pass_t<sqk::df64, 256, false>(s, a, p, grid, block, smem);
+    else if (s->prec == SQ_F64)
+        rc = big ? launch_pass_t<double, 1024, false>(s, a, p, grid, block, smem)
+                 : launch_pass_t<double, 256, false>(s, a, p, grid, block, smem);
+    else if (tcp)
+        rc = big ? launch_pass_t<float, 1024, true>(s, a, p, grid, block, smem)
+                 : launch_pass_t<float, 256, true>(s, a, p, grid, block, smem);
+    else
+        rc = big ? launch_pass_t<float, 1024, false>(s, a, p, grid, block, smem)
+                 : launch_pass_t<float, 256, false>(s, a, p, grid, block, smem);
     if (rc) return rc;
     if (dcount) {
         SQ_CUDA(cudaEventRecord(s->dense_ev[dslot_i], s->stream));

@@ -307,7 +307,12 @@ namespace sqk {
 // T = double (FP64 state), float (FP32 state), or df64 (FP64 state, arithmetic in
 // double-float on the FP32 pipe; multi-tile passes only).  MAXT = 256 for
 // multi-tile passes (three CTAs per SM), 1024 for single-tile passes.
-template <typename T, int MAXT = 1024>
+//
+// TC: the instantiation that can run dense blocks on the tensor cores (FP32).  Only
+// passes holding such blocks use it: a kernel that contains tcgen05.alloc is given
+// one resident CTA per SM by the occupancy calculation, so every other pass runs an
+// instantiation without it (three CTAs per SM).
+template <typename T, int MAXT = 1024, bool TC = false>
 __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid_constant__ PassArgs a,
                                                                    const __grid_constant__ Prog p) {
     typedef typename VecT<T>::type V;
@@ -345,7 +350,7 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
     // dense ops: mbarriers, and on the tensor-core path a 64-column TMEM accumulator
     // held by warp 0 for the whole launch
     __shared__ __align__(16) DenseSmem dsm;
-    const bool dense_tc = p.ndense > 0 && a.dense_tc != 0 && sizeof(T) == 4;
+    const bool dense_tc = TC && sizeof(T) == 4 && p.ndense > 0 && a.dense_tc != 0;
     uint32_t ph_b = 0u, ph_mma = 0u;
     int b_loaded = -1;
     unsigned char* dbuf = smem_raw + a.dense_off;
@@ -361,9 +366,9 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
         if (bulk || dense_tc) asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (dense_tc && threadIdx.x < 32) tmem_alloc(&dsm.tmem, kDenseTmemCols);
-    tc_fence_before();
+    if (dense_tc) tc_fence_before();
     __syncthreads();
-    tc_fence_after();
+    if (dense_tc) tc_fence_after();
 
     T* gre = reinterpret_cast<T*>(a.re);
     T* gim = reinterpret_cast<T*>(a.im);
@@ -484,7 +489,7 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
                 bool ok = true;
                 if constexpr (kIsDf<T>) {
                     // not reached: the host runs passes with dense blocks in FP64
-                } else if constexpr (sizeof(T) == 4) {
+                } else if constexpr (TC && sizeof(T) == 4) {
                     if (dense_tc)
                         ok = dense_tc_apply(sre, TS, op, reinterpret_cast<const float*>(a.dense), dbuf, dsm, ph_b,
                                             ph_mma, b_loaded, a.err);
@@ -497,7 +502,7 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
                 }
                 if (!ok) {  // a bounded wait gave up: nothing in flight is left behind
                     if (bulk && threadIdx.x < 32) bulk_wait_all();
-                    if (threadIdx.x < 32) tmem_dealloc(dsm.tmem, kDenseTmemCols);
+                    if (dense_tc && threadIdx.x < 32) tmem_dealloc(dsm.tmem, kDenseTmemCols);
                     return;
                 }
             } else if (kind <= OP_PAULI && !(kind == OP_PAULI && op.lflip == 0u) || kind == OP_W) {

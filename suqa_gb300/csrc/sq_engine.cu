@@ -613,7 +613,10 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     if (red == 2) p.lrv ^= xm & p.lrm;
     p.defer = p.defer >= 2 ? 1 : 0;  // deferring one factor costs as much as it saves
     const bool single = (K == n);
-    const int block = single ? (K >= 10 ? 1024 : (K >= 8 ? 256 : 128)) : 256;
+    // multi-tile passes with tensor-core dense blocks run one CTA per SM (a kernel
+    // holding TMEM gets one), so they take 512 threads
+    const int block = single ? (K >= 10 ? 1024 : (K >= 8 ? 256 : 128))
+                             : ((ndense && s->prec == SQ_F32 && K >= 12 && s->dense_engine == 0) ? 512 : 256);
     // double-float arithmetic: FP64 multi-tile passes without tables or dense blocks
     bool use_df = s->prec == SQ_F64 && s->dfloat && !single && ndense == 0;
     for (size_t i = i0; i < i1 && use_df; ++i)
@@ -641,8 +644,8 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
             orc = big ? resident_ctas<double, 1024, false>(s, block, smem, &occ)
                       : resident_ctas<double, 256, false>(s, block, smem, &occ);
         else if (tcp)
-            orc = big ? resident_ctas<float, 1024, true>(s, block, smem, &occ)
-                      : resident_ctas<float, 256, true>(s, block, smem, &occ);
+            orc = single ? resident_ctas<float, 1024, true>(s, block, smem, &occ)
+                         : resident_ctas<float, 512, true>(s, block, smem, &occ);
         else
             orc = big ? resident_ctas<float, 1024, false>(s, block, smem, &occ)
                       : resident_ctas<float, 256, false>(s, block, smem, &occ);
@@ -670,8 +673,8 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         rc = big ? launch_pass_t<double, 1024, false>(s, a, p, grid, block, smem)
                  : launch_pass_t<double, 256, false>(s, a, p, grid, block, smem);
     else if (tcp)
-        rc = big ? launch_pass_t<float, 1024, true>(s, a, p, grid, block, smem)
-                 : launch_pass_t<float, 256, true>(s, a, p, grid, block, smem);
+        rc = single ? launch_pass_t<float, 1024, true>(s, a, p, grid, block, smem)
+                    : launch_pass_t<float, 512, true>(s, a, p, grid, block, smem);
     else
         rc = big ? launch_pass_t<float, 1024, false>(s, a, p, grid, block, smem)
                  : launch_pass_t<float, 256, false>(s, a, p, grid, block, smem);

@@ -311,7 +311,8 @@ namespace sqk {
 // TC: the instantiation that can run dense blocks on the tensor cores (FP32).  Only
 // passes holding such blocks use it: a kernel that contains tcgen05.alloc is given
 // one resident CTA per SM by the occupancy calculation, so every other pass runs an
-// instantiation without it (three CTAs per SM).
+// instantiation without it (three CTAs per SM), and the multi-tile tensor-core
+// passes run 512 threads (MAXT = 512) to keep twice the warps on the SM.
 template <typename T, int MAXT = 1024, bool TC = false>
 __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid_constant__ PassArgs a,
                                                                    const __grid_constant__ Prog p) {
@@ -326,7 +327,7 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
     const uint32_t lowmask = (1u << L) - 1u;
     // one tile buffer (re block then im block), or two when the next tile is
     // prefetched (staging mode 2); the run offsets follow the buffers
-    const int nbuf = (MAXT == 256 && a.stage == 2 && !kIsDf<T>) ? 2 : 1;
+    const int nbuf = (MAXT <= 512 && a.stage == 2 && !kIsDf<T>) ? 2 : 1;
     T* tiles = reinterpret_cast<T*>(smem_raw);
     T* sre = tiles;
     T* sim = sre + TS;
@@ -342,7 +343,7 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
     // (re and im) against an mbarrier, and writes tiles back the same way; the
     // host enables it only when a run is a multiple of 16 bytes
     // (single-tile passes, the 1024-thread instantiation, never stage in bulk)
-    const bool bulk = MAXT == 256 && a.stage != 0 && !kIsDf<T>;
+    const bool bulk = MAXT <= 512 && a.stage != 0 && !kIsDf<T>;
     const uint32_t run_bytes = (1u << L) * (uint32_t)sizeof(T);
     __shared__ __align__(8) uint64_t stage_bar[2];
     uint32_t stage_phase = 0u;  // bit b: parity of the next completion of stage_bar[b]

@@ -407,9 +407,31 @@ int ensure_dense_ring(sq_state* s) {
     return SQ_OK;
 }
 
+// Whether a pass over ops[i0, i1) of an FP64 state runs the double-float kernel:
+// the option is on, the pass is multi-tile (the tile size rule of run_pass) and
+// holds no table ops (W, phase lists) or dense blocks.
+bool pass_uses_df(const sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1) {
+    if (s->prec != SQ_F64 || !s->dfloat) return false;
+    const int n = (int)s->n;
+    uint64_t need = 0;
+    for (size_t i = i0; i < i1; ++i) {
+        const uint8_t k = ops[i].kind;
+        if (k == sqk::OP_DENSE || k == sqk::OP_W || k == sqk::OP_PLIST) return false;
+        need |= ops[i].flip;
+    }
+    int K = s->kp;
+    const int needbits = popc(need | 3ull);
+    if (n > small_max(s) && needbits > K) K = needbits;
+    if (s->staging == 2 && n > small_max(s)) K = std::max(needbits, 11);
+    if (K > n) K = n;
+    return K != n;
+}
+
 // Executes ops[i0, i1) as one pass, with an optional reduction at its end.
+// df_in / df_out: the state holds double-float pairs before / after the pass
+// (consecutive double-float passes of one flush, see flush()).
 int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, int red, uint64_t rmask,
-             uint64_t rval) {
+             uint64_t rval, int df_in = 0, int df_out = 0) {
     const int n = (int)s->n;
     uint64_t need = 0;
     int ndense = 0;
@@ -475,8 +497,9 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     };
 
     // outer qubits every op of the pass requires at one value: the grid skips the rest
+    // (not when the pass changes the storage format: every tile is converted)
     uint64_t fixm = 0, fixv = 0;
-    if (!red && i1 > i0) {
+    if (!red && i1 > i0 && df_in == df_out) {
         fixm = outer;
         for (size_t i = i0; i < i1; ++i) fixm &= ops[i].skm;
         for (size_t i = i0 + 1; i < i1; ++i) fixm &= ~(ops[i].skv ^ ops[i0].skv);
@@ -618,9 +641,11 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     const int block = single ? (K >= 10 ? 1024 : (K >= 8 ? 256 : 128))
                              : ((ndense && s->prec == SQ_F32 && K >= 12 && s->dense_engine == 0) ? 512 : 256);
     // double-float arithmetic: FP64 multi-tile passes without tables or dense blocks
-    bool use_df = s->prec == SQ_F64 && s->dfloat && !single && ndense == 0;
-    for (size_t i = i0; i < i1 && use_df; ++i)
-        if (ops[i].kind == sqk::OP_W || ops[i].kind == sqk::OP_PLIST) use_df = false;
+    const bool use_df = pass_uses_df(s, ops, i0, i1);
+    if (use_df && single) return fail(SQ_ERR_UNSUPPORTED, "internal: double-float pass on a single tile");
+    if ((df_in || df_out) && !use_df) return fail(SQ_ERR_UNSUPPORTED, "internal: double-float format on an FP64 pass");
+    a.df_in = df_in;
+    a.df_out = df_out;
     if (use_df) a.stage = 0;  // the tile is converted on its way in and out
     if (ndense && a.stage == 2) a.stage = 1;
     size_t smem = tile_smem(s, K, L) + (a.stage == 2 ? (size_t)2 * ((size_t)1 << K) * s->esz : 0);
@@ -734,6 +759,7 @@ int flush(sq_state* s, int red = 0, uint64_t rmask = 0, uint64_t rval = 0) {
         ops = fuse_dense(std::move(ops), s->dense_fusion);
     size_t i = 0;
     const int kcap = ((int)s->n <= small_max(s)) ? (int)s->n : std::max(s->kp, std::min(tile_cap(s), (int)s->n));
+    std::vector<std::pair<size_t, size_t>> ranges;
     while (i < ops.size()) {
         size_t j = i;
         uint64_t need = 0;
@@ -757,10 +783,20 @@ int flush(sq_state* s, int red = 0, uint64_t rmask = 0, uint64_t rval = 0) {
             if (h.kind == sqk::OP_DENSE) ++nd;
             ++j;
         }
-        const bool last = (j == ops.size());
-        int rc = run_pass(s, ops, i, j, last ? red : 0, rmask, rval);
-        if (rc) return rc;
+        ranges.emplace_back(i, j);
         i = j;
+    }
+    // Consecutive double-float passes hand the state on as hi/lo FP32 pairs (the
+    // same 8 bytes per component): only the first converts from doubles and only
+    // the last converts back, so between flushes the state is always IEEE doubles.
+    std::vector<char> df(ranges.size());
+    for (size_t r = 0; r < ranges.size(); ++r) df[r] = pass_uses_df(s, ops, ranges[r].first, ranges[r].second);
+    for (size_t r = 0; r < ranges.size(); ++r) {
+        const bool last = (r + 1 == ranges.size());
+        const int din = (r > 0 && df[r] && df[r - 1]) ? 1 : 0;
+        const int dout = (!last && df[r] && df[r + 1]) ? 1 : 0;
+        int rc = run_pass(s, ops, ranges[r].first, ranges[r].second, last ? red : 0, rmask, rval, din, dout);
+        if (rc) return rc;
     }
     if (ops.empty() && red) {
         int rc = run_pass(s, ops, 0, 0, red, rmask, rval);

@@ -99,6 +99,7 @@ struct PassArgs {
     const void* dense;     // OP_DENSE data of this launch (op.tab selects a 32 KiB block)
     int dense_tc;          // 1: dense ops on the tensor cores (FP32, tiles >= 2^12), 0: CUDA cores
     uint32_t dense_off;    // byte offset of the dense work area in dynamic shared memory
+    int df_in, df_out;     // double-float kernel: the state holds hi/lo FP32 pairs before / after the pass
 };
 
 // ---- bulk asynchronous copies (the TMA engine's cp.async.bulk) and mbarriers
@@ -388,7 +389,8 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
         return b;
     };
     auto tile_active = [&](uint64_t b) {
-        bool any = p.red != 0 || p.xm != 0u;  // a frame permutes every tile
+        // a frame permutes every tile; a pass that changes the storage format converts every tile
+        bool any = p.red != 0 || p.xm != 0u || a.df_in != a.df_out;
         for (int k = 0; k < p.nops && !any; ++k) any = (b & p.ops[k].ocm) == p.ops[k].ocv;
         return any;
     };
@@ -443,6 +445,11 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
             for (uint32_t v = threadIdx.x; v < TS / 2; v += blockDim.x) {
                 const uint32_t t = v * 2;
                 const uint64_t g = base | offs[t >> L] | (t & lowmask);
+                if (a.df_in) {  // already hi/lo pairs (an earlier pass of the same flush stored them)
+                    *reinterpret_cast<float4*>(sre + t) = __ldcs(reinterpret_cast<const float4*>(dre + g));
+                    *reinterpret_cast<float4*>(sim + t) = __ldcs(reinterpret_cast<const float4*>(dim + g));
+                    continue;
+                }
                 const double2 r2 = __ldcs(reinterpret_cast<const double2*>(dre + g));
                 const double2 i2 = __ldcs(reinterpret_cast<const double2*>(dim + g));
                 const df64 r0 = df_from_double(r2.x), r1 = df_from_double(r2.y);
@@ -712,8 +719,13 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
                     if (scaled) {
                         r0 = r0 * sg; r1 = r1 * sg; i0 = i0 * sg; i1 = i1 * sg;
                     }
-                    __stcs(reinterpret_cast<double2*>(dre + g), make_double2(df_to_double(r0), df_to_double(r1)));
-                    __stcs(reinterpret_cast<double2*>(dim + g), make_double2(df_to_double(i0), df_to_double(i1)));
+                    if (a.df_out) {  // the next pass of this flush reads the pairs as they are
+                        __stcs(reinterpret_cast<float4*>(dre + g), make_float4(r0.hi, r0.lo, r1.hi, r1.lo));
+                        __stcs(reinterpret_cast<float4*>(dim + g), make_float4(i0.hi, i0.lo, i1.hi, i1.lo));
+                    } else {
+                        __stcs(reinterpret_cast<double2*>(dre + g), make_double2(df_to_double(r0), df_to_double(r1)));
+                        __stcs(reinterpret_cast<double2*>(dim + g), make_double2(df_to_double(i0), df_to_double(i1)));
+                    }
                 }
             } else if (bulk && !scaled && (xm & lowmask) == 0u) {
                 // the frame only permutes whole runs: logical run h is physical run h ^ xh

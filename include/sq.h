@@ -123,9 +123,9 @@ int sq_apply_pauli_rotation(sq_state* s, uint32_t k, const uint32_t* qubits, con
  * qubits[0..k-1] (index bit b of U <-> qubits[b]), k in 1..5, on the elements
  * where every bit of gc is set (gc disjoint from the qubits).  U is applied as
  * given (no unitarity check).  FP32 states of 2^12 amplitudes or more run it on
- * the tensor cores (tcgen05, TF32 three-term split: ~2^-21 relative per
- * product), otherwise on the CUDA cores in FP64 arithmetic.  States need at
- * least 5 qubits. */
+ * the tensor cores (tcgen05, TF32 high/remainder split of both operands, four
+ * products: ~2^-24 relative per product), otherwise on the CUDA cores in FP64
+ * arithmetic.  States need at least 5 qubits. */
 int sq_apply_unitary(sq_state* s, uint32_t k, const uint32_t* qubits, const double* u_re, const double* u_im,
                      uint64_t gc);
 /* FP64 states: run the arithmetic of multi-tile passes (gates without tables or

@@ -26,7 +26,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                      "-I" + INCLUDE, "-I" + CSRC]
 
-LIB_SOURCES = ["sq_engine.cu", "sq_noalloc.cu", "sq_batch.cu", "sq_mlp.cu", "sq_evo.cu", "sq_walk.cu"] + [
+LIB_SOURCES = ["sq_engine.cu", "sq_pass_f64.cu", "sq_pass_f32.cu", "sq_pass_tc.cu", "sq_pass_df.cu", "sq_noalloc.cu",
+               "sq_batch.cu", "sq_mlp.cu", "sq_evo.cu", "sq_walk.cu"] + [
     "sq_batch_%s_m%d.cu" % (t, m) for t in ("f32", "f64") for m in (0, 1, 2)]
 
 

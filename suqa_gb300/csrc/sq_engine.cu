@@ -2,6 +2,7 @@
 // declared in include/sq.h.  Device work is the tile-pass kernel in sq_pass.cuh.
 #include "sq.h"
 #include "sq_pass.cuh"
+#include "sq_pass_host.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -127,58 +128,69 @@ size_t tile_smem(const sq_state* s, int K, int L) {
 }
 
 // The pass kernel for element type T (FP64, FP32, or double-float arithmetic on
-// an FP64 state) and CTA size bound MAXT: multi-tile passes run 256 threads (no
-// 64-register cap), single-tile passes of small states up to 1024.
+// an FP64 state), CTA size bound MAXT (multi-tile passes 256 threads, 512 with
+// tensor-core blocks; single-tile passes up to 1024) and optional parts F
+// (sq_pass.cuh, PassFeat), reached through the entry points of sq_pass_host.cuh.
 
 // Opts the pass kernel into the shared memory a tile needs (above the default 48 KiB).
-template <typename T, int MAXT, bool TC>
+template <class Tag>
 int configure_smem(sq_state* s, size_t smem) {
-    static std::atomic<int> configured_smem{-1};  // states may run in several host threads
-    if ((int)smem > 48 * 1024 && configured_smem.load() < (int)smem) {
-        int optin = 0;
-        cudaFuncAttributes fa;
-        SQ_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
-        SQ_CUDA(cudaFuncGetAttributes(&fa, sqk::k_pass<T, MAXT, TC>));
-        const int dyn = optin - (int)fa.sharedSizeBytes;
-        if ((int)smem > dyn) return fail(SQ_ERR_UNSUPPORTED, "tile does not fit in shared memory");
-        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T, MAXT, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-        // the whole unified L1 / shared array as shared memory: tiles are staged
-        // explicitly, and several CTAs per SM hide each other's waits
-        SQ_CUDA(cudaFuncSetAttribute(sqk::k_pass<T, MAXT, TC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-        configured_smem = dyn;
-    }
+    bool fits = true;
+    SQ_CUDA((sqk::pass_set_smem<typename Tag::T, Tag::MAXT, Tag::F>(s->device, smem, &fits)));
+    if (!fits) return fail(SQ_ERR_UNSUPPORTED, "tile does not fit in shared memory");
     return SQ_OK;
 }
 
 // CTAs of the pass kernel resident per SM at this block and tile size (cached per
 // state): a pass launches one full wave, every CTA looping over an equal share of
 // the tiles, so no partial last wave leaves SMs idle.
-template <typename T, int MAXT, bool TC>
+template <class Tag>
 int resident_ctas(sq_state* s, int block, size_t smem, int* out) {
-    // kernels differ by element type: FP64 and double-float passes of one state share the cache
-    const uint64_t key = ((uint64_t)(std::is_same<T, sqk::df64>::value ? 1 : 0) << 63) |
-                         ((uint64_t)(TC ? 1 : 0) << 62) | ((uint64_t)block << 32) | (uint64_t)smem;
+    // kernels differ by element type and parts: FP64 and double-float passes of one state share the cache
+    const uint64_t key = ((uint64_t)(std::is_same<typename Tag::T, sqk::df64>::value ? 1 : 0) << 63) |
+                         ((uint64_t)Tag::F << 56) | ((uint64_t)block << 32) | (uint64_t)smem;
     for (const auto& kv : s->occ_cache)
         if (kv.first == key) {
             *out = kv.second;
             return SQ_OK;
         }
-    int rc = configure_smem<T, MAXT, TC>(s, smem);
+    int rc = configure_smem<Tag>(s, smem);
     if (rc) return rc;
     int occ = 0;
-    SQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sqk::k_pass<T, MAXT, TC>, block, smem));
+    SQ_CUDA((sqk::pass_occupancy<typename Tag::T, Tag::MAXT, Tag::F>(block, smem, &occ)));
     s->occ_cache.emplace_back(key, occ);
     *out = occ;
     return SQ_OK;
 }
 
-template <typename T, int MAXT, bool TC>
+template <class Tag>
 int launch_pass_t(sq_state* s, const sqk::PassArgs& a, const sqk::Prog& p, int grid, int block, size_t smem) {
-    int rc = configure_smem<T, MAXT, TC>(s, smem);
+    int rc = configure_smem<Tag>(s, smem);
     if (rc) return rc;
-    sqk::k_pass<T, MAXT, TC><<<grid, block, smem, s->stream>>>(a, p);
-    SQ_CUDA(cudaGetLastError());
+    SQ_CUDA((sqk::pass_launch<typename Tag::T, Tag::MAXT, Tag::F>(a, p, grid, block, smem, s->stream)));
     return SQ_OK;
+}
+
+// Calls fn(KTag<T, MAXT, F>{}) with the leanest instantiation a pass needs:
+// double-float arithmetic, single tile (1024-thread bound), dense blocks (on the
+// tensor cores: FP32 only), bulk staging (multi-tile passes without dense blocks).
+template <class Fn>
+int with_pass_kernel(const sq_state* s, bool use_df, bool single, bool dense, bool tc, bool bulk, Fn&& fn) {
+    using sqk::KTag;
+    using sqk::PF_BULK;
+    using sqk::PF_DENSE;
+    using sqk::PF_TC;
+    if (use_df) return fn(KTag<sqk::df64, 256, 0>{});
+    if (s->prec == SQ_F64) {
+        if (single) return dense ? fn(KTag<double, 1024, PF_DENSE>{}) : fn(KTag<double, 1024, 0>{});
+        if (dense) return fn(KTag<double, 256, PF_DENSE>{});
+        return bulk ? fn(KTag<double, 256, PF_BULK>{}) : fn(KTag<double, 256, 0>{});
+    }
+    if (dense && tc)
+        return single ? fn(KTag<float, 1024, PF_DENSE | PF_TC>{}) : fn(KTag<float, 512, PF_DENSE | PF_TC>{});
+    if (single) return dense ? fn(KTag<float, 1024, PF_DENSE>{}) : fn(KTag<float, 1024, 0>{});
+    if (dense) return fn(KTag<float, 256, PF_DENSE>{});
+    return bulk ? fn(KTag<float, 256, PF_BULK>{}) : fn(KTag<float, 256, 0>{});
 }
 
 // ---- dense blocks ---------------------------------------------------------
@@ -647,7 +659,7 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     a.df_in = df_in;
     a.df_out = df_out;
     if (use_df) a.stage = 0;  // the tile is converted on its way in and out
-    if (ndense && a.stage == 2) a.stage = 1;
+    if (dcount) a.stage = 0;  // dense passes stage through registers (no bulk part in their kernels)
     size_t smem = tile_smem(s, K, L) + (a.stage == 2 ? (size_t)2 * ((size_t)1 << K) * s->esz : 0);
     if (dcount) {
         // the dense work area: tensor-core operands (A chunk + B), or the scratch tile
@@ -660,20 +672,11 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         a.dense = dev;
     }
     int occ = 0;
-    const bool big = block > 256;
-    const bool tcp = dcount > 0 && dense_tc;  // the tensor-core instantiation (FP32)
+    const bool bulk = a.stage != 0;
     {
-        int orc;
-        if (use_df) orc = resident_ctas<sqk::df64, 256, false>(s, block, smem, &occ);
-        else if (s->prec == SQ_F64)
-            orc = big ? resident_ctas<double, 1024, false>(s, block, smem, &occ)
-                      : resident_ctas<double, 256, false>(s, block, smem, &occ);
-        else if (tcp)
-            orc = single ? resident_ctas<float, 1024, true>(s, block, smem, &occ)
-                         : resident_ctas<float, 512, true>(s, block, smem, &occ);
-        else
-            orc = big ? resident_ctas<float, 1024, false>(s, block, smem, &occ)
-                      : resident_ctas<float, 256, false>(s, block, smem, &occ);
+        const int orc = with_pass_kernel(s, use_df, single, dcount > 0, dense_tc, bulk, [&](auto tag) {
+            return resident_ctas<decltype(tag)>(s, block, smem, &occ);
+        });
         if (orc) return orc;
     }
     const uint64_t wave = occ > 0 ? (uint64_t)s->nsm * (uint64_t)occ : (uint64_t)s->max_grid;
@@ -692,17 +695,9 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
         }
         SQ_CUDA(cudaEventRecord(e0, s->stream));
     }
-    int rc;
-    if (use_df) rc = launch_pass_t<sqk::df64, 256, false>(s, a, p, grid, block, smem);
-    else if (s->prec == SQ_F64)
-        rc = big ? launch_pass_t<double, 1024, false>(s, a, p, grid, block, smem)
-                 : launch_pass_t<double, 256, false>(s, a, p, grid, block, smem);
-    else if (tcp)
-        rc = single ? launch_pass_t<float, 1024, true>(s, a, p, grid, block, smem)
-                    : launch_pass_t<float, 512, true>(s, a, p, grid, block, smem);
-    else
-        rc = big ? launch_pass_t<float, 1024, false>(s, a, p, grid, block, smem)
-                 : launch_pass_t<float, 256, false>(s, a, p, grid, block, smem);
+    const int rc = with_pass_kernel(s, use_df, single, dcount > 0, dense_tc, bulk, [&](auto tag) {
+        return launch_pass_t<decltype(tag)>(s, a, p, grid, block, smem);
+    });
     if (rc) return rc;
     if (dcount) {
         SQ_CUDA(cudaEventRecord(s->dense_ev[dslot_i], s->stream));

@@ -40,6 +40,13 @@ enum OpKind : uint8_t {
     OP_DENSE = 9      // 32 x 32 complex matrix on the five tile bits of lflip (sq_dense.cuh)
 };
 
+// Optional parts of a pass-kernel instantiation (the template argument F of k_pass)
+enum PassFeat : int {
+    PF_BULK = 1,   // bulk asynchronous tile staging
+    PF_DENSE = 2,  // OP_DENSE blocks
+    PF_TC = 4      // OP_DENSE blocks on the tensor cores (with PF_DENSE)
+};
+
 // One gate in tile-local form (144 bytes).  For pair operations the pairs are
 // (t0, t0 ^ lflip) with t0 the tile index whose bit lpair is clear.  Control
 // conditions are split into the tile-local part (lcm, lcv: bits of the tile
@@ -309,14 +316,26 @@ namespace sqk {
 // double-float on the FP32 pipe; multi-tile passes only).  MAXT = 256 for
 // multi-tile passes (three CTAs per SM), 1024 for single-tile passes.
 //
-// TC: the instantiation that can run dense blocks on the tensor cores (FP32).  Only
-// passes holding such blocks use it: a kernel that contains tcgen05.alloc is given
-// one resident CTA per SM by the occupancy calculation, so every other pass runs an
-// instantiation without it (three CTAs per SM), and the multi-tile tensor-core
-// passes run 512 threads (MAXT = 512) to keep twice the warps on the SM.
-template <typename T, int MAXT = 1024, bool TC = false>
+// F: the optional parts compiled into this instantiation (PassFeat).  Each costs
+// registers and instructions on every pass that carries it, used or not (the
+// 28-qubit FP32 benchmark step ran 7 % slower with both in the one kernel), so
+// the host picks the leanest instantiation that a pass needs:
+//   PF_BULK   tiles staged by bulk asynchronous copies (multi-tile, not df64);
+//   PF_DENSE  OP_DENSE blocks (on the CUDA cores through a scratch tile);
+//   PF_TC     with PF_DENSE, FP32 blocks on the tensor cores.  A kernel that
+//             contains tcgen05.alloc is given one resident CTA per SM by the
+//             occupancy calculation, so only passes holding such blocks use it,
+//             and its multi-tile form runs 512 threads (MAXT = 512) to keep twice
+//             the warps on the SM.
+template <typename T, int MAXT = 1024, int F = 0>
 __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid_constant__ PassArgs a,
                                                                    const __grid_constant__ Prog p) {
+    static_assert(!(F & PF_BULK) || (MAXT <= 512 && !kIsDf<T>), "bulk staging: multi-tile, not double-float");
+    static_assert(!(F & PF_DENSE) || !kIsDf<T>, "double-float passes hold no dense blocks");
+    static_assert(!(F & PF_TC) || ((F & PF_DENSE) && sizeof(T) == 4), "tensor-core blocks: FP32 dense passes");
+    constexpr bool kBulk = (F & PF_BULK) != 0;
+    constexpr bool kDense = (F & PF_DENSE) != 0;
+    constexpr bool kTC = (F & PF_TC) != 0;
     typedef typename VecT<T>::type V;
     constexpr int W = VecT<T>::W;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -328,7 +347,7 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
     const uint32_t lowmask = (1u << L) - 1u;
     // one tile buffer (re block then im block), or two when the next tile is
     // prefetched (staging mode 2); the run offsets follow the buffers
-    const int nbuf = (MAXT <= 512 && a.stage == 2 && !kIsDf<T>) ? 2 : 1;
+    const int nbuf = (kBulk && a.stage == 2) ? 2 : 1;
     T* tiles = reinterpret_cast<T*>(smem_raw);
     T* sre = tiles;
     T* sim = sre + TS;
@@ -343,8 +362,8 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
     // bulk staging: warp 0 issues one asynchronous copy per run of 2^L elements
     // (re and im) against an mbarrier, and writes tiles back the same way; the
     // host enables it only when a run is a multiple of 16 bytes
-    // (single-tile passes, the 1024-thread instantiation, never stage in bulk)
-    const bool bulk = MAXT <= 512 && a.stage != 0 && !kIsDf<T>;
+    // (only instantiations with PF_BULK; never single-tile passes)
+    const bool bulk = kBulk && a.stage != 0;
     const uint32_t run_bytes = (1u << L) * (uint32_t)sizeof(T);
     __shared__ __align__(8) uint64_t stage_bar[2];
     uint32_t stage_phase = 0u;  // bit b: parity of the next completion of stage_bar[b]
@@ -352,7 +371,7 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
     // dense ops: mbarriers, and on the tensor-core path a 64-column TMEM accumulator
     // held by warp 0 for the whole launch
     __shared__ __align__(16) DenseSmem dsm;
-    const bool dense_tc = TC && sizeof(T) == 4 && p.ndense > 0 && a.dense_tc != 0;
+    const bool dense_tc = kTC && p.ndense > 0 && a.dense_tc != 0;
     uint32_t ph_b = 0u, ph_mma = 0u;
     int b_loaded = -1;
     unsigned char* dbuf = smem_raw + a.dense_off;
@@ -493,11 +512,11 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
             }
             const int kind = op.kind;
             const uint32_t lcm = op.lcm, lcv = op.lcv;
-            if (kind == OP_DENSE) {
+            if (kDense && kind == OP_DENSE) {
                 bool ok = true;
-                if constexpr (kIsDf<T>) {
-                    // not reached: the host runs passes with dense blocks in FP64
-                } else if constexpr (TC && sizeof(T) == 4) {
+                if constexpr (!kDense || kIsDf<T>) {
+                    // not reached: the host runs passes with dense blocks in an instantiation with PF_DENSE
+                } else if constexpr (kTC) {
                     if (dense_tc)
                         ok = dense_tc_apply(sre, TS, op, reinterpret_cast<const float*>(a.dense), dbuf, dsm, ph_b,
                                             ph_mma, b_loaded, a.err);

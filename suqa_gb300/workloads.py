@@ -107,6 +107,21 @@ def fp64_instructions(gates, n: int) -> int:
     return sum(cost.get(g[0], 0) for g in gates) * (1 << n)
 
 
+def single_kind_circuit(n: int, kind: str, ngates: int = 60, seed: int = 11):
+    """H on every qubit, then ngates gates of one kind of the benchmark's set
+    (drawn as random_circuit draws them, without measurements): the per-gate
+    instruction and time costs of the tile pass are read off such circuits."""
+    if kind not in KINDS:
+        raise ValueError(f"kind must be one of {KINDS}")
+    rng = np.random.default_rng(seed)
+    gates = [("h", q) for q in range(n)]
+    while len(gates) < n + ngates:
+        g = random_circuit(n, 1, seed=int(rng.integers(1 << 31)), measure_every=0)[0]
+        if g[0] == kind:
+            gates.append(g)
+    return gates
+
+
 def qft_blocks(n: int, pairs: int = 40, seed: int = 3):
     """QFT / inverse-QFT pairs on random 5-qubit registers (the dense-block
     workload): a list of registers, each applied as QFT then inverse QFT."""
@@ -120,11 +135,13 @@ def _main(argv=None):
 
         python -m suqa_gb300.workloads random --n 24 --gates 300 --precision f64 [--double-float]
         python -m suqa_gb300.workloads qft-blocks --n 24 --pairs 40 --precision f32 --dense-fusion 4
+        python -m suqa_gb300.workloads single --gate u1 --n 22 --gates 60 --precision f64 --repeat 1
     """
     import argparse
     from . import State
     ap = argparse.ArgumentParser(prog="python -m suqa_gb300.workloads")
-    ap.add_argument("kind", choices=["random", "qft-blocks"])
+    ap.add_argument("kind", choices=["random", "qft-blocks", "single"])
+    ap.add_argument("--gate", default="h", choices=list(KINDS))
     ap.add_argument("--n", type=int, default=24)
     ap.add_argument("--gates", type=int, default=300)
     ap.add_argument("--pairs", type=int, default=40)
@@ -145,6 +162,8 @@ def _main(argv=None):
         for _ in range(args.repeat):
             if args.kind == "random":
                 apply_circuit(st, random_circuit(args.n, args.gates, seed=7))
+            elif args.kind == "single":
+                apply_circuit(st, single_kind_circuit(args.n, args.gate, args.gates))
             else:
                 for r in qft_blocks(args.n, args.pairs):
                     st.apply_qft(r)

@@ -329,6 +329,13 @@ typedef struct sq_qsa_walk_result {
  * pass (per-warp class sums).  Process-wide; results agree to FP32 rounding (the
  * class sums are added in different orders).  No counterpart in the reference. */
 int sq_set_walk_orbit_warps(int warps);
+/* FP32 walks by orbit classes with the 16-warp pass: 1 (default) records where
+ * the per-chunk sort by class puts every orbit, the first time a part of a walk
+ * runs a move (2 bytes per orbit and move, when that table fits 8 GiB and a
+ * quarter of the free device memory), and later steps with that move take the
+ * places from the table instead of sorting; 0 sorts at every step.  Results are
+ * bit-identical.  Process-wide.  No counterpart in the reference. */
+int sq_set_walk_presort(int on);
 int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int precision, sq_qsa_walk_result* results,
                       double* p0_trace, float* kernel_ms);
 

@@ -72,6 +72,7 @@ struct WalkDev {
     uint32_t slot0;      // class-table temperature slot of stage 0 (algo 1)
     uint32_t jplane[5];  // bit planes of J_b + joff over the bonds b < s
     int joff, jnp;       // offset making every J_b + joff >= 0; planes in use
+    uint64_t ord_off;    // first entry of the walk's orbit order table (16-warp orbit pass)
 };
 
 struct WalkRec {
@@ -1281,18 +1282,108 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
 // may continue in the neighbouring warps, so their partial sums go to a per-warp
 // edge buffer that is added in warp order after the chunk (the sums stay
 // deterministic).  Rows of 16 floats (the in-place S needs the row's 16 slots).
+//
+// Orbit order table.  An orbit's class depends only on the ring's couplings and
+// the move, not on the state, so the chunk's counting sort puts every orbit at the
+// same place at every step with that move.  With a table (`order`: per walk, move
+// and orbit the 16-bit entry place | class << 9), the first step of a CTA with a
+// move sorts as usual and records the places; its flag in `ready` (per CTA and
+// move) then lets every later step with that move take the places from the table
+// and skip the class keys, the hash lookups and the sort with its two extra CTA
+// barriers per chunk.  Either way the places, and so the sums, are the same.
 // process-wide choice of the FP32 class-sorted orbit pass (sq_set_walk_orbit_warps)
 std::atomic<int> g_orbit_warps{16};
+// process-wide use of the orbit order table where it fits (sq_set_walk_presort)
+std::atomic<int> g_presort{1};
+constexpr uint64_t kOrderBudget = 8ull << 30;  // largest batch orbit order table (bytes)
 
 constexpr int kS2Threads = 512;
 constexpr int kS2Warps = kS2Threads / 32;
 constexpr int kS2Chunk = kS2Threads;
 constexpr int kS2Row = 16;
+constexpr int kS2Chunks = kClsOrbitsPerCta / kS2Chunk;
+
+// entries of a walk's order table: every move, every orbit slot of its CTAs
+__host__ __device__ inline uint64_t order_entries(int s, uint32_t ncta) {
+    return (uint64_t)s * ncta * (uint64_t)kClsOrbitsPerCta;
+}
+
+// dynamic shared memory of k_walk_step_sorted2 for nslot classes
+__host__ __device__ inline size_t sorted2_smem_bytes(int nslot) {
+    const size_t nk = 2 * (size_t)nslot;
+    return sizeof(float) * ((size_t)nslot * 512 + (size_t)nslot * 16 + (size_t)kS2Warps * 2 * 16 +
+                            (size_t)kS2Chunk * kS2Row) +
+           sizeof(unsigned long long) * (kHash + kMaxCls) + sizeof(int) * ((size_t)kS2Warps * nk + nk + kS2Warps +
+                                                                          2 * kS2Warps + 4) +
+           kS2Chunk;
+}
+
+// One orbit of the chunk: its 16 amplitudes and either its order entry (table) or
+// its class key (sort), issued before the products of the previous chunk.
+struct S2Load {
+    uint32_t b0, dp;
+    bool active, single;
+    uint16_t ord;
+    unsigned long long key;
+    float raw[16];
+};
+
+__device__ __forceinline__ void s2_issue(uint32_t o, uint32_t norb, int s, int C, uint32_t eC, const RingBonds& B,
+                                         bool have, const float* __restrict__ st, const uint16_t* __restrict__ ord,
+                                         S2Load& L) {
+    uint32_t x0 = 0, dp = 0;
+    L.active = o < norb;
+    L.single = true;
+    L.ord = 0xffff;
+    L.key = 0;
+    if (L.active) {
+        L.single = orbit_decode(o, s, C, dp, x0);
+        if (have) L.ord = ord[o];
+    }
+    L.b0 = (dp << s) | x0;
+    L.dp = dp;
+    if (!have) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {  // orbit_key's terms: dE at x = x0 ^ (j&1 ? e_C), d = dp ^ (j&2 ? e_C)
+            const uint32_t x = x0 ^ ((j & 1) ? eC : 0u);
+            const uint32_t d = dp ^ ((j & 2) ? eC : 0u);
+            L.key |= (unsigned long long)(ring_dE(x, d, B) + 256) << (9 * j);
+        }
+    }
+    const uint32_t mc = eC << s, macc = 1u << (2 * s);
+#pragma unroll
+    for (int pos = 0; pos < 8; ++pos) {
+        const int a = pos >> 2, b = (pos >> 1) & 1, c = pos & 1;
+        const uint32_t i0 = L.b0 ^ (a ? dp : 0u) ^ (b ? eC : 0u) ^ (c ? mc : 0u);
+#pragma unroll
+        for (int acc = 0; acc < 2; ++acc) L.raw[SLOT(a, b, c, acc)] = st[i0 ^ (acc ? macc : 0u)];
+    }
+}
+
+__device__ __forceinline__ void s2_finish(const S2Load& L, bool fresh, float scale, float init, float (&v)[16]) {
+#pragma unroll
+    for (int pos = 0; pos < 8; ++pos) {
+        const int a = pos >> 2, c = pos & 1;
+#pragma unroll
+        for (int acc = 0; acc < 2; ++acc) {
+            const int j = SLOT(a, (pos >> 1) & 1, c, acc);
+            float val;
+            if (fresh) val = (L.single && c == 0 && acc == 0) ? init : 0.f;
+            else val = (L.single && a == 1) ? 0.f : L.raw[j] * scale;
+            v[j] = val;
+        }
+    }
+    if (L.single) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[8 + j] = v[j];
+    }
+}
 
 __global__ void __launch_bounds__(kS2Threads, 1) k_walk_step_sorted2(
     const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk, const WalkRec* __restrict__ recs,
     const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ ncls, const float* __restrict__ cls,
-    const uint32_t* __restrict__ gid, float* __restrict__ states, double* __restrict__ npart, int nslot) {
+    const uint32_t* __restrict__ gid, uint16_t* __restrict__ order, unsigned char* __restrict__ ready,
+    float* __restrict__ states, double* __restrict__ npart, int nslot) {
     const int w = cta_walk[blockIdx.x];
     const WalkDev& W = walks[w];
     const WalkRec& R = recs[w];
@@ -1307,25 +1398,29 @@ __global__ void __launch_bounds__(kS2Threads, 1) k_walk_step_sorted2(
     unsigned long long* sent = htab + kHash;                          // [kMaxCls] class data entries
     int* wcnt = reinterpret_cast<int*>(sent + kMaxCls);               // [warps][nk]
     int* kstart = wcnt + kS2Warps * nk;                               // [nk]
-    int* kend = kstart + nk;                                          // [nk]
-    int* wsum = kend + nk;                                            // [warps]
+    int* wsum = kstart + nk;                                          // [warps]
     int* ecls = wsum + kS2Warps;                                      // [warps][2] class of each edge sum (-1: none)
-    int* nact_s = ecls + 2 * kS2Warps;
-    unsigned char* csort = reinterpret_cast<unsigned char*>(nact_s + 4);  // [kS2Chunk]
+    unsigned char* csort = reinterpret_cast<unsigned char*>(ecls + 2 * kS2Warps + 4);  // [kS2Chunk]
     const int s = W.s, C = (int)R.C;
     const uint32_t nc = ncls[(uint64_t)w * kMaxMoves + C];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // the order table's places for this CTA and move (uniform over the CTA)
+    uint16_t* ord = order ? order + W.ord_off + (uint64_t)C * W.ncta * kClsOrbitsPerCta : nullptr;
+    const bool have = ord != nullptr && ready[(uint64_t)blockIdx.x * kMaxMoves + C] != 0;
     for (int i = threadIdx.x; i < nslot * 16; i += kS2Threads) slots[i] = 0.f;
-    for (int i = threadIdx.x; i < kHash; i += kS2Threads) htab[i] = 0ull;
+    for (int i = threadIdx.x; i < kS2Chunk; i += kS2Threads) csort[i] = 0;  // every key read stays a class of the CTA
+    if (!have)
+        for (int i = threadIdx.x; i < kHash; i += kS2Threads) htab[i] = 0ull;
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < nc; i += kS2Threads) {
-        const unsigned long long key = keys[((uint64_t)w * kMaxMoves + C) * kMaxCls + i];
-        uint32_t h = cls_hash(key);
-        for (int probe = 0; probe < kHash; ++probe) {  // distinct keys, nc <= 96 < kHash: always placed
-            if (atomicCAS(&htab[h], 0ull, (key << 8) | (unsigned long long)i) == 0ull) break;
-            h = (h + 1u) & (kHash - 1);
+    if (!have)
+        for (uint32_t i = threadIdx.x; i < nc; i += kS2Threads) {
+            const unsigned long long key = keys[((uint64_t)w * kMaxMoves + C) * kMaxCls + i];
+            uint32_t h = cls_hash(key);
+            for (int probe = 0; probe < kHash; ++probe) {  // distinct keys, nc <= 96 < kHash: always placed
+                if (atomicCAS(&htab[h], 0ull, (key << 8) | (unsigned long long)i) == 0ull) break;
+                h = (h + 1u) & (kHash - 1);
+            }
         }
-    }
     for (uint32_t i = threadIdx.x; i < max(nc, 1u); i += kS2Threads) sent[i] = cls_entry(W, R, gid, w, i);
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < nc * 128u; i += kS2Threads) {
@@ -1347,67 +1442,86 @@ __global__ void __launch_bounds__(kS2Threads, 1) k_walk_step_sorted2(
     const float scale = (float)R.scale;
     const float init = (float)(1.0 / sqrt((double)(1u << s)));
     const uint32_t first = (blockIdx.x - W.cta0) * (uint32_t)kClsOrbitsPerCta;
-    constexpr int kChunks = kClsOrbitsPerCta / kS2Chunk;
     const int row = lane & 15, part = lane >> 4;
 
-    SortedLoad ld;
-    sorted_issue(first + threadIdx.x, norb, s, C, eC, bonds, st, ld);
-    for (int k = 0; k < kChunks; ++k) {
+    S2Load ld;
+    s2_issue(first + threadIdx.x, norb, s, C, eC, bonds, have, st, ord, ld);
+    for (int k = 0; k < kS2Chunks; ++k) {
         const uint32_t cbase = first + (uint32_t)(k * kS2Chunk);
         if (cbase >= norb) break;  // uniform over the CTA
         float vn[16];
-        const int ci = sorted_finish(ld, htab, fresh, scale, init, vn);
+        s2_finish(ld, fresh, scale, init, vn);
         const bool single = ld.single;
         const uint32_t b0 = ld.b0, dp = ld.dp;
-        const int q = ci >= 0 ? 2 * ci + (single ? 1 : 0) : -1;
-        for (int c = lane; c < nk; c += 32) wcnt[warp * nk + c] = 0;
-        __syncwarp();
-        const unsigned grp = __match_any_sync(0xffffffffu, q);
-        const int rank = __popc(grp & ((1u << lane) - 1u));
-        if (q >= 0 && rank == 0) wcnt[warp * nk + q] = __popc(grp);
-        __syncthreads();
-        int tot = 0;
-        if (kslot < nk) {
-            for (int wp = 0; wp < kS2Warps; ++wp) {
-                const int t = wcnt[wp * nk + kslot];
-                wcnt[wp * nk + kslot] = tot;
-                tot += t;
+        int pos = -1, q = -1;
+        if (have) {
+            // the recorded place; an orbit whose class was not found keeps the table's fill 0xffff
+            if (ld.active && (uint32_t)(ld.ord >> 9) < nc) {
+                pos = (int)(ld.ord & 511u);
+                q = 2 * (int)(ld.ord >> 9) + (single ? 1 : 0);
+            }
+        } else {
+            int ci = -1;
+            if (ld.active) {
+                const unsigned long long key = ld.key;
+                uint32_t h = cls_hash(key);
+                for (int probe = 0; probe < kHash; ++probe) {  // bounded; the table is at most 3/8 full
+                    const unsigned long long e = htab[h];
+                    if (e == 0ull) break;
+                    if ((e >> 8) == key) {
+                        ci = (int)(e & 255ull);
+                        break;
+                    }
+                    h = (h + 1u) & (kHash - 1);
+                }
+            }
+            q = ci >= 0 ? 2 * ci + (single ? 1 : 0) : -1;
+            // stable counting sort by q: place = orbits of smaller q + orbits of equal q
+            // in earlier warps + in earlier lanes of this warp
+            for (int c = lane; c < nk; c += 32) wcnt[warp * nk + c] = 0;
+            __syncwarp();
+            const unsigned grp = __match_any_sync(0xffffffffu, q);
+            const int rank = __popc(grp & ((1u << lane) - 1u));
+            if (q >= 0 && rank == 0) wcnt[warp * nk + q] = __popc(grp);
+            __syncthreads();
+            int tot = 0;
+            if (kslot < nk) {
+                for (int wp = 0; wp < kS2Warps; ++wp) {
+                    const int t = wcnt[wp * nk + kslot];
+                    wcnt[wp * nk + kslot] = tot;
+                    tot += t;
+                }
+            }
+            int incl = tot;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += y;
+            }
+            if (lane == 31) wsum[warp] = incl;
+            __syncthreads();
+            if (kslot < nk) {
+                int base = incl - tot;
+                for (int wp = 0; wp < warp; ++wp) base += wsum[wp];
+                kstart[kslot] = base;
+            }
+            __syncthreads();
+            if (q >= 0) {
+                pos = kstart[q] + wcnt[warp * nk + q] + rank;
+                if (ord) ord[cbase + threadIdx.x] = (uint16_t)(pos | (ci << 9));
             }
         }
-        int incl = tot;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, d);
-            if (lane >= d) incl += y;
-        }
-        if (lane == 31) wsum[warp] = incl;
-        __syncthreads();
-        if (kslot < nk) {
-            int base = incl - tot;
-            for (int wp = 0; wp < warp; ++wp) base += wsum[wp];
-            kstart[kslot] = base;
-            kend[kslot] = base + tot;
-        }
-        if (threadIdx.x == 0) {
-            int n = 0;
-            for (int wp = 0; wp < kS2Warps; ++wp) n += wsum[wp];
-            *nact_s = n;
-        }
-        __syncthreads();
-        int pos = -1;
-        if (q >= 0) {
-            pos = kstart[q] + wcnt[warp * nk + q] + rank;
+        if (pos >= 0) {
 #pragma unroll
             for (int u = 0; u < 4; ++u)
                 *reinterpret_cast<float4*>(vbuf + pos * kS2Row + 4 * u) =
                     make_float4(vn[4 * u], vn[4 * u + 1], vn[4 * u + 2], vn[4 * u + 3]);
             csort[pos] = (unsigned char)q;
         }
-        __syncthreads();
-        if (k + 1 < kChunks)  // the next chunk's loads overlap this chunk's products
-            sorted_issue(cbase + kS2Chunk + threadIdx.x, norb, s, C, eC, bonds, st, ld);
+        const int nact = __syncthreads_count(pos >= 0);  // the placed orbits fill places 0 .. nact-1
+        if (k + 1 < kS2Chunks)  // the next chunk's loads overlap this chunk's products
+            s2_issue(cbase + kS2Chunk + threadIdx.x, norb, s, C, eC, bonds, have, st, ord, ld);
         {
-            const int nact = *nact_s;
             const int p1 = nact * (warp + 1) / kS2Warps;
             int p = nact * warp / kS2Warps;
             // the classes at the two ends of this warp's range
@@ -1427,7 +1541,17 @@ __global__ void __launch_bounds__(kS2Threads, 1) k_walk_step_sorted2(
             };
             while (p < p1) {  // one run (one key) per iteration; uniform over the warp
                 const int qq = csort[p];
-                const int e = max(min(kend[qq], p1), p + 1);
+                // the run ends at the first place past p with another key (the keys ascend)
+                int e = p + 1;
+                for (;;) {
+                    const int idx = e + lane;
+                    const unsigned same = __ballot_sync(0xffffffffu, idx < p1 && csort[idx] == qq);
+                    if (same != 0xffffffffu) {
+                        e += __ffs(~same) - 1;
+                        break;
+                    }
+                    e += 32;
+                }
                 const float wt = (qq & 1) ? 0.5f : 1.f;
                 if ((qq >> 1) != cur) {
                     close_class(cur);
@@ -1484,7 +1608,7 @@ __global__ void __launch_bounds__(kS2Threads, 1) k_walk_step_sorted2(
                     if (c >= 0) slots[c * 16 + threadIdx.x] += edge[(wp * 2 + e2) * 16 + threadIdx.x];
                 }
         }
-        if (q >= 0) {
+        if (pos >= 0) {
             float S[16];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
@@ -1505,6 +1629,8 @@ __global__ void __launch_bounds__(kS2Threads, 1) k_walk_step_sorted2(
         }
         __syncthreads();  // S read back and edges added before the next chunk reuses the buffers
     }
+    // this CTA's places for the move are recorded: later steps take them from the table
+    if (ord && !have && threadIdx.x == 0) ready[(uint64_t)blockIdx.x * kMaxMoves + C] = 1;
     __syncthreads();
     for (uint32_t e = threadIdx.x; e < nc * 16u; e += blockDim.x) npart[(uint64_t)blockIdx.x * kMaxCls * 16 + e] = (double)slots[e];
 }
@@ -1704,6 +1830,12 @@ extern "C" int sq_set_walk_orbit_warps(int warps) {
     return SQ_OK;
 }
 
+extern "C" int sq_set_walk_presort(int on) {
+    if (on != 0 && on != 1) return wfail(SQ_ERR_ARG, "presort must be 0 or 1");
+    sqw::g_presort.store(on);
+    return SQ_OK;
+}
+
 extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int precision,
                                  sq_qsa_walk_result* results, double* p0_trace, float* kernel_ms) {
     using namespace sqw;
@@ -1722,7 +1854,7 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
     std::vector<WalkDev> wd(nwalks);
     std::vector<int> energies;
     std::vector<int> cta_walk;
-    uint64_t state_elems = 0, trace_len = 0;
+    uint64_t state_elems = 0, trace_len = 0, order_len = 0;
     uint32_t max_cap = 0;
     for (uint32_t i = 0; i < nwalks; ++i) {
         const sq_qsa_walk& a = walks[i];
@@ -1775,6 +1907,8 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
         const uint32_t ncta = (norbits(d.s) + orbits_per_cta - 1) / orbits_per_cta;
         d.cta0 = (uint32_t)cta_walk.size();
         d.ncta = ncta;
+        d.ord_off = order_len;
+        order_len += order_entries(d.s, ncta);
         for (uint32_t c = 0; c < ncta; ++c) cta_walk.push_back((int)i);
         state_elems += 2ull << (2 * a.spins);
         trace_len += d.cap;
@@ -1800,7 +1934,11 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
     unsigned long long* d_gkeys = nullptr;
     double* d_sbeta = nullptr;
     int* d_sq = nullptr;
+    uint16_t* d_order = nullptr;
+    unsigned char* d_ready = nullptr;
     auto cleanup = [&]() {
+        cudaFree(d_order);
+        cudaFree(d_ready);
         cudaFree(d_gid);
         cudaFree(d_gkeys);
         cudaFree(d_sbeta);
@@ -1978,15 +2116,27 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
             if (err == cudaSuccess) err = cudaGetDevice(&cur_dev);  // the device the walks run on
             if (err == cudaSuccess)
                 err = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cur_dev);
-            const size_t sorted2_smem =
-                sizeof(float) * ((size_t)nslot * 512 + (size_t)nslot * 16 + (size_t)kS2Warps * 2 * 16 +
-                                 (size_t)kS2Chunk * kS2Row) +
-                sizeof(unsigned long long) * (kHash + kMaxCls) +
-                sizeof(int) * ((size_t)(kS2Warps + 2) * 2 * nslot + kS2Warps + 2 * kS2Warps + 4) + kS2Chunk;
+            const size_t sorted2_smem = sorted2_smem_bytes(nslot);
             sorted2 = precision == SQ_F32 && g_orbit_warps.load() == 16 && sorted2_smem <= (size_t)optin;
             sorted = !sorted2 && precision == SQ_F32 && sorted_smem <= (size_t)optin;
             staged = !sorted2 && !sorted && precision == SQ_F32 && staged_smem <= (size_t)optin;
             cls_smem = sorted2 ? sorted2_smem : sorted ? sorted_smem : staged ? staged_smem : base_smem;
+            // the 16-warp pass records each CTA's orbit places per move where the batch's table fits
+            const uint64_t order_bytes = order_len * sizeof(uint16_t);
+            if (err == cudaSuccess && sorted2 && g_presort.load() == 1 &&
+                order_bytes <= std::min<uint64_t>(kOrderBudget, free_b / 4)) {
+                if (cudaMalloc(&d_order, order_bytes) == cudaSuccess &&
+                    cudaMalloc(&d_ready, nct * kMaxMoves) == cudaSuccess) {
+                    err = cudaMemsetAsync(d_order, 0xff, order_bytes, st);
+                    if (err == cudaSuccess) err = cudaMemsetAsync(d_ready, 0, nct * kMaxMoves, st);
+                } else {
+                    cudaGetLastError();  // no room: the 16-warp pass sorts every chunk at every step
+                    cudaFree(d_order);
+                    cudaFree(d_ready);
+                    d_order = nullptr;
+                    d_ready = nullptr;
+                }
+            }
             if (err == cudaSuccess && precision == SQ_F64) {
                 err = tabled ? cudaFuncSetAttribute(k_cls_table<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     (int)prep_smem)
@@ -2044,8 +2194,8 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
                                                                                    (float*)d_cls);
                     if (sorted2)
                         k_walk_step_sorted2<<<(unsigned)nct, kS2Threads, cls_smem, st>>>(
-                            d_walks, d_cta, d_recs, d_keys, d_ncls, (const float*)d_cls, d_gid, (float*)d_states,
-                            d_partial, nslot);
+                            d_walks, d_cta, d_recs, d_keys, d_ncls, (const float*)d_cls, d_gid, d_order, d_ready,
+                            (float*)d_states, d_partial, nslot);
                     else if (sorted)
                         k_walk_step_sorted<<<(unsigned)nct, kThreads, cls_smem, st>>>(
                             d_walks, d_cta, d_recs, d_keys, d_ncls, (const float*)d_cls, d_gid, (float*)d_states,

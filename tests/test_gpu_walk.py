@@ -214,6 +214,33 @@ def test_orbit_class_algorithm_refuses_rings_with_too_many_classes():
     _check(runs, [w], 1e-10)
 
 
+def test_presorted_orbit_pass_is_bit_identical_to_the_sorting_pass():
+    """The 16-warp orbit pass with the batch's orbit order table (orbits placed
+    by class from a table made once per batch) and without it (a counting sort
+    of every chunk at every step): the same places, hence the same sums in the
+    same order -- identical walks and identical p0 traces; each against the
+    oracle."""
+    from suqa_gb300 import _lib
+    from suqa_gb300.walk import ising_ring_walks, run_qsa_walks
+    L = _lib.load()
+    walks = ising_ring_walks(24, 10, 1.0, 3, 2, 6, seed=23, algo=1)
+    walks += ising_ring_walks(8, 7, 0.7, 2, 3, 4, seed=5, algo=1)
+    out = {}
+    try:
+        for on in (0, 1):
+            assert L.sq_set_walk_presort(on) == 0
+            out[on], _ = run_qsa_walks(walks, "f32", trace=True)
+    finally:
+        L.sq_set_walk_presort(1)
+    assert L.sq_set_walk_presort(2) != 0
+    for a, b in zip(out[0], out[1]):
+        assert (a.done, a.restarts, a.steps, a.readout, a.E, a.absM) == (b.done, b.restarts, b.steps, b.readout,
+                                                                         b.E, b.absM)
+        assert np.array_equal(a.p0, b.p0)
+    _check(out[1][:4], walks[:4], 5e-5)
+    _check(out[1][24:26], walks[24:26], 5e-5)
+
+
 def test_sixteen_and_eight_warp_orbit_passes_agree():
     """The class-sorted FP32 orbit pass with 16 warps per CTA (CTA-level class
     sums, end-of-range sums added in warp order) and with 8 warps (per-warp class

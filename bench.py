@@ -49,7 +49,9 @@ def parse():
     ap.add_argument("--skip-30", action="store_true", help="skip the 30-qubit FP64 repeat")
     ap.add_argument("--skip-qsa", action="store_true")
     ap.add_argument("--qsa-walks", type=int, default=1024)
-    ap.add_argument("--qsa-steps", type=int, default=8)
+    # walk steps per walk in the walk line: enough for the 16-warp orbit pass's order
+    # table to serve most steps, as it does over a full anneal
+    ap.add_argument("--qsa-steps", type=int, default=32)
     return ap.parse_args()
 
 

@@ -1281,7 +1281,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
 // it adds those classes' sums directly; the classes at the two ends of its range
 // may continue in the neighbouring warps, so their partial sums go to a per-warp
 // edge buffer that is added in warp order after the chunk (the sums stay
-// deterministic).  Rows of 16 floats (the in-place S needs the row's 16 slots).
+// deterministic).  Sorted rows of 20 floats (16 amplitudes, then S in place; the
+// padding spreads the scattered row stores of a quarter-warp over the banks).
 //
 // Orbit order table.  An orbit's class depends only on the ring's couplings and
 // the move, not on the state, so the chunk's counting sort puts every orbit at the
@@ -1300,7 +1301,7 @@ constexpr uint64_t kOrderBudget = 8ull << 30;  // largest batch orbit order tabl
 constexpr int kS2Threads = 512;
 constexpr int kS2Warps = kS2Threads / 32;
 constexpr int kS2Chunk = kS2Threads;
-constexpr int kS2Row = 16;
+constexpr int kS2Row = 20;  // floats per sorted row: 16 amplitudes, rows 5 bank groups apart
 constexpr int kS2Chunks = kClsOrbitsPerCta / kS2Chunk;
 
 // entries of a walk's order table: every move, every orbit slot of its CTAs
@@ -1393,7 +1394,7 @@ __global__ void __launch_bounds__(kS2Threads, 1) k_walk_step_sorted2(
     float* cls_s = reinterpret_cast<float*>(smem_raw);               // [nslot][512]: V^T rows, then Q rows
     float* slots = cls_s + nslot * 512;                               // [nslot][16] class sums of the CTA
     float* edge = slots + nslot * 16;                                 // [warps][2][16] end-of-range partial sums
-    float* vbuf = edge + kS2Warps * 2 * 16;                           // [kS2Chunk][16] amplitudes, then S
+    float* vbuf = edge + kS2Warps * 2 * 16;                           // [kS2Chunk][kS2Row] amplitudes, then S
     unsigned long long* htab = reinterpret_cast<unsigned long long*>(vbuf + kS2Chunk * kS2Row);  // [kHash]
     unsigned long long* sent = htab + kHash;                          // [kMaxCls] class data entries
     int* wcnt = reinterpret_cast<int*>(sent + kMaxCls);               // [warps][nk]
@@ -1423,9 +1424,12 @@ __global__ void __launch_bounds__(kS2Threads, 1) k_walk_step_sorted2(
         }
     for (uint32_t i = threadIdx.x; i < max(nc, 1u); i += kS2Threads) sent[i] = cls_entry(W, R, gid, w, i);
     __syncthreads();
+    // class rows with their 16-byte chunks swizzled by row (chunk u of row l at u ^ ((l >> 1) & 3)): the
+    // eight lanes of a quarter-warp loading eight consecutive rows then hit eight different bank groups
     for (uint32_t i = threadIdx.x; i < nc * 128u; i += kS2Threads) {
-        const uint32_t c = i >> 7, e = (i & 127u) * 4u;
-        *reinterpret_cast<float4*>(cls_s + c * 512 + e) = __ldg(reinterpret_cast<const float4*>(cls + sent[c] * kClsStride + e));
+        const uint32_t c = i >> 7, e = (i & 127u) * 4u, l = e >> 4, u = (e >> 2) & 3u;
+        *reinterpret_cast<float4*>(cls_s + c * 512 + l * 16 + 4 * (u ^ ((l >> 1) & 3u))) =
+            __ldg(reinterpret_cast<const float4*>(cls + sent[c] * kClsStride + e));
     }
     const uint32_t norb = norbits(s), eC = 1u << C;
     const uint32_t mc = eC << s, macc = 1u << (2 * s);
@@ -1560,7 +1564,7 @@ __global__ void __launch_bounds__(kS2Threads, 1) k_walk_step_sorted2(
                     const ulonglong2* rp = reinterpret_cast<const ulonglong2*>(cls_s + cur * 512 + lane * 16);
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
-                        const ulonglong2 t = rp[u];
+                        const ulonglong2 t = rp[u ^ ((lane >> 1) & 3)];
                         r[2 * u] = t.x;
                         r[2 * u + 1] = t.y;
                     }

@@ -336,6 +336,11 @@ int sq_set_walk_orbit_warps(int warps);
  * places from the table instead of sorting; 0 sorts at every step.  Results are
  * bit-identical.  Process-wide.  No counterpart in the reference. */
 int sq_set_walk_presort(int on);
+/* FP32 walks by orbit classes with the 16-warp pass: the 16 x 16 class products
+ * on the tensor cores (1, default: mma.sync m16n8k8 TF32 with the three-product
+ * split hi/lo of both operands, ~2^-22 relative per product) or on the CUDA cores
+ * in FP32 (0).  Process-wide.  No counterpart in the reference. */
+int sq_set_walk_mma(int on);
 int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int precision, sq_qsa_walk_result* results,
                       double* p0_trace, float* kernel_ms);
 

@@ -114,6 +114,7 @@ _SIGS = {
     "sq_kernel_time": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "sq_set_walk_orbit_warps": (C.c_int, [C.c_int]),
     "sq_set_walk_presort": (C.c_int, [C.c_int]),
+    "sq_set_walk_mma": (C.c_int, [C.c_int]),
     "sq_qms_tfim_batch": (C.c_int, [C.POINTER(SqTfimChain), C.c_uint32, C.c_int, C.POINTER(SqChainResult),
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_float)]),
     "sq_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(SqTfimChain), C.c_uint32, C.c_int,

@@ -1296,6 +1296,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_walk_step_sorted(const WalkDev*
 std::atomic<int> g_orbit_warps{16};
 // process-wide use of the orbit order table where it fits (sq_set_walk_presort)
 std::atomic<int> g_presort{1};
+// process-wide choice of the 16-warp pass's products: tensor cores (1) or CUDA cores (0) (sq_set_walk_mma)
+std::atomic<int> g_walk_mma{1};
 constexpr uint64_t kOrderBudget = 8ull << 30;  // largest batch orbit order table (bytes)
 
 constexpr int kS2Threads = 512;
@@ -1380,6 +1382,52 @@ __device__ __forceinline__ void s2_finish(const S2Load& L, bool fresh, float sca
     }
 }
 
+// ---- the products of a run on the tensor cores (mma.sync m16n8k8, TF32) ----
+// For a run of orbits of one class, [V^T; Q] (32 x 16) times the run's amplitude
+// rows (16 x 8 orbits per tile): the class rows are the A operand (two 16-row
+// tiles, two 8-column k-steps), eight orbits the B operand.  FP32 accuracy from
+// TF32 inputs by the three-product split x = hi + lo (hi = x rounded to TF32,
+// lo = x - hi, whose bits below TF32 the tensor cores drop): A_hi B_hi + A_hi B_lo
+// + A_lo B_hi, each product exact and summed in FP32; the dropped A_lo B_lo and
+// the truncation of lo are ~2^-22 of the product.  Fragment layout (PTX ISA,
+// m16n8k8 .tf32): g = lane / 4, t = lane % 4; A: a0 (g, t), a1 (g + 8, t),
+// a2 (g, t + 4), a3 (g + 8, t + 4); B: b0 (k = t, n = g), b1 (t + 4, g);
+// D: d0 (g, 2t), d1 (g, 2t + 1), d2 (g + 8, 2t), d3 (g + 8, 2t + 1).
+__device__ __forceinline__ uint32_t tf32_hi(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// The class's A fragments (hi and lo) for this lane from the staged class rows
+// (row l's 16-byte chunk u at u ^ ((l >> 1) & 3)): [m-tile][k-step][4].
+__device__ __forceinline__ void mma_class_frags(const float* crow, int lane, uint32_t (&ahi)[2][2][4],
+                                                uint32_t (&alo)[2][2][4]) {
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int l = 16 * mt + g + ((j & 1) ? 8 : 0);
+                const int chunk = 2 * ks + ((j & 2) ? 1 : 0);  // columns 8 ks + t (+ 4)
+                const float x = crow[l * 16 + 4 * (chunk ^ ((l >> 1) & 3)) + t];
+                const uint32_t h = tf32_hi(x);
+                ahi[mt][ks][j] = h;
+                alo[mt][ks][j] = __float_as_uint(x - __uint_as_float(h));
+            }
+}
+
+template <bool MMA>
 __global__ void __launch_bounds__(kS2Threads, 1) k_walk_step_sorted2(
     const WalkDev* __restrict__ walks, const int* __restrict__ cta_walk, const WalkRec* __restrict__ recs,
     const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ ncls, const float* __restrict__ cls,
@@ -1525,6 +1573,96 @@ __global__ void __launch_bounds__(kS2Threads, 1) k_walk_step_sorted2(
         const int nact = __syncthreads_count(pos >= 0);  // the placed orbits fill places 0 .. nact-1
         if (k + 1 < kS2Chunks)  // the next chunk's loads overlap this chunk's products
             s2_issue(cbase + kS2Chunk + threadIdx.x, norb, s, C, eC, bonds, have, st, ord, ld);
+        if constexpr (MMA) {
+            const int p1 = nact * (warp + 1) / kS2Warps;
+            int p = nact * warp / kS2Warps;
+            // the classes at the two ends of this warp's range
+            const int cfirst = p < p1 ? (int)(csort[p] >> 1) : -1;
+            const int clast = p < p1 ? (int)(csort[p1 - 1] >> 1) : -1;
+            if (lane < 2) ecls[warp * 2 + lane] = lane == 0 ? cfirst : (clast != cfirst ? clast : -1);
+            const int g = lane >> 2, t = lane & 3;
+            int cur = -1;
+            float nacc0 = 0.f, nacc1 = 0.f;  // class sums of rows g and g + 8 (this lane's columns)
+            uint32_t ahi[2][2][4], alo[2][2][4];
+            auto close_class = [&](int c) {
+                if (c < 0) return;
+                // rows g and g + 8: the four lanes of group g hold columns 2t, 2t + 1 of each tile
+                nacc0 += __shfl_xor_sync(0xffffffffu, nacc0, 1);
+                nacc1 += __shfl_xor_sync(0xffffffffu, nacc1, 1);
+                nacc0 += __shfl_xor_sync(0xffffffffu, nacc0, 2);
+                nacc1 += __shfl_xor_sync(0xffffffffu, nacc1, 2);
+                if (t != 0) return;
+                float* dst = c == cfirst ? edge + (warp * 2) * 16
+                             : c == clast ? edge + (warp * 2 + 1) * 16
+                                          : slots + c * 16;  // only this warp holds class c in this chunk
+                if (c == cfirst || c == clast) {
+                    dst[g] = nacc0;
+                    dst[g + 8] = nacc1;
+                } else {
+                    dst[g] += nacc0;
+                    dst[g + 8] += nacc1;
+                }
+            };
+            while (p < p1) {  // one run (one key) per iteration; uniform over the warp
+                const int qq = csort[p];
+                // the run ends at the first place past p with another key (the keys ascend)
+                int e = p + 1;
+                for (;;) {
+                    const int idx = e + lane;
+                    const unsigned same = __ballot_sync(0xffffffffu, idx < p1 && csort[idx] == qq);
+                    if (same != 0xffffffffu) {
+                        e += __ffs(~same) - 1;
+                        break;
+                    }
+                    e += 32;
+                }
+                const float wt = (qq & 1) ? 0.5f : 1.f;
+                if ((qq >> 1) != cur) {
+                    close_class(cur);
+                    nacc0 = 0.f;
+                    nacc1 = 0.f;
+                    cur = qq >> 1;
+                    mma_class_frags(cls_s + cur * 512, lane, ahi, alo);
+                }
+                for (; p < e; p += 8) {  // tiles of eight orbits; columns past the run are zero
+                    const bool in = p + g < e;
+                    const float* vr = vbuf + (p + g) * kS2Row + t;
+                    uint32_t bhi[4], blo[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {  // k = t + 4 j: b0, b1 of k-step 0, then of k-step 1
+                        const float x = in ? vr[4 * j] : 0.f;
+                        const uint32_t h = tf32_hi(x);
+                        bhi[j] = h;
+                        blo[j] = __float_as_uint(x - __uint_as_float(h));
+                    }
+                    float dy[4] = {0.f, 0.f, 0.f, 0.f}, ds[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                    for (int ks = 0; ks < 2; ++ks) {
+                        mma_tf32(dy, ahi[0][ks], bhi[2 * ks], bhi[2 * ks + 1]);
+                        mma_tf32(dy, ahi[0][ks], blo[2 * ks], blo[2 * ks + 1]);
+                        mma_tf32(dy, alo[0][ks], bhi[2 * ks], bhi[2 * ks + 1]);
+                        mma_tf32(ds, ahi[1][ks], bhi[2 * ks], bhi[2 * ks + 1]);
+                        mma_tf32(ds, ahi[1][ks], blo[2 * ks], blo[2 * ks + 1]);
+                        mma_tf32(ds, alo[1][ks], bhi[2 * ks], bhi[2 * ks + 1]);
+                    }
+                    nacc0 += wt * (dy[0] * dy[0] + dy[1] * dy[1]);
+                    nacc1 += wt * (dy[2] * dy[2] + dy[3] * dy[3]);
+                    __syncwarp();  // every lane has read these rows before S overwrites them
+                    // S of orbits 2t, 2t + 1 of the tile, rows g and g + 8
+                    if (p + 2 * t < e) {
+                        vbuf[(p + 2 * t) * kS2Row + g] = ds[0];
+                        vbuf[(p + 2 * t) * kS2Row + g + 8] = ds[2];
+                    }
+                    if (p + 2 * t + 1 < e) {
+                        vbuf[(p + 2 * t + 1) * kS2Row + g] = ds[1];
+                        vbuf[(p + 2 * t + 1) * kS2Row + g + 8] = ds[3];
+                    }
+                    __syncwarp();
+                }
+                p = e;
+            }
+            close_class(cur);
+        } else
         {
             const int p1 = nact * (warp + 1) / kS2Warps;
             int p = nact * warp / kS2Warps;
@@ -1834,6 +1972,12 @@ extern "C" int sq_set_walk_orbit_warps(int warps) {
     return SQ_OK;
 }
 
+extern "C" int sq_set_walk_mma(int on) {
+    if (on != 0 && on != 1) return wfail(SQ_ERR_ARG, "walk mma must be 0 or 1");
+    sqw::g_walk_mma.store(on);
+    return SQ_OK;
+}
+
 extern "C" int sq_set_walk_presort(int on) {
     if (on != 0 && on != 1) return wfail(SQ_ERR_ARG, "presort must be 0 or 1");
     sqw::g_presort.store(on);
@@ -2001,6 +2145,7 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
     size_t prep_smem = 0, cls_smem = 0;
     int nslot = 1;
     bool staged = false, sorted = false, sorted2 = false;
+    const bool use_mma = g_walk_mma.load() == 1;
     bool tabled = false;
     uint32_t tab_entries = 0, tab_slots = 0;
     if (err == cudaSuccess && classes) {
@@ -2155,8 +2300,12 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
                              : cudaFuncSetAttribute(k_cls_prep<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     (int)prep_smem);
                 if (err == cudaSuccess)
-                    err = sorted2  ? cudaFuncSetAttribute(k_walk_step_sorted2, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                          (int)cls_smem)
+                    err = sorted2  ? (use_mma ? cudaFuncSetAttribute(k_walk_step_sorted2<true>,
+                                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                                     (int)cls_smem)
+                                              : cudaFuncSetAttribute(k_walk_step_sorted2<false>,
+                                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                                     (int)cls_smem))
                           : sorted ? cudaFuncSetAttribute(k_walk_step_sorted, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                           (int)cls_smem)
                           : staged ? cudaFuncSetAttribute(k_walk_step_cls<float, true>,
@@ -2196,8 +2345,12 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
                     if (!tabled)
                         k_cls_prep<float><<<nwalks, kPrepThreads, prep_smem, st>>>(d_walks, d_recs, d_keys, d_ncls,
                                                                                    (float*)d_cls);
-                    if (sorted2)
-                        k_walk_step_sorted2<<<(unsigned)nct, kS2Threads, cls_smem, st>>>(
+                    if (sorted2 && use_mma)
+                        k_walk_step_sorted2<true><<<(unsigned)nct, kS2Threads, cls_smem, st>>>(
+                            d_walks, d_cta, d_recs, d_keys, d_ncls, (const float*)d_cls, d_gid, d_order, d_ready,
+                            (float*)d_states, d_partial, nslot);
+                    else if (sorted2)
+                        k_walk_step_sorted2<false><<<(unsigned)nct, kS2Threads, cls_smem, st>>>(
                             d_walks, d_cta, d_recs, d_keys, d_ncls, (const float*)d_cls, d_gid, d_order, d_ready,
                             (float*)d_states, d_partial, nslot);
                     else if (sorted)

@@ -241,6 +241,34 @@ def test_presorted_orbit_pass_is_bit_identical_to_the_sorting_pass():
     _check(out[1][24:26], walks[24:26], 5e-5)
 
 
+def test_tensor_and_cuda_core_orbit_products_agree():
+    """The 16-warp orbit pass with its class products on the tensor cores
+    (mma.sync TF32, three-product split) and on the CUDA cores (FP32): the same
+    walks (restarts, steps, read-outs) and probabilities to FP32 rounding; the
+    tensor-core walks against the oracle."""
+    from suqa_gb300 import _lib
+    from suqa_gb300.walk import ising_ring_walks, run_qsa_walks
+    L = _lib.load()
+    walks = ising_ring_walks(24, 10, 1.0, 3, 2, 6, seed=29, algo=1)
+    walks += ising_ring_walks(8, 6, 0.8, 2, 3, 5, seed=31, algo=1)
+    out = {}
+    try:
+        for on in (0, 1):
+            assert L.sq_set_walk_mma(on) == 0
+            out[on], _ = run_qsa_walks(walks, "f32", trace=True)
+    finally:
+        L.sq_set_walk_mma(1)
+    assert L.sq_set_walk_mma(3) != 0
+    same = 0
+    for a, b in zip(out[0], out[1]):
+        if (a.done, a.restarts, a.steps, a.readout) == (b.done, b.restarts, b.steps, b.readout):
+            same += 1
+            assert np.max(np.abs(a.p0 - b.p0)) < 2e-5
+    assert same >= len(walks) - 1
+    _check(out[1][:6], walks[:6], 5e-5)
+    _check(out[1][24:28], walks[24:28], 5e-5)
+
+
 def test_sixteen_and_eight_warp_orbit_passes_agree():
     """The class-sorted FP32 orbit pass with 16 warps per CTA (CTA-level class
     sums, end-of-range sums added in warp order) and with 8 warps (per-warp class

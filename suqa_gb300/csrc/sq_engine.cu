@@ -70,7 +70,8 @@ struct sq_state {
     double* d_partials = nullptr;
     double* d_result = nullptr;
     unsigned int* d_ticket = nullptr;
-    double* h_result = nullptr;     // pinned
+    double* h_result = nullptr;     // pinned (and mapped, where the device can map host memory)
+    double* h_result_dev = nullptr; // device address of h_result, or null: results come by copy
     int fusion = 1;
     // global scale: the state is gscale x the stored amplitudes.  Uncontrolled H
     // and Pauli rotations leave their common factor (1/sqrt 2, cos or sin of the
@@ -488,6 +489,7 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
     a.store = (i1 > i0) ? 1 : 0;
     a.partials = s->d_partials;
     a.result = s->d_result;
+    a.result_host = s->h_result_dev;
     a.ticket = s->d_ticket;
     a.err = reinterpret_cast<unsigned int*>(s->d_result + 3);
     // bulk staging for multi-tile passes whose runs are whole 16-byte units of at
@@ -740,7 +742,9 @@ int run_pass(sq_state* s, const std::vector<HostOp>& ops, size_t i0, size_t i1, 
 // h_result[3]): a bounded wait inside a pass that gave up.
 int device_error(sq_state* s) {
     unsigned int e = 0;
-    std::memcpy(&e, &s->h_result[3], sizeof(e));
+    const volatile double* h = s->h_result;
+    const double w = h[3];
+    std::memcpy(&e, &w, sizeof(e));
     if (e == 0u) return SQ_OK;
     return fail(SQ_ERR_CUDA, "a pass kernel gave up waiting for its tile copies (error word " + std::to_string(e) + ")");
 }
@@ -798,7 +802,9 @@ int flush(sq_state* s, int red = 0, uint64_t rmask = 0, uint64_t rval = 0) {
         if (rc) return rc;
     }
     if (red) {
-        SQ_CUDA(cudaMemcpyAsync(s->h_result, s->d_result, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        // the reduction's last CTA wrote the mapped copy; without a mapping, copy it
+        if (!s->h_result_dev)
+            SQ_CUDA(cudaMemcpyAsync(s->h_result, s->d_result, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
         SQ_CUDA(cudaStreamSynchronize(s->stream));
         int rc = device_error(s);
         if (rc) return rc;
@@ -881,10 +887,18 @@ int sq_state_create(sq_state** out, uint32_t n, int precision) {
         cudaMalloc(&s->d_partials, sizeof(double) * 2 * (size_t)s->max_grid) != cudaSuccess ||
         cudaMalloc(&s->d_result, sizeof(double) * 4) != cudaSuccess ||
         cudaMalloc(&s->d_ticket, sizeof(unsigned int)) != cudaSuccess ||
-        cudaMallocHost(&s->h_result, sizeof(double) * 4) != cudaSuccess) {
+        cudaHostAlloc(reinterpret_cast<void**>(&s->h_result), sizeof(double) * 4, cudaHostAllocMapped) != cudaSuccess) {
         cudaGetLastError();
         sq_state_destroy(s);
         return fail(SQ_ERR_NOMEM, "allocation of work buffers failed");
+    }
+    {
+        int can_map = 0;
+        void* dptr = nullptr;
+        if (cudaDeviceGetAttribute(&can_map, cudaDevAttrCanMapHostMemory, s->device) == cudaSuccess && can_map &&
+            cudaHostGetDevicePointer(&dptr, s->h_result, 0) == cudaSuccess)
+            s->h_result_dev = static_cast<double*>(dptr);
+        cudaGetLastError();  // without a mapping the results come back by copy
     }
     s->own_stream = true;
     cudaMemsetAsync(s->d_ticket, 0, sizeof(unsigned int), s->stream);

@@ -107,6 +107,11 @@ struct PassArgs {
     int dense_tc;          // 1: dense ops on the tensor cores (FP32, tiles >= 2^12), 0: CUDA cores
     uint32_t dense_off;    // byte offset of the dense work area in dynamic shared memory
     int df_in, df_out;     // double-float kernel: the state holds hi/lo FP32 pairs before / after the pass
+    // mapped page-locked host copy of result (4 doubles, or null): the last CTA of a
+    // reduction also writes (p0, p1) and the error word there, so the host reads them
+    // after a stream synchronisation without a copy that could queue on the copy
+    // engines behind other streams' bulk transfers
+    double* result_host;
 };
 
 // ---- bulk asynchronous copies (the TMA engine's cp.async.bulk) and mbarriers
@@ -830,6 +835,12 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_pass(const __grid
     if (threadIdx.x == 0) {
         a.result[0] = s0;
         a.result[1] = s1;
+        if (a.result_host) {
+            volatile double* h = a.result_host;
+            h[0] = s0;
+            h[1] = s1;
+            h[3] = __ldcg(a.result + 3);  // the error word of this pass and earlier ones
+        }
         *a.ticket = 0u;
     }
 }

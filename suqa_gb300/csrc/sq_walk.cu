@@ -1777,29 +1777,41 @@ __global__ void __launch_bounds__(kS2Threads, 1) k_walk_step_sorted2(
     for (uint32_t e = threadIdx.x; e < nc * 16u; e += blockDim.x) npart[(uint64_t)blockIdx.x * kMaxCls * 16 + e] = (double)slots[e];
 }
 
-// g_k of a walk from its class sums (algo 1): g_k = sum_{c,i} N_{c,i} d_{c,k,i}.
+// g_k of a walk from its class sums (algo 1): g_k = sum_{c,i} N_{c,i} d_{c,k,i}, with
+// N_{c,i} the class sums added over the walk's CTAs (first, into shared memory).  A
+// class's d block is [k][i] (16 i per k, at offset 512 of its class-data entry):
+// thread t takes k = t / 4 and i = 4 (t % 4) .. +3, so a warp reads eight k rows of
+// the block contiguously, and the four threads of a k are combined by shuffles
+// (a fixed order: the sums are deterministic).  kMeasThreads = 4 kMaxL threads.
+constexpr int kMeasThreads = 4 * kMaxL;
+
 template <typename T>
 __device__ void cls_overlaps(const WalkDev& W, const WalkRec& R, uint32_t nc, const double* __restrict__ npart,
                              const T* __restrict__ cls, const uint32_t* __restrict__ gid, int w, int L, double* g,
-                             double (*gl)[kMaxL + 1]) {
-    const int t = threadIdx.x;  // kMaxL threads
-    for (int k = 0; k < L; ++k) gl[t][k] = 0.0;
-    for (uint32_t e = t; e < nc * 16u; e += kMaxL) {
+                             double* Nsh) {
+    const int t = threadIdx.x;
+    for (uint32_t e = t; e < nc * 16u; e += kMeasThreads) {
         double Nv = 0.0;
         for (uint32_t c = 0; c < W.ncta; ++c) Nv += npart[(uint64_t)(W.cta0 + c) * kMaxCls * 16 + e];
-        const T* d = cls + cls_entry(W, R, gid, w, e / 16) * kClsStride + 512 + (e & 15);
-        for (int k = 0; k < L; ++k) gl[t][k] += Nv * (double)d[k * 16];
+        Nsh[e] = Nv;
     }
     __syncthreads();
-    if (t < L) {
-        double sum = 0.0;
-        for (int u = 0; u < kMaxL; ++u) sum += gl[u][t];
-        g[t] = sum;
+    const int k = t >> 2, q4 = t & 3;
+    double acc = 0.0;
+    if (k < L) {
+        for (uint32_t c = 0; c < nc; ++c) {
+            const T* d = cls + cls_entry(W, R, gid, w, c) * kClsStride + 512 + k * 16 + 4 * q4;
+            const double* Nc = Nsh + c * 16 + 4 * q4;
+            acc += Nc[0] * (double)d[0] + Nc[1] * (double)d[1] + Nc[2] * (double)d[2] + Nc[3] * (double)d[3];
+        }
     }
+    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+    if (k < L && q4 == 0) g[k] = acc;
 }
 
-// One CTA of kMaxL threads per walk.
-__global__ void k_walk_measure(const WalkDev* __restrict__ walks, WalkRec* __restrict__ recs,
+// One CTA of kMeasThreads threads per walk.
+__global__ void __launch_bounds__(kMeasThreads) k_walk_measure(const WalkDev* __restrict__ walks, WalkRec* __restrict__ recs,
                                const double* __restrict__ partial, const double* __restrict__ cos64,
                                double* __restrict__ trace, unsigned int* __restrict__ running, int algo,
                                const uint32_t* __restrict__ ncls, const void* __restrict__ cls,
@@ -1809,14 +1821,14 @@ __global__ void k_walk_measure(const WalkDev* __restrict__ walks, WalkRec* __res
     WalkRec& R = recs[w];
     if (R.status != 0) return;
     __shared__ double g[kMaxL], P[kMaxL];
-    __shared__ double gl[kMaxL][kMaxL + 1];
+    __shared__ double Nsh[kMaxCls * 16];
     __shared__ double n2;
     const int L = 1 << W.q;
     const int t = threadIdx.x;
     if (algo == 1) {
         const uint32_t nc = ncls[(uint64_t)w * kMaxMoves + R.C];
-        if (cls_f64) cls_overlaps<double>(W, R, nc, partial, (const double*)cls, gid, w, L, g, gl);
-        else cls_overlaps<float>(W, R, nc, partial, (const float*)cls, gid, w, L, g, gl);
+        if (cls_f64) cls_overlaps<double>(W, R, nc, partial, (const double*)cls, gid, w, L, g, Nsh);
+        else cls_overlaps<float>(W, R, nc, partial, (const float*)cls, gid, w, L, g, Nsh);
     } else if (t < L) {
         double sum = 0.0;
         for (uint32_t c = 0; c < W.ncta; ++c) sum += partial[(uint64_t)(W.cta0 + c) * kMaxL + t];
@@ -2375,7 +2387,7 @@ extern "C" int sq_qsa_walk_batch(const sq_qsa_walk* walks, uint32_t nwalks, int 
             }
             err = cudaGetLastError();
             if (err != cudaSuccess) break;
-            k_walk_measure<<<nwalks, kMaxL, 0, st>>>(d_walks, d_recs, d_partial, d_cos, d_trace, d_running,
+            k_walk_measure<<<nwalks, kMeasThreads, 0, st>>>(d_walks, d_recs, d_partial, d_cos, d_trace, d_running,
                                                      classes ? 1 : 0, d_ncls, d_cls, d_gid, precision == SQ_F64 ? 1 : 0);
             err = cudaGetLastError();
         }

@@ -95,3 +95,25 @@ def test_walk_batch_rejects_bad_arguments_before_any_device_call():
     w[0] = walk()
     assert L.sq_qsa_walk_batch(w, 0, _lib.SQ_F32, res, None, ctypes.byref(ms)) == _lib.SQ_ERR_ARG
     assert L.sq_qsa_walk_batch(w, 1, 7, res, None, ctypes.byref(ms)) == _lib.SQ_ERR_ARG
+
+
+def test_walk_pass_switches_validate_their_arguments():
+    """The process-wide switches of the FP32 orbit pass (warps per CTA, the orbit
+    order table, tensor-core products) accept their documented values and refuse
+    others on the host, with no device call."""
+    from suqa_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("libsq not built")
+    L = _lib.load()
+    try:
+        for fn, good, bad in ((L.sq_set_walk_orbit_warps, (8, 16), (0, 4, 32)),
+                              (L.sq_set_walk_presort, (0, 1), (-1, 2)),
+                              (L.sq_set_walk_mma, (0, 1), (-1, 2))):
+            for v in good:
+                assert fn(v) == _lib.SQ_OK, (fn, v)
+            for v in bad:
+                assert fn(v) == _lib.SQ_ERR_ARG, (fn, v)
+    finally:
+        L.sq_set_walk_orbit_warps(16)
+        L.sq_set_walk_presort(1)
+        L.sq_set_walk_mma(1)

@@ -30,8 +30,10 @@
 //                   restart on a nonzero value, the next move and temperature.
 // algo 1 and 2 work per orbit class instead (the section "Orbit classes" below):
 // k_cls_keys and k_cls_table once per batch (or k_cls_prep every step), then
-// k_walk_step_sorted (FP32) or k_walk_step_cls and k_walk_measure per step.
-// k_walk_readout reads the spins of every completed walk.
+// per step one orbit pass -- k_walk_step_sorted2 (FP32, 16 warps, orbit order
+// table, class products on the tensor cores), k_walk_step_sorted (FP32, 8
+// warps) or k_walk_step_cls (FP64, and batches with too many classes) -- and
+// k_walk_measure.  k_walk_readout reads the spins of every completed walk.
 #include <algorithm>
 #include <atomic>
 #include <cmath>

@@ -481,15 +481,24 @@ def main():
     # on the state's stream, so the end-to-end time can be attributed
     pipe_ev = [None] * pipe_steps
 
-    turn = {"next": 0}
+    # uploads also go in step order: the second state's first upload waits for the
+    # first state's, instead of sharing the host link with it and delaying the
+    # first circuit (later uploads fall inside the other state's circuit anyway)
+    turn = {"next": 0, "uploaded": 0}
     turn_cv = threading.Condition()
 
     def pipeline(stx, strm, ore, oim, steps):
         for i in steps:
             ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            with turn_cv:
+                turn_cv.wait_for(lambda: turn["uploaded"] >= i)
             ev[0].record(strm)
             stx.upload(h_re.data_ptr(), h_im.data_ptr())
             ev[1].record(strm)
+            ev[1].synchronize()
+            with turn_cv:
+                turn["uploaded"] = max(turn["uploaded"], i + 1)
+                turn_cv.notify_all()
             with turn_cv:  # step i's circuit runs after step i-1's has completed
                 turn_cv.wait_for(lambda: turn["next"] == i)
             pipe_bits[i] = apply_circuit(stx, gates)

@@ -140,6 +140,66 @@ def training_set(chains, runs, burn_in):
     return np.array(xs), np.array(ts), np.array(ms)
 
 
+def spin_bloch(psi, spins):
+    """Per-spin <X_i> and bond <Z_i Z_{i+1}> of a chain state (spins on the low
+    qubits, the energy and acceptance registers above them, traced out)."""
+    S = 1 << spins
+    amp = np.asarray(psi).reshape(-1, S)  # [higher registers][spin configuration]
+    pz = np.sum(np.abs(amp) ** 2, axis=0)
+    x = np.arange(S)
+    bits = (x[:, None] >> np.arange(spins)[None, :]) & 1
+    z = 1.0 - 2.0 * bits  # [config][spin]
+    zz = np.array([float(np.dot(pz, z[:, i] * z[:, (i + 1) % spins])) for i in range(spins)])
+    X = np.zeros(spins)
+    for i in range(spins):
+        low = x[(x >> i) & 1 == 0]
+        X[i] = 2.0 * float(np.real(np.sum(np.conj(amp[:, low]) * amp[:, low | (1 << i)])))
+    return X, zz
+
+
+def bloch_targets(points, ene_qbits, chains_per_point, burn, samples, every, precision="f32", seed=7):
+    """Warm-start targets from the plain chains' equilibrium states: for every
+    parameter point (spins, J, h, beta), cold chains run `burn` steps, then their
+    states are read `samples` times, `every` steps apart.  Each state's per-spin
+    Bloch data give the target angle of a product state RY(theta)|0>, whose Bloch
+    vector is (sin theta, 0, cos theta): theta_i = atan2(<X_i>, sqrt(<Z_i Z_{i+1}>)).
+    <Z_i> itself vanishes in the chains' states (they are parity eigenstates of the
+    ring), so the symmetry-broken magnitude sqrt(<Z_i Z_{i+1}>) stands for it; the
+    angle then reproduces the field term sin theta = <X> and the bond term
+    cos^2 theta = <ZZ> of the equilibrium state in their ratio.  Returns the
+    training rows (one per point, angles averaged over its chains and samples) and
+    a summary per point."""
+    from .batch import Batch, TfimChain
+    chains, owner = [], []
+    for pi, (sp, J, h, beta) in enumerate(points):
+        for k in range(chains_per_point):
+            chains.append(TfimChain(spins=sp, ene_qbits=ene_qbits, steps=burn + samples * every, beta=beta, h=h, J=J,
+                                    thermalization=0, seed=seed * 100_000 + 1000 * pi + k))
+            owner.append(pi)
+    b = Batch(chains, precision, segment_steps=0, use_graph=False)
+    acc = [[] for _ in points]
+    b.run(burn)
+    for _ in range(samples):
+        for ci, c in enumerate(chains):
+            X, zz = spin_bloch(b.state(ci), c.spins)
+            acc[owner[ci]].append(np.arctan2(X, np.sqrt(np.clip(zz, 0.0, None))))
+        b.run(every)
+    b.close()
+    xs, ts, ms, info = [], [], [], []
+    for pi, (sp, J, h, beta) in enumerate(points):
+        th = np.mean(np.array(acc[pi]), axis=0)
+        t = np.zeros(MAX_SPINS, np.float32)
+        m = np.zeros(MAX_SPINS, np.float32)
+        t[:sp] = th
+        m[:sp] = 1.0
+        xs.append(features(sp, J, h, beta))
+        ts.append(t)
+        ms.append(m)
+        info.append({"spins": sp, "J": J, "h": h, "beta": beta, "theta_mean": float(np.mean(th)),
+                     "samples": len(acc[pi])})
+    return np.array(xs), np.array(ts), np.array(ms), info
+
+
 def scan_targets(points, ene_qbits, thetas, warm_chains, warm_steps, cold_chains, cold_steps, precision="f32",
                  seed=7):
     """Warm-start targets from plain chains by an angle scan.  For every
@@ -211,7 +271,9 @@ def burn_in_experiment(spins=(4, 5, 6), ene_qbits=4, train_chains=512, train_ste
     ene_qbits energy qubits, the evaluation chains eval_ene_qbits (default: the
     same).  target = "scan": the angles come from scan_targets(**scan) (chains of
     the evaluation width started at a grid of angles), the angle whose plain
-    chains reach the cold chains' long-run energy first."""
+    chains reach the cold chains' long-run energy first.  target = "bloch": the
+    angles come from bloch_targets(**scan), the per-spin Bloch data of the plain
+    chains' states."""
     from .batch import TfimChain, run_tfim_batch
     ee = ene_qbits if eval_ene_qbits is None else eval_ene_qbits
     rng = np.random.default_rng(seed)
@@ -219,6 +281,11 @@ def burn_in_experiment(spins=(4, 5, 6), ene_qbits=4, train_chains=512, train_ste
         t0 = time.perf_counter()
         x, t, m, sinfo = scan_targets(precision=precision, seed=seed, **scan)
         data = {"target": "angle scan", "scan": sinfo, "scan_s": time.perf_counter() - t0,
+                "train_rows": int(x.shape[0]), "train_qubits": [scan["points"][0][0] + scan["ene_qbits"] + 1]}
+    elif target == "bloch":
+        t0 = time.perf_counter()
+        x, t, m, binfo = bloch_targets(precision=precision, seed=seed, **scan)
+        data = {"target": "equilibrium Bloch angles", "bloch": binfo, "bloch_s": time.perf_counter() - t0,
                 "train_rows": int(x.shape[0]), "train_qubits": [scan["points"][0][0] + scan["ene_qbits"] + 1]}
     else:
         chains = [TfimChain(spins=int(rng.choice(spins)), ene_qbits=ene_qbits, steps=train_steps,
@@ -331,6 +398,17 @@ SMALL_SCAN_STUDY = dict(ene_qbits=4, eval_groups=((6, 0.8, 0.9), (6, 1.2, 1.6)),
 # width (6 energy qubits, 19 qubits): 32 cold chains x 60 steps per point and 8
 # chains x 12 steps per grid angle; the evaluation groups are off the grid.
 SCAN_ANGLES = tuple(float(v) for v in np.linspace(-1.2, 0.0, 9))
+
+# Equilibrium Bloch-angle targets (bloch_targets): small (6-spin rings, 11 qubits)
+# and full size (12-spin rings at the evaluation width, 19 qubits).
+SMALL_BLOCH_STUDY = dict(ene_qbits=4, eval_groups=((6, 0.8, 0.9), (6, 1.2, 1.6)), eval_chains=64, eval_steps=30,
+                         iters=1500, target="bloch",
+                         scan=dict(points=[(6, 1.0, h, b) for h in (0.6, 1.0, 1.4) for b in (0.5, 1.2, 1.9)],
+                                   ene_qbits=4, chains_per_point=16, burn=10, samples=4, every=5))
+FULL_BLOCH_STUDY = dict(ene_qbits=6, eval_groups=((12, 0.8, 1.15), (12, 1.2, 1.65)), eval_chains=48,
+                        eval_steps=100, eval_ene_qbits=6, iters=2000, target="bloch",
+                        scan=dict(points=[(12, 1.0, h, b) for h in (0.6, 1.0, 1.4) for b in (0.4, 0.9, 1.4, 1.9)],
+                                  ene_qbits=6, chains_per_point=8, burn=30, samples=3, every=10))
 FULL_SCAN_STUDY = dict(ene_qbits=6, eval_groups=((12, 0.8, 1.15), (12, 1.2, 1.65)), eval_chains=48,
                        eval_steps=100, eval_ene_qbits=6, iters=2000, target="scan",
                        scan=dict(points=[(12, 1.0, h, b) for h in (0.6, 1.0, 1.4) for b in (0.4, 0.9, 1.4, 1.9)],
@@ -344,8 +422,12 @@ if __name__ == "__main__":
     ap = argparse.ArgumentParser(description="learned warm-start burn-in study")
     ap.add_argument("--full", action="store_true", help="the full-size study (several GPU minutes)")
     ap.add_argument("--scan", action="store_true", help="angle-scan targets (with --full: FULL_SCAN_STUDY)")
+    ap.add_argument("--bloch", action="store_true", help="equilibrium Bloch-angle targets (with --full: "
+                                                         "FULL_BLOCH_STUDY)")
     a = ap.parse_args()
-    if a.scan:
+    if a.bloch:
+        res = burn_in_experiment(**FULL_BLOCH_STUDY) if a.full else burn_in_experiment(**SMALL_BLOCH_STUDY)
+    elif a.scan:
         res = burn_in_experiment(**FULL_SCAN_STUDY) if a.full else burn_in_experiment(**SMALL_SCAN_STUDY)
     else:
         res = burn_in_experiment(**FULL_STUDY) if a.full else burn_in_experiment()

@@ -258,7 +258,8 @@ def scan_targets(points, ene_qbits, thetas, warm_chains, warm_steps, cold_chains
 
 def burn_in_experiment(spins=(4, 5, 6), ene_qbits=4, train_chains=512, train_steps=12, train_burn=6,
                        eval_groups=((6, 1.0, 0.3), (6, 1.0, 1.0), (6, 0.7, 1.8)), eval_chains=96, eval_steps=8,
-                       precision="f32", iters=1500, seed=7, eval_ene_qbits=None, target="energy", scan=None):
+                       precision="f32", iters=1500, seed=7, eval_ene_qbits=None, target="energy", scan=None,
+                       eval_seed=50_000):
     """Trains the network on plain chains and compares warm- and cold-started
     chains of held-out parameter sets.  Returns a dict with, per group, the
     equilibrium energy (cold chains after burn-in), the mean energy error of the
@@ -312,8 +313,8 @@ def burn_in_experiment(spins=(4, 5, 6), ene_qbits=4, train_chains=512, train_ste
         base = dict(spins=s, ene_qbits=ee, steps=eval_steps, beta=beta, h=h, thermalization=0)
         ang = net.angles(s, 1.0, h, beta)
         angs.append(ang)
-        allc += [TfimChain(seed=50_000 + 1000 * gi + k, **base) for k in range(eval_chains)]
-        allc += [TfimChain(seed=50_000 + 1000 * gi + k, warm_angles=ang, **base) for k in range(eval_chains)]
+        allc += [TfimChain(seed=eval_seed + 1000 * gi + k, **base) for k in range(eval_chains)]
+        allc += [TfimChain(seed=eval_seed + 1000 * gi + k, warm_angles=ang, **base) for k in range(eval_chains)]
     out["eval_qubits"] = allc[0].nqubits
     rall, ms_eval = run_tfim_batch(allc, precision)
     out["eval_device_ms"] = ms_eval
@@ -424,9 +425,11 @@ if __name__ == "__main__":
     ap.add_argument("--scan", action="store_true", help="angle-scan targets (with --full: FULL_SCAN_STUDY)")
     ap.add_argument("--bloch", action="store_true", help="equilibrium Bloch-angle targets (with --full: "
                                                          "FULL_BLOCH_STUDY)")
+    ap.add_argument("--eval-seed", type=int, default=50_000, help="first seed of the evaluation chains")
     a = ap.parse_args()
     if a.bloch:
-        res = burn_in_experiment(**FULL_BLOCH_STUDY) if a.full else burn_in_experiment(**SMALL_BLOCH_STUDY)
+        st = FULL_BLOCH_STUDY if a.full else SMALL_BLOCH_STUDY
+        res = burn_in_experiment(eval_seed=a.eval_seed, **st)
     elif a.scan:
         res = burn_in_experiment(**FULL_SCAN_STUDY) if a.full else burn_in_experiment(**SMALL_SCAN_STUDY)
     else:

@@ -41,3 +41,17 @@ def test_registers_are_traced_out():
     psi = (a + b) / np.sqrt(2)
     X, zz = spin_bloch(psi, s)
     assert np.allclose(X, 0.0) and np.allclose(zz, 1.0)
+
+
+def test_energy_target_angle_inverts_the_product_energy():
+    """angle_for_energy returns the product-state angle of an energy inside the
+    product states' range on [-pi/2, theta*], and clamps outside it."""
+    import math
+    from suqa_gb300.warmstart import angle_for_energy, product_energy
+    for spins, J, h in ((6, 1.0, 0.7), (12, 1.0, 1.4), (4, 1.0, 2.5)):
+        tmin = math.asin(min(1.0, h / (2.0 * J)))
+        for th in np.linspace(-math.pi / 2 + 1e-3, tmin - 1e-3, 7):
+            E = product_energy(th, spins, J, h)
+            assert abs(angle_for_energy(E, spins, J, h) - th) < 1e-9
+        assert angle_for_energy(1e9, spins, J, h) == -math.pi / 2
+        assert abs(angle_for_energy(-1e9, spins, J, h) - tmin) < 1e-12
